@@ -1,0 +1,165 @@
+"""ctypes binding of libecsgpu (include/ecsgpu.h) and libecshost (include/ecs_host.h).
+
+The libraries are built in-tree by :mod:`ecsprt_gb300.build`.  Loading never
+falls back to another implementation: if ``libecsgpu.so`` is missing or
+cannot be loaded, :func:`gpu` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_BUILD = Path(__file__).resolve().parent / "_build"
+GPU_LIB_PATH = _BUILD / "libecsgpu.so"
+HOST_LIB_PATH = _BUILD / "libecshost.so"
+
+ECS_OK = 0
+ECS_ERR_INVALID = -1
+ECS_ERR_NOMEM = -2
+ECS_ERR_NOT_CONVERGED = -3
+ECS_ERR_NONFINITE = -4
+ECS_ERR_TIMEOUT = -5
+ECS_ERR_CUDA = -6
+ECS_ERR_COLLISION = -7
+ECS_ERR_RANGE = -8
+ECS_ERR_STATE = -9
+ECS_ERR_UNSUPPORTED = -10
+
+ECS_PREC_FP64 = 0
+ECS_PREC_MIXED = 1
+
+BC_NAMES = ("periodic", "inject-reflect", "inject-advect")
+
+
+class EcsParams(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("Nx", C.c_int32), ("Ny", C.c_int32), ("Nz", C.c_int32),
+        ("bc", C.c_int32 * 3),
+        ("lhs_type", C.c_int32), ("rhs_type", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("x0", C.c_double), ("y0", C.c_double), ("z0", C.c_double),
+        ("x1", C.c_double), ("y1", C.c_double), ("z1", C.c_double),
+        ("Lx", C.c_double), ("Ly", C.c_double), ("Lz", C.c_double),
+        ("qi", C.c_double), ("mi", C.c_double), ("B0", C.c_double), ("E0", C.c_double), ("n0", C.c_double),
+        ("nui", C.c_double),
+        ("viT", C.c_double), ("viTx", C.c_double), ("viTy", C.c_double), ("viTz", C.c_double),
+        ("vi0x", C.c_double), ("vi0y", C.c_double), ("vi0z", C.c_double), ("vi0", C.c_double),
+        ("Ti", C.c_double),
+        ("qe", C.c_double), ("me", C.c_double), ("nue", C.c_double), ("Te", C.c_double),
+        ("veTx", C.c_double), ("veTy", C.c_double), ("veTz", C.c_double), ("veT", C.c_double),
+        ("ve0x", C.c_double), ("ve0y", C.c_double), ("ve0z", C.c_double), ("ve0", C.c_double),
+        ("Omega_e", C.c_double), ("kappa_e", C.c_double), ("Omega_i", C.c_double), ("kappa_i", C.c_double),
+        ("gammaT", C.c_double),
+        ("mn", C.c_double), ("Tn", C.c_double), ("vnT", C.c_double),
+        ("vn0x", C.c_double), ("vn0y", C.c_double), ("vn0z", C.c_double), ("vn0", C.c_double),
+        ("scale", C.c_double),
+        ("cth", C.c_double), ("cG", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if name == "bc" else v
+        return out
+
+
+class EcsSolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("relres", C.c_double), ("seconds", C.c_double)]
+
+
+class EcsStepStats(C.Structure):
+    _fields_ = [("collisions", C.c_int64), ("refused", C.c_int64), ("sorted", C.c_int32), ("solve", EcsSolveStats)]
+
+
+class EcsPicApp(C.Structure):
+    _fields_ = [("Nt", C.c_int32), ("dt", C.c_double), ("every", C.c_int32), ("Np", C.c_int64),
+                ("pdist", C.c_int32), ("vdist", C.c_int32), ("output_particles", C.c_int32)]
+
+
+class EcsSolverApp(C.Structure):
+    _fields_ = [("input", C.c_char * 4096), ("flux_scale", C.c_double * 3), ("view_lhs", C.c_int32)]
+
+
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+
+# (name, restype, argtypes): every symbol include/ecsgpu.h declares.
+GPU_API = [
+    ("ecs_version", C.c_char_p, []),
+    ("ecs_status_string", C.c_char_p, [C.c_int]),
+    ("ecs_last_error", C.c_char_p, [_vp]),
+    ("ecs_ctx_create", C.c_int, [C.POINTER(EcsParams), C.c_int, C.c_int64, _vp, C.POINTER(_vp)]),
+    ("ecs_ctx_destroy", C.c_int, [_vp]),
+    ("ecs_ctx_sync", C.c_int, [_vp]),
+    ("ecs_ctx_device_bytes", C.c_int64, [C.POINTER(EcsParams), C.c_int, C.c_int64]),
+    ("ecs_set_sort_every", C.c_int, [_vp, C.c_int]),
+    ("ecs_set_seed", C.c_int, [_vp, C.c_uint64]),
+    ("ecs_set_warm_start", C.c_int, [_vp, C.c_int]),
+    ("ecs_particles_upload", C.c_int, [_vp, _vp, _vp, C.c_int64]),
+    ("ecs_particles_download", C.c_int, [_vp, _vp, _vp]),
+    ("ecs_particles_count", C.c_int64, [_vp]),
+    ("ecs_phi_upload", C.c_int, [_vp, _vp]),
+    ("ecs_phi_download", C.c_int, [_vp, _vp]),
+    ("ecs_moments_upload", C.c_int, [_vp, _vp]),
+    ("ecs_moments_download", C.c_int, [_vp, _vp]),
+    ("ecs_rhs_download", C.c_int, [_vp, _vp]),
+    ("ecs_push", C.c_int, [_vp, C.c_double]),
+    ("ecs_collide", C.c_int, [_vp, C.c_double]),
+    ("ecs_move", C.c_int, [_vp, C.c_double]),
+    ("ecs_collect", C.c_int, [_vp]),
+    ("ecs_rhs", C.c_int, [_vp]),
+    ("ecs_lhs", C.c_int, [_vp]),
+    ("ecs_solve", C.c_int, [_vp, C.c_double, C.c_int, C.c_int, C.POINTER(EcsSolveStats)]),
+    ("ecs_lhs_apply_host", C.c_int, [_vp, _vp, _vp]),
+    ("ecs_step", C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.POINTER(EcsStepStats)]),
+    ("ecs_step_host", C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_double, C.c_int, _vp, _vp,
+                                C.POINTER(EcsStepStats)]),
+    ("ecs_launch_count", C.c_int64, [_vp]),
+]
+
+HOST_API = [
+    ("ecs_options_create", _vp, []),
+    ("ecs_options_destroy", None, [_vp]),
+    ("ecs_options_parse", C.c_int, [_vp, C.c_char_p]),
+    ("ecs_options_load_file", C.c_int, [_vp, C.c_char_p]),
+    ("ecs_options_get", C.c_char_p, [_vp, C.c_char_p, C.POINTER(C.c_int)]),
+    ("ecs_params_from_options", C.c_int, [_vp, C.POINTER(EcsParams), C.c_char_p, C.c_int]),
+    ("ecs_pic_app_from_options", C.c_int, [_vp, C.POINTER(EcsParams), C.POINTER(EcsPicApp), C.c_char_p, C.c_int]),
+    ("ecs_solver_app_from_options", C.c_int, [_vp, C.POINTER(EcsSolverApp)]),
+    ("ecs_echo_options", C.c_int, [C.c_char_p, _vp, C.POINTER(EcsParams)]),
+    ("ecs_write_petsc_vec", C.c_int, [C.c_char_p, _vp, C.c_int64]),
+    ("ecs_read_petsc_vec", C.c_int, [C.c_char_p, _vp, C.c_int64]),
+    ("ecs_write_fluid", C.c_int, [C.c_char_p, _vp, _vp, _vp, C.c_int64]),
+]
+
+_gpu = None
+_host = None
+
+
+def _bind(lib, table):
+    for name, res, args in table:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+def gpu():
+    """The loaded libecsgpu; raises if it has not been built."""
+    global _gpu
+    if _gpu is None:
+        if not GPU_LIB_PATH.exists():
+            raise RuntimeError(f"{GPU_LIB_PATH} is missing: run `python -m ecsprt_gb300.build` (nvcc, sm_103a)")
+        _gpu = _bind(C.CDLL(str(GPU_LIB_PATH)), GPU_API)
+    return _gpu
+
+
+def host():
+    """The loaded libecshost (options, parameters, output files)."""
+    global _host
+    if _host is None:
+        if not HOST_LIB_PATH.exists():
+            raise RuntimeError(f"{HOST_LIB_PATH} is missing: run `python -m ecsprt_gb300.build`")
+        _host = _bind(C.CDLL(str(HOST_LIB_PATH)), HOST_API)
+    return _host

@@ -1,0 +1,418 @@
+// C ABI of libecsgpu (declared in include/ecsgpu.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "ecs_internal.cuh"
+
+static thread_local std::string g_create_err;
+
+int ecs_fail(EcsCtx *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  else g_create_err = buf;
+  return code;
+}
+
+int ecs_cuda_check(EcsCtx *ctx, cudaError_t e, const char *what) {
+  return ecs_fail(ctx, e == cudaErrorMemoryAllocation ? ECS_ERR_NOMEM : ECS_ERR_CUDA, "%s: %s", what,
+                  cudaGetErrorString(e));
+}
+
+namespace {
+
+__global__ void k_moments_aos(size_t n, const double *__restrict__ mom, double *__restrict__ out) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < 4; d++) out[4 * c + d] = mom[(size_t)d * n + c];
+}
+__global__ void k_moments_soa(size_t n, const double *__restrict__ in, double *__restrict__ mom) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < 4; d++) mom[(size_t)d * n + c] = in[4 * c + d];
+}
+
+unsigned int blocks(const EcsCtx *ctx, size_t n) {
+  size_t want = (n + 255) / 256, cap = (size_t)ctx->nsm * 8;
+  return (unsigned int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+int validate(const EcsParams *p) {
+  if (!p) return ecs_fail(nullptr, ECS_ERR_INVALID, "params is NULL");
+  if (p->ndim != 3) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "ndim %d: the GPU path is 3-D", p->ndim);
+  if (p->Nx < 4 || p->Ny < 4 || p->Nz < 4 || p->Nx > 1024 || p->Ny > 1024 || p->Nz > 1024)
+    return ecs_fail(nullptr, ECS_ERR_INVALID, "grid %dx%dx%d outside 4..1024 per axis", p->Nx, p->Ny, p->Nz);
+  if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return ecs_fail(nullptr, ECS_ERR_INVALID, "non-positive cell width");
+  if (!(p->mi > 0)) return ecs_fail(nullptr, ECS_ERR_INVALID, "non-positive ion mass");
+  for (int d = 0; d < 3; d++) {
+    if (p->bc[d] == ECS_BC_INJECT_ADVECT) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "inject-advect boundaries are not implemented");
+    if (p->bc[d] == ECS_BC_INJECT_REFLECT && d != 2) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "reflecting boundaries are supported on z only");
+  }
+  if (p->lhs_type != ECS_LHS_FULL || p->rhs_type != ECS_RHS_FULL)
+    return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "only -lhs full and -rhs full run on the GPU path");
+  return ECS_OK;
+}
+
+int ensure_eext(EcsCtx *ctx, bool &ready) {
+  if (ready) return ECS_OK;
+  int rc = ecs_grid_eext(ctx);
+  if (rc) return rc;
+  ready = true;
+  return ECS_OK;
+}
+
+int read_status(EcsCtx *ctx) {
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned int f = ctx->hstat->flags;
+  if (f & ECS_FLAG_NONFINITE) return ecs_fail(ctx, ECS_ERR_NONFINITE, "non-finite particle velocity");
+  if (f & ECS_FLAG_RANGE) return ecs_fail(ctx, ECS_ERR_RANGE, "particle outside the domain or deposit range exceeded");
+  return ECS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ecs_version(void) { return "ecsprt-gb300 0.1.0 (sm_103a)"; }
+
+const char *ecs_status_string(int s) {
+  switch (s) {
+    case ECS_OK: return "ok";
+    case ECS_ERR_INVALID: return "invalid argument";
+    case ECS_ERR_NOMEM: return "out of memory";
+    case ECS_ERR_NOT_CONVERGED: return "solve did not converge";
+    case ECS_ERR_NONFINITE: return "non-finite value";
+    case ECS_ERR_TIMEOUT: return "device wait timed out";
+    case ECS_ERR_CUDA: return "CUDA error";
+    case ECS_ERR_COLLISION: return "too many refused collisions";
+    case ECS_ERR_RANGE: return "out of range";
+    case ECS_ERR_STATE: return "call out of order";
+    case ECS_ERR_UNSUPPORTED: return "unsupported option";
+    default: return "unknown status";
+  }
+}
+
+const char *ecs_last_error(const EcsCtx *ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
+  if (!p) return -1;
+  size_t n = (size_t)p->Nx * p->Ny * p->Nz;
+  size_t ne = (size_t)(p->Nx + 1) * (p->Ny + 1) * (p->Nz + 1);
+  int64_t m = 30;
+  int64_t b = 0;
+  b += n * 8 * (1 + 4 + 1) + n * 8 * 4;  // phi, mom, rhs, acc
+  b += n * 8 * 2 + (m + 2) * 1024 * 8;   // r64, w64, reductions
+  if (precision == ECS_PREC_FP64) {
+    b += cap * 48 + ne * 32;
+    b += (2 * m + 1) * n * 8 + (int64_t)(n * 8 * 10 * 8 / 7);  // Krylov + multigrid levels
+  } else {
+    b += cap * 56 + ne * 16 + n * 4 * 2 + n / 1024 * 4;
+    b += (2 * m + 3) * n * 4 + (int64_t)(n * 4 * 10 * 8 / 7);
+  }
+  return b;
+}
+
+int ecs_ctx_create(const EcsParams *params, int precision, int64_t np_capacity, void *stream, EcsCtx **out) {
+  if (!out) return ecs_fail(nullptr, ECS_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate(params);
+  if (rc) return rc;
+  if (precision != ECS_PREC_FP64 && precision != ECS_PREC_MIXED) return ecs_fail(nullptr, ECS_ERR_INVALID, "unknown precision %d", precision);
+  if (np_capacity < 0 || np_capacity > (int64_t)2147483647) return ecs_fail(nullptr, ECS_ERR_INVALID, "np_capacity out of range");
+  EcsCtx *ctx = new (std::nothrow) EcsCtx();
+  if (!ctx) return ecs_fail(nullptr, ECS_ERR_NOMEM, "host allocation failed");
+  ctx->p = *params;
+  ctx->prec = precision;
+  ctx->cap = np_capacity;
+  ctx->ncell = (size_t)params->Nx * params->Ny * params->Nz;
+  ctx->next = (size_t)(params->Nx + 1) * (params->Ny + 1) * (params->Nz + 1);
+  cudaError_t ce = cudaGetDevice(&ctx->device);
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (ce != cudaSuccess) {
+    ecs_fail(nullptr, ECS_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(ce));
+    delete ctx;
+    return ECS_ERR_CUDA;
+  }
+  if (stream) {
+    ctx->stream = (cudaStream_t)stream;
+  } else {
+    ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    ctx->own_stream = true;
+  }
+#define CREATE_ALLOC(ptr, bytes)                                                   \
+  do {                                                                            \
+    cudaError_t a_ = cudaMalloc((void **)&(ptr), (bytes));                        \
+    if (a_ != cudaSuccess) {                                                      \
+      ecs_fail(nullptr, ECS_ERR_NOMEM, "cudaMalloc %zu bytes: %s", (size_t)(bytes), \
+               cudaGetErrorString(a_));                                           \
+      ecs_ctx_destroy(ctx);                                                       \
+      return ECS_ERR_NOMEM;                                                       \
+    }                                                                             \
+  } while (0)
+  CREATE_ALLOC(ctx->phi, ctx->ncell * sizeof(double));
+  CREATE_ALLOC(ctx->acc, ctx->ncell * 4 * sizeof(long long));
+  CREATE_ALLOC(ctx->mom, ctx->ncell * 4 * sizeof(double));
+  CREATE_ALLOC(ctx->rhs, ctx->ncell * sizeof(double));
+  CREATE_ALLOC(ctx->dstat, sizeof(EcsDevStatus));
+  if (precision == ECS_PREC_FP64) CREATE_ALLOC(ctx->eext64, ctx->next * sizeof(double4_32a));
+  else CREATE_ALLOC(ctx->eext32, ctx->next * sizeof(float4));
+#undef CREATE_ALLOC
+  if (cudaMallocHost((void **)&ctx->hstat, sizeof(EcsDevStatus)) != cudaSuccess) {
+    ecs_fail(nullptr, ECS_ERR_NOMEM, "pinned allocation failed");
+    ecs_ctx_destroy(ctx);
+    return ECS_ERR_NOMEM;
+  }
+  cudaMemsetAsync(ctx->phi, 0, ctx->ncell * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->mom, 0, ctx->ncell * 4 * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream);
+  rc = ecs_particles_alloc(ctx);
+  if (rc) {
+    g_create_err = ctx->err;
+    ecs_ctx_destroy(ctx);
+    return rc;
+  }
+  ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) {
+    ecs_fail(nullptr, ECS_ERR_CUDA, "stream sync: %s", cudaGetErrorString(ce));
+    ecs_ctx_destroy(ctx);
+    return ECS_ERR_CUDA;
+  }
+  *out = ctx;
+  return ECS_OK;
+}
+
+int ecs_ctx_destroy(EcsCtx *ctx) {
+  if (!ctx) return ECS_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ecs_particles_free(ctx);
+  ecs_solver_free(ctx);
+  void *ptrs[] = {ctx->phi, ctx->acc, ctx->mom, ctx->rhs, ctx->dstat, ctx->eext64, ctx->eext32};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  if (ctx->hstat) cudaFreeHost(ctx->hstat);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return ECS_OK;
+}
+
+int ecs_ctx_sync(EcsCtx *ctx) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_set_sort_every(EcsCtx *ctx, int every) {
+  if (!ctx || every < 0) return ECS_ERR_INVALID;
+  ctx->sort_every = every;
+  return ECS_OK;
+}
+
+int ecs_set_seed(EcsCtx *ctx, uint64_t seed) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ctx->seed = seed;
+  return ECS_OK;
+}
+
+int ecs_set_warm_start(EcsCtx *ctx, int warm) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ctx->warm_start = warm ? 1 : 0;
+  return ECS_OK;
+}
+
+int ecs_particles_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np) {
+  if (!ctx || (np > 0 && (!pos || !vel))) return ECS_ERR_INVALID;
+  int rc = ecs_part_upload(ctx, pos, vel, np);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel) {
+  if (!ctx) return ECS_ERR_INVALID;
+  return ecs_part_download(ctx, pos, vel);
+}
+
+int64_t ecs_particles_count(const EcsCtx *ctx) { return ctx ? ctx->np : -1; }
+
+int ecs_phi_upload(EcsCtx *ctx, const double *phi) {
+  if (!ctx || !phi) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->phi, phi, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->eext_ready = false;
+  return ECS_OK;
+}
+
+int ecs_phi_download(EcsCtx *ctx, double *phi) {
+  if (!ctx || !phi) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaMemcpyAsync(phi, ctx->phi, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_moments_upload(EcsCtx *ctx, const double *m) {
+  if (!ctx || !m) return ECS_ERR_INVALID;
+  double *stage = nullptr;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, ctx->ncell * 4 * sizeof(double), ctx->stream));
+  ECS_CUDA(ctx, cudaMemcpyAsync(stage, m, ctx->ncell * 4 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  k_moments_soa<<<blocks(ctx, ctx->ncell), 256, 0, ctx->stream>>>(ctx->ncell, stage, ctx->mom);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->moments_ready = true;
+  ctx->lhs_ready = false;
+  return ECS_OK;
+}
+
+static int moments_to_host(EcsCtx *ctx, double *m) {
+  double *stage = nullptr;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, ctx->ncell * 4 * sizeof(double), ctx->stream));
+  k_moments_aos<<<blocks(ctx, ctx->ncell), 256, 0, ctx->stream>>>(ctx->ncell, ctx->mom, stage);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaMemcpyAsync(m, stage, ctx->ncell * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_moments_download(EcsCtx *ctx, double *m) {
+  if (!ctx || !m) return ECS_ERR_INVALID;
+  return moments_to_host(ctx, m);
+}
+
+int ecs_rhs_download(EcsCtx *ctx, double *b) {
+  if (!ctx || !b) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaMemcpyAsync(b, ctx->rhs, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_push(EcsCtx *ctx, double dt) {
+  if (!ctx) return ECS_ERR_INVALID;
+  int rc = ensure_eext(ctx, ctx->eext_ready);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  if ((rc = ecs_part_push(ctx, dt))) return rc;
+  return read_status(ctx);
+}
+
+int ecs_collide(EcsCtx *ctx, double dt) {
+  if (!ctx) return ECS_ERR_INVALID;
+  return ecs_part_collide(ctx, dt);
+}
+
+int ecs_move(EcsCtx *ctx, double dt) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  int rc = ecs_part_move(ctx, dt);
+  if (rc) return rc;
+  // DMSwarmMigrate analogue (src/boundaries.c:92): keep particles cell-sorted
+  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ++ctx->steps_since_sort >= ctx->sort_every)
+    if ((rc = ecs_part_sort(ctx))) return rc;
+  return read_status(ctx);
+}
+
+int ecs_collect(EcsCtx *ctx) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  int rc = ecs_part_collect(ctx);
+  if (rc) return rc;
+  if ((rc = ecs_grid_moments(ctx))) return rc;
+  ctx->lhs_ready = false;
+  return read_status(ctx);
+}
+
+int ecs_rhs(EcsCtx *ctx) {
+  if (!ctx) return ECS_ERR_INVALID;
+  if (!ctx->moments_ready) return ecs_fail(ctx, ECS_ERR_STATE, "rhs called before collect");
+  int rc = ecs_grid_rhs(ctx);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_lhs(EcsCtx *ctx) {
+  if (!ctx) return ECS_ERR_INVALID;
+  if (!ctx->moments_ready) return ecs_fail(ctx, ECS_ERR_STATE, "lhs called before collect");
+  int rc = ecs_solver_setup(ctx);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_solve(EcsCtx *ctx, double rtol, int max_it, int warm_start, EcsSolveStats *stats) {
+  if (!ctx || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
+  int rc = ecs_solver_run(ctx, rtol, max_it, warm_start, stats);
+  ctx->eext_ready = false;
+  return rc;
+}
+
+int ecs_lhs_apply_host(EcsCtx *ctx, const double *x, double *y) {
+  if (!ctx || !x || !y) return ECS_ERR_INVALID;
+  if (!ctx->moments_ready) return ecs_fail(ctx, ECS_ERR_STATE, "lhs apply before moments");
+  double *dx = nullptr, *dy = nullptr;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&dx, ctx->ncell * sizeof(double), ctx->stream));
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&dy, ctx->ncell * sizeof(double), ctx->stream));
+  ECS_CUDA(ctx, cudaMemcpyAsync(dx, x, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  int rc = ecs_operator_apply64(ctx, dx, dy);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaMemcpyAsync(y, dy, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaFreeAsync(dx, ctx->stream));
+  ECS_CUDA(ctx, cudaFreeAsync(dy, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stats) {
+  if (!ctx || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
+  int rc = ensure_eext(ctx, ctx->eext_ready);
+  if (rc) return rc;
+  int sorted = 0;
+  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ctx->steps_since_sort >= ctx->sort_every) {
+    if ((rc = ecs_part_sort(ctx))) return rc;
+    sorted = 1;
+  }
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  if ((rc = ecs_part_fused(ctx, dt, 1))) return rc;
+  EcsDevStatus coll = *ctx->hstat;
+  if (ctx->p.mn <= 0.0) memset(&coll, 0, sizeof coll);
+  ctx->steps_since_sort++;
+  if ((rc = ecs_grid_moments(ctx))) return rc;
+  if ((rc = read_status(ctx))) return rc;
+  if ((rc = ecs_grid_rhs(ctx))) return rc;
+  if ((rc = ecs_solver_setup(ctx))) return rc;
+  EcsSolveStats st;
+  memset(&st, 0, sizeof st);
+  rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, &st);
+  ctx->eext_ready = false;
+  if (stats) {
+    stats->collisions = (int64_t)coll.collisions;
+    stats->refused = (int64_t)coll.refused;
+    stats->sorted = sorted;
+    stats->solve = st;
+  }
+  return rc;
+}
+
+int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, double rtol, int max_it,
+                  double *moments_out, double *phi_out, EcsStepStats *stats) {
+  if (!ctx || !pos || !vel) return ECS_ERR_INVALID;
+  int rc = ecs_part_upload(ctx, pos, vel, np);
+  if (rc) return rc;
+  if ((rc = ecs_step(ctx, dt, rtol, max_it, stats))) return rc;
+  if ((rc = ecs_part_download(ctx, pos, vel))) return rc;
+  if (moments_out && (rc = moments_to_host(ctx, moments_out))) return rc;
+  if (phi_out) {
+    ECS_CUDA(ctx, cudaMemcpyAsync(phi_out, ctx->phi, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return ECS_OK;
+}
+
+int64_t ecs_launch_count(const EcsCtx *ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

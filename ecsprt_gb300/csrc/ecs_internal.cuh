@@ -1,0 +1,199 @@
+// Internal declarations shared by the libecsgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ecsgpu.h"
+
+#define ECS_FULL_MASK 0xffffffffu
+
+// Fixed-point scales of the deposit accumulators: contributions are rounded
+// to integer multiples of 2^-S and summed exactly in int64, which makes the
+// moments independent of the order in which particles are processed.
+#define ECS_FIX_SHIFT_FP64 44
+#define ECS_FIX_SHIFT_MIXED 40
+
+// Device status word bits (EcsDevStatus::flags).
+#define ECS_FLAG_NONFINITE 1u
+#define ECS_FLAG_RANGE 2u
+#define ECS_FLAG_COLLISION 4u
+
+struct EcsDevStatus {
+  unsigned long long collisions;   // accepted collisions
+  unsigned long long refused;      // refused collisions (final speed > 10 viT)
+  unsigned long long acc_fix;      // fixed-point sum (2^-24 units) of acceptance probabilities
+  unsigned long long acc_count;    // number of acceptance samples in acc_fix
+  unsigned int flags;              // ECS_FLAG_*
+  unsigned int pad;
+};
+
+// Multigrid level (one precision).
+template <typename T>
+struct MgLevel {
+  int nx, ny, nz;
+  size_t n;
+  double hx, hy, hz;
+  T *dens = nullptr;   // density defining the operator on this level
+  T *x = nullptr;      // iterate (correction) on this level
+  T *b = nullptr;      // right-hand side on this level
+  T *r = nullptr;      // residual / scratch
+  T *t = nullptr;      // smoother scratch
+  // z-line factorisation of the (lower, diag, upper) z-tridiagonal part,
+  // cyclic closure by Sherman-Morrison (periodic z) or plain (reflecting z).
+  T *zl_a = nullptr, *zl_cp = nullptr, *zl_minv = nullptr, *zl_q = nullptr;
+  T *zl_dp = nullptr;  // per-sweep forward-substitution scratch
+  T *zl_a0g = nullptr, *zl_qden = nullptr;  // per-column Sherman-Morrison scalars
+};
+
+template <typename T>
+struct Multigrid {
+  std::vector<MgLevel<T>> lv;
+  bool built = false;
+};
+
+struct EcsCtx {
+  EcsParams p;
+  int prec = ECS_PREC_FP64;
+  int64_t cap = 0, np = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0;
+  int nsm = 0;
+  size_t ncell = 0;    // Nx*Ny*Nz
+  size_t next = 0;     // (Nx+1)*(Ny+1)*(Nz+1) extended nodes
+
+  // FP64 plain particles: absolute positions and velocities, SoA.
+  double *px = nullptr, *py = nullptr, *pz = nullptr;
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+
+  // Mixed particles: int32 cell + FP32 in-cell offset + FP32 velocity, SoA,
+  // double-buffered for the counting sort.
+  int32_t *cell[2] = {nullptr, nullptr};
+  float *ox[2] = {nullptr, nullptr}, *oy[2] = {nullptr, nullptr}, *oz[2] = {nullptr, nullptr};
+  float *ux[2] = {nullptr, nullptr}, *uy[2] = {nullptr, nullptr}, *uz[2] = {nullptr, nullptr};
+  int cur = 0;
+  int32_t *sort_count = nullptr;   // [ncell]
+  int32_t *sort_offset = nullptr;  // [ncell+1]
+  int32_t *scan_blocks = nullptr;  // block sums of the scan
+  int sort_every = 4;
+  int steps_since_sort = 0;
+
+  // Grid fields.
+  double *phi = nullptr;            // potential [ncell]
+  double4_32a *eext64 = nullptr;        // difference numerators on extended nodes
+  float4 *eext32 = nullptr;
+  long long *acc = nullptr;         // fixed-point moments [4][ncell]
+  double *mom = nullptr;            // FP64 moments SoA [4][ncell]
+  double *rhs = nullptr;            // [ncell]
+  double *red = nullptr;            // reduction scratch (FP64)
+  int nred = 0;
+
+  // Solver state.
+  Multigrid<double> mg64;
+  Multigrid<float> mg32;
+  int krylov_m = 30;
+  double *kv64 = nullptr;           // FP64 Krylov basis V [(m+1)*ncell]
+  double *kz64 = nullptr;           // FP64 preconditioned basis Z [m*ncell]
+  float *kv32 = nullptr;            // FP32 Krylov basis for the inner solve
+  float *kz32 = nullptr;
+  double *w64 = nullptr;            // FP64 work vectors
+  double *r64 = nullptr;
+  double *dots = nullptr;           // device dot results [m+2]
+  double *h_dots = nullptr;         // pinned host copy
+  bool lhs_ready = false;
+  bool moments_ready = false;
+  bool eext_ready = false;          // difference numerators valid for the current phi
+  int warm_start = 0;               // ecs_step starts the solve from the previous phi
+
+  // Collision state.
+  uint64_t seed = 20261203ull;
+  int64_t step_index = 0;
+  double attempt_rate = -1.0;       // attempts per ion per call (< 0: not yet estimated)
+  EcsDevStatus *dstat = nullptr;
+  EcsDevStatus *hstat = nullptr;    // pinned
+
+  int64_t launches = 0;
+  std::string err;
+};
+
+// ---- error helpers -------------------------------------------------------
+int ecs_fail(EcsCtx *ctx, int code, const char *fmt, ...);
+int ecs_cuda_check(EcsCtx *ctx, cudaError_t e, const char *what);
+#define ECS_CUDA(ctx, call)                                        \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return ecs_cuda_check((ctx), e_, #call); \
+  } while (0)
+#define ECS_LAUNCHED(ctx)                                                   \
+  do {                                                                      \
+    (ctx)->launches++;                                                      \
+    cudaError_t e_ = cudaGetLastError();                                    \
+    if (e_ != cudaSuccess) return ecs_cuda_check((ctx), e_, "kernel launch"); \
+  } while (0)
+
+static inline unsigned int ecs_div_up(size_t a, size_t b) { return (unsigned int)((a + b - 1) / b); }
+
+// ---- counter-based RNG: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) --
+struct EcsU4 {
+  uint32_t x, y, z, w;
+};
+__device__ __forceinline__ EcsU4 ecs_philox(EcsU4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    EcsU4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+// Uniform in (0,1): 24 random bits, offset by half a step.
+__device__ __forceinline__ float ecs_u01f(uint32_t u) { return ((u >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ double ecs_u01d(uint32_t a, uint32_t b) {
+  uint64_t v = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);  // 52 bits
+  return ((double)v + 0.5) * (1.0 / 4503599627370496.0);
+}
+// 32-bit mixing (splitmix-style finaliser) for hashing particle state.
+__device__ __forceinline__ uint32_t ecs_mix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7feb352du;
+  h ^= h >> 15;
+  h *= 0x846ca68bu;
+  h ^= h >> 16;
+  return h;
+}
+
+// ---- kernels launched from several translation units --------------------
+// (defined in ecs_grid.cu)
+int ecs_grid_eext(EcsCtx *ctx);          // difference numerators from phi
+int ecs_grid_moments(EcsCtx *ctx);       // fixed-point -> FP64 moments
+int ecs_grid_rhs(EcsCtx *ctx);           // RHS (+ mean removal) from moments
+int ecs_grid_clear_acc(EcsCtx *ctx);
+int ecs_solver_setup(EcsCtx *ctx);       // multigrid hierarchy from the density
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st);
+int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y);
+int ecs_solver_free(EcsCtx *ctx);
+// (defined in ecs_particles.cu)
+int ecs_particles_alloc(EcsCtx *ctx);
+int ecs_particles_free(EcsCtx *ctx);
+int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
+int ecs_part_download(EcsCtx *ctx, double *pos, double *vel);
+int ecs_part_push(EcsCtx *ctx, double dt);
+int ecs_part_collide(EcsCtx *ctx, double dt);
+int ecs_part_move(EcsCtx *ctx, double dt);
+int ecs_part_collect(EcsCtx *ctx);
+int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide);
+int ecs_part_sort(EcsCtx *ctx);
+int ecs_part_estimate_rate(EcsCtx *ctx, double dt);

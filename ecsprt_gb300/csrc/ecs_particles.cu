@@ -1,0 +1,1096 @@
+// Particle phase of the ECSPRT hot path on sm_103a.
+//
+//   push     BorisMoverBz3D + DifferenceVector3D   src/velocities.c:281-371,
+//                                                  src/vector-math.c:596-722
+//   collide  ScatterElastic                        src/collisions.c:9-167
+//   move     UpdatePositions + ApplyBC             src/positions.c:436-472,
+//                                                  src/boundaries.c:6-34
+//   collect  Collect3DFluidMoments                 src/moments.c:108-226
+//
+// Two data layouts:
+//   FP64 plain: absolute positions and velocities, FP64 SoA, reference
+//     arithmetic operand for operand (separately rounded, no FMA), so push and
+//     move agree bit for bit with the reference.
+//   Mixed: packed int32 cell (i | j<<10 | k<<20) + FP32 in-cell offset in
+//     [0,1) + FP32 velocity, SoA, counting-sorted by cell every few steps.
+//
+// Deposition: every contribution is rounded to an integer multiple of 2^-S and
+// added into int64 accumulators, so moments do not depend on the order of
+// particles or atomics (bit-reproducible run to run).  Warps whose 32 lanes
+// share one cell (the common case for cell-sorted particles) combine their
+// 32 values per lane with a register reduce-scatter and issue one atomic per
+// lane; other warps issue per-lane atomics.
+//
+// Collisions: the reference picks Nc random ions with replacement and accepts
+// each attempt with the product of two uniforms below |vr|^2/vrm^2
+// (PetscSqr(ran3()) expands to two draws).  Here every ion draws a Poisson
+// number of attempts with mean rate = Nc / (np * <P_accept>), so the expected
+// number of accepted collisions is Nc and each ion is chosen with probability
+// proportional to its acceptance, as in the reference.  <P_accept> is
+// measured (fixed-point, order independent) on every pass and used on the
+// next one.  Random numbers come from Philox4x32-10 keyed by a hash of the
+// particle's own state and the step index, so results do not depend on the
+// particle order in memory.
+#include <math.h>
+
+#include "ecs_internal.cuh"
+
+namespace {
+
+// ---- exact FP64 arithmetic: every operation separately rounded ------------
+struct rd {
+  double v;
+};
+__device__ __forceinline__ rd operator+(rd a, rd b) { return {__dadd_rn(a.v, b.v)}; }
+__device__ __forceinline__ rd operator-(rd a, rd b) { return {__dsub_rn(a.v, b.v)}; }
+__device__ __forceinline__ rd operator*(rd a, rd b) { return {__dmul_rn(a.v, b.v)}; }
+__device__ __forceinline__ rd operator/(rd a, rd b) { return {__ddiv_rn(a.v, b.v)}; }
+
+constexpr int kBlock = 256;
+
+struct PartK {
+  int Nx, Ny, Nz;
+  int bc[3];
+  size_t ncell;
+  double dx, dy, dz;
+  double lo[3], hi[3], L[3];  // grid bounds (x0, x1, Lx per axis)
+  // Boris constants, src/velocities.c:307-320
+  double t, s, esc[3];
+  float tf, sf, escf[3];
+  double dt;
+  float dtc[3];  // dt / cell width, FP32 (mixed move)
+  // collisions, src/collisions.c:18-63
+  int collide;
+  double rate, p0, vrm2, viT, vnT, vn0[3], mi, mn, M;  // p0 = exp(-rate)
+  uint32_t key0, key1, step;
+  double fix64;
+  float fix32;
+};
+
+// ---- deposit ---------------------------------------------------------------
+__device__ __forceinline__ long long fix_rn(double v, double s) { return __double2ll_rn(v * s); }
+__device__ __forceinline__ long long fix_rn(float v, float s) { return __float2ll_rn(v * s); }
+
+// Linear node index of corner b (xb = b&1, yb = b>>1&1, zb = b>>2) of cell
+// (i,j,k), or -1 when it falls outside a non-periodic dimension.
+__device__ __forceinline__ long long corner_node(const PartK &k, int i, int j, int kk, int b) {
+  int ii = i + (b & 1), jj = j + ((b >> 1) & 1), zz = kk + (b >> 2);
+  if (ii >= k.Nx) { if (k.bc[0]) return -1; ii -= k.Nx; }
+  if (jj >= k.Ny) { if (k.bc[1]) return -1; jj -= k.Ny; }
+  if (zz >= k.Nz) { if (k.bc[2]) return -1; zz -= k.Nz; }
+  return ((long long)zz * k.Ny + jj) * k.Nx + ii;
+}
+
+// Deposit one particle's CIC contributions (src/moments.c:162-205): weights
+// w_b = wz*wy*wx over the 8 corners, density += w_b, flux_d += v_d*w_b.
+// All lanes of the warp must call this together.
+template <typename T>
+__device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, const PartK &k,
+                                             bool active, int i, int j, int kk, T wxh, T wyh,
+                                             T wzh, T v0, T v1, T v2, T scale) {
+  const int lane = threadIdx.x & 31;
+  T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
+  T w[8];
+  w[0] = wzl * wyl * wxl;
+  w[1] = wzl * wyl * wxh;
+  w[2] = wzl * wyh * wxl;
+  w[3] = wzl * wyh * wxh;
+  w[4] = wzh * wyl * wxl;
+  w[5] = wzh * wyl * wxh;
+  w[6] = wzh * wyh * wxl;
+  w[7] = wzh * wyh * wxh;
+  long long c[32];
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    c[b] = active ? fix_rn(w[b], scale) : 0;
+    c[8 + b] = active ? fix_rn(v0 * w[b], scale) : 0;
+    c[16 + b] = active ? fix_rn(v1 * w[b], scale) : 0;
+    c[24 + b] = active ? fix_rn(v2 * w[b], scale) : 0;
+  }
+  int key = active ? (i | (j << 10) | (kk << 20)) : -1;
+  unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+  if (peers == ECS_FULL_MASK && key >= 0) {
+    // Register reduce-scatter: afterwards lane l holds the warp sum of slot l.
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+      const bool upper = (lane & s) != 0;
+#pragma unroll
+      for (int q = 0; q < s; q++) {
+        long long send = upper ? c[q] : c[q + s];
+        long long keep = upper ? c[q + s] : c[q];
+        c[q] = keep + __shfl_xor_sync(ECS_FULL_MASK, send, s);
+      }
+    }
+    long long node = corner_node(k, i, j, kk, lane & 7);
+    if (node >= 0 && c[0] != 0)
+      atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node],
+                (unsigned long long)c[0]);
+  } else if (active) {
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+      long long node = corner_node(k, i, j, kk, b);
+      if (node < 0) continue;
+#pragma unroll
+      for (int d = 0; d < 4; d++)
+        if (c[8 * d + b] != 0)
+          atomicAdd((unsigned long long *)&acc[(size_t)d * k.ncell + node],
+                    (unsigned long long)c[8 * d + b]);
+    }
+  }
+}
+
+// ---- collisions --------------------------------------------------------------
+__device__ __forceinline__ void state_hash(const uint32_t *w, int n, uint32_t &h0, uint32_t &h1) {
+  uint32_t a = 0x811C9DC5u, b = 0x27D4EB2Fu;
+  for (int q = 0; q < n; q++) {
+    a = ecs_mix32(a ^ w[q]);
+    b = ecs_mix32(b + w[q] * 0x9E3779B1u);
+  }
+  h0 = a;
+  h1 = ecs_mix32(b ^ a);
+}
+
+template <typename T>
+struct RMath;
+template <>
+struct RMath<float> {
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float log_(float x) { return logf(x); }
+  static __device__ __forceinline__ void sincospi_(float x, float *s, float *c) { sincospif(x, s, c); }
+  static __device__ __forceinline__ float u01(uint32_t a, uint32_t) { return ecs_u01f(a); }
+};
+template <>
+struct RMath<double> {
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double log_(double x) { return log(x); }
+  static __device__ __forceinline__ void sincospi_(double x, double *s, double *c) { sincospi(x, s, c); }
+  static __device__ __forceinline__ double u01(uint32_t a, uint32_t b) { return ecs_u01d(a, b); }
+};
+
+// Acceptance probability of one attempt: P(U1*U2 < a) = a(1 - ln a), a < 1.
+template <typename T>
+__device__ __forceinline__ T accept_prob(T a) {
+  if (a >= T(1)) return T(1);
+  if (a <= T(0)) return T(0);
+  return a * (T(1) - RMath<T>::log_(a));
+}
+
+// One ion's collisions in one pass (src/collisions.c:70-157).  Returns the
+// acceptance probability sample used to estimate the next pass's rate.
+template <typename T>
+__device__ float collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &vy, T &vz,
+                             unsigned int &nacc, unsigned int &nref) {
+  typedef RMath<T> M;
+  // acceptance sample for the rate estimate (uses pre-collision velocity)
+  EcsU4 e = ecs_philox({h0, h1, 0xFFFFFFFEu, k.step}, k.key0, k.key1);
+  T r1 = M::sqrt_(T(-2) * M::log_(M::u01(e.x, e.y)));
+  T s1, c1, s2, c2;
+  M::sincospi_(T(2) * M::u01(e.z, e.w), &s1, &c1);
+  EcsU4 e2 = ecs_philox({h0, h1, 0xFFFFFFFDu, k.step}, k.key0, k.key1);
+  T r2 = M::sqrt_(T(-2) * M::log_(M::u01(e2.x, e2.y)));
+  M::sincospi_(T(2) * M::u01(e2.z, e2.w), &s2, &c2);
+  T wx = vx - (T(r1 * c1) * T(k.vnT) + T(k.vn0[0]));
+  T wy = vy - (T(r1 * s1) * T(k.vnT) + T(k.vn0[1]));
+  T wz = vz - (T(r2 * c2) * T(k.vnT) + T(k.vn0[2]));
+  float sample = (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
+
+  // number of attempts ~ Poisson(rate), by inversion
+  EcsU4 pz = ecs_philox({h0, h1, 0xFFFFFFFFu, k.step}, k.key0, k.key1);
+  T u = M::u01(pz.x, pz.y);
+  T p = T(k.p0), cdf = p, rate = T(k.rate);
+  int natt = 0;
+  while (u > cdf && natt < 16) {
+    natt++;
+    p *= rate / T(natt);
+    cdf += p;
+  }
+  for (int a = 0; a < natt; a++) {
+    EcsU4 q1 = ecs_philox({h0, h1, 2u * a, k.step}, k.key0, k.key1);
+    EcsU4 q2 = ecs_philox({h0, h1, 2u * a + 1u, k.step}, k.key0, k.key1);
+    T ra = M::sqrt_(T(-2) * M::log_(M::u01(q1.x, q1.y)));
+    T sa, ca;
+    M::sincospi_(T(2) * M::u01(q1.z, q1.w), &sa, &ca);
+    EcsU4 q3 = ecs_philox({h0, h1, 0x40000000u + a, k.step}, k.key0, k.key1);
+    T rb = M::sqrt_(T(-2) * M::log_(M::u01(q3.x, q3.y)));
+    T sb, cb;
+    M::sincospi_(T(2) * M::u01(q3.z, q3.w), &sb, &cb);
+    T vn[3] = {ra * ca * T(k.vnT) + T(k.vn0[0]), ra * sa * T(k.vnT) + T(k.vn0[1]),
+               rb * cb * T(k.vnT) + T(k.vn0[2])};
+    T vi[3] = {vx, vy, vz};
+    T vr[3] = {vi[0] - vn[0], vi[1] - vn[1], vi[2] - vn[2]};
+    T vrr2 = vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2];
+    T U1 = M::u01(q2.x, q2.x), U2 = M::u01(q2.y, q2.y);
+    if (!(U1 * U2 < vrr2 / T(k.vrm2))) continue;
+    T vrr = M::sqrt_(vrr2);
+    T vc[3], tmp = T(0);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      vc[d] = (vi[d] * T(k.mi) + vn[d] * T(k.mn)) / T(k.M);
+      tmp += (vi[d] - vc[d]) * (vi[d] - vc[d]);
+    }
+    T vcr = M::sqrt_(tmp);
+    T u0z = T(2) * M::u01(q2.z, q2.z) - T(1);
+    T uperp = M::sqrt_(T(1) - u0z * u0z);
+    T sphi, cphi;
+    M::sincospi_(T(2) * M::u01(q2.w, q2.w), &sphi, &cphi);
+    T u0x = uperp * cphi, u0y = uperp * sphi;
+    T costht = vr[2] / vrr;
+    T sintht = M::sqrt_(T(1) - costht * costht);
+    T cosphi = vr[0] / (vrr * sintht);
+    T sinphi = vr[1] / (vrr * sintht);
+    T u1x = u0z * sintht + u0x * costht;
+    T u1y = u0y;
+    T u1z = u0z * costht - u0x * sintht;
+    T u2[3] = {u1x * cosphi - u1y * sinphi, u1x * sinphi + u1y * cosphi, u1z};
+    T vf[3], vf2 = T(0);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      vf[d] = vc[d] + vcr * u2[d];
+      vf2 += vf[d] * vf[d];
+    }
+    if (M::sqrt_(vf2) / T(k.viT) > T(10)) {
+      nref++;
+    } else {
+      vx = vf[0];
+      vy = vf[1];
+      vz = vf[2];
+      nacc++;
+    }
+  }
+  return sample;
+}
+
+// Warp-aggregated status counters.
+__device__ __forceinline__ void flush_counts(EcsDevStatus *st, unsigned int nacc,
+                                             unsigned int nref, float sample, bool active,
+                                             bool collide) {
+  if (!collide) return;
+  unsigned int a = __reduce_add_sync(ECS_FULL_MASK, nacc);
+  unsigned int r = __reduce_add_sync(ECS_FULL_MASK, nref);
+  unsigned int f = __reduce_add_sync(ECS_FULL_MASK, active ? (unsigned int)__float2uint_rn(sample * 16777216.0f) : 0u);
+  unsigned int n = __popc(__ballot_sync(ECS_FULL_MASK, active));
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(&st->collisions, (unsigned long long)a);
+    if (r) atomicAdd(&st->refused, (unsigned long long)r);
+    if (n) {
+      atomicAdd(&st->acc_fix, (unsigned long long)f);
+      atomicAdd(&st->acc_count, (unsigned long long)n);
+    }
+  }
+}
+
+// ==========================================================================
+// FP64 plain path
+// ==========================================================================
+
+// Difference numerators at the 8 corners, interpolated with the reference's
+// weight order (src/vector-math.c:645-651): along y with wyh, across the z
+// pair with wxh, across the x pair with wzh.
+__device__ __forceinline__ void gather64(const double4_32a *__restrict__ E, const PartK &k, int i,
+                                         int j, int kk, rd wx, rd wy, rd wz, rd f[3]) {
+  const size_t sx = (size_t)k.Nx + 1, sxy = sx * ((size_t)k.Ny + 1);
+  const size_t base = (size_t)kk * sxy + (size_t)j * sx + i;
+  double4_32a D[8];
+  D[0] = E[base];
+  D[1] = E[base + 1];
+  D[2] = E[base + sx];
+  D[3] = E[base + sx + 1];
+  D[4] = E[base + sxy];
+  D[5] = E[base + sxy + 1];
+  D[6] = E[base + sxy + sx];
+  D[7] = E[base + sxy + sx + 1];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    rd v[8];
+#pragma unroll
+    for (int b = 0; b < 8; b++) v[b] = {c == 0 ? D[b].x : (c == 1 ? D[b].y : D[b].z)};
+    // a[zb][xb] = D(zb,0,xb) + wy*(D(zb,1,xb) - D(zb,0,xb)); index b = zb*4+yb*2+xb
+    rd a00 = v[0] + wy * (v[2] - v[0]);
+    rd a01 = v[1] + wy * (v[3] - v[1]);
+    rd a10 = v[4] + wy * (v[6] - v[4]);
+    rd a11 = v[5] + wy * (v[7] - v[5]);
+    rd c0 = a00 + wx * (a10 - a00);
+    rd c1 = a01 + wx * (a11 - a01);
+    f[c] = c0 + wz * (c1 - c0);
+  }
+}
+
+// Fractional grid coordinate and cell index along one axis; positions at
+// exactly the upper bound (possible only when r + L rounds to L in the
+// reference's single wrap) are folded onto the lower bound.
+__device__ __forceinline__ bool cell_coord(double pos, double d, int N, rd &x, int &ix) {
+  x = rd{pos} / rd{d};
+  ix = (int)x.v;
+  if (ix >= N) {
+    x = x - rd{(double)N};
+    ix -= N;
+  }
+  return ix >= 0 && ix < N && x.v >= 0.0;
+}
+
+__device__ __forceinline__ void push64(const PartK &k, const double4_32a *__restrict__ E, double px,
+                                       double py, double pz, double &vx, double &vy, double &vz,
+                                       bool &ok) {
+  rd x, y, z;
+  int i, j, kk;
+  ok = cell_coord(px, k.dx, k.Nx, x, i) & cell_coord(py, k.dy, k.Ny, y, j) &
+       cell_coord(pz, k.dz, k.Nz, z, kk);
+  if (!ok) return;
+  rd f[3];
+  gather64(E, k, i, j, kk, x - rd{(double)i}, y - rd{(double)j}, z - rd{(double)kk}, f);
+  rd vxm = rd{vx} + rd{k.esc[0]} * f[0];
+  rd vym = rd{vy} + rd{k.esc[1]} * f[1];
+  rd vzm = rd{vz} + rd{k.esc[2]} * f[2];
+  rd vxt = vxm + vym * rd{k.t};
+  rd vyp = vym - vxt * rd{k.s};
+  rd vxp = vxt + vyp * rd{k.t};
+  vx = vxp.v;
+  vy = vyp.v;
+  vz = vzm.v;
+}
+
+// src/positions.c:455-459 then src/boundaries.c:19-31 (one periodic wrap);
+// reflecting axes reflect specularly.
+__device__ __forceinline__ void move64(const PartK &k, double &p, double &v, int d) {
+  rd r = rd{p} + rd{v} * rd{k.dt};
+  if (k.bc[d] == ECS_BC_PERIODIC) {
+    if (r.v < k.lo[d]) r = r + rd{k.L[d]};
+    if (r.v >= k.hi[d]) r = r - rd{k.L[d]};
+  } else {
+    if (r.v < k.lo[d]) { r = rd{2.0 * k.lo[d]} - r; v = -v; }
+    if (r.v >= k.hi[d]) { r = rd{2.0 * k.hi[d]} - r; v = -v; }
+  }
+  p = r.v;
+}
+
+__device__ __forceinline__ void deposit64(long long *acc, const PartK &k, bool active, double px,
+                                          double py, double pz, double vx, double vy, double vz) {
+  rd x{0}, y{0}, z{0};
+  int i = 0, j = 0, kk = 0;
+  bool ok = active;
+  if (active)
+    ok = cell_coord(px, k.dx, k.Nx, x, i) & cell_coord(py, k.dy, k.Ny, y, j) &
+         cell_coord(pz, k.dz, k.Nz, z, kk);
+  double wx = ok ? (x - rd{(double)i}).v : 0.0;
+  double wy = ok ? (y - rd{(double)j}).v : 0.0;
+  double wz = ok ? (z - rd{(double)kk}).v : 0.0;
+  deposit_warp<double>(acc, k, ok, i, j, kk, wx, wy, wz, vx, vy, vz, k.fix64);
+}
+
+__device__ __forceinline__ void hash64(double px, double py, double pz, double vx, double vy,
+                                       double vz, uint32_t &h0, uint32_t &h1) {
+  uint32_t w[12];
+  double s[6] = {px, py, pz, vx, vy, vz};
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    unsigned long long b = __double_as_longlong(s[q]);
+    w[2 * q] = (uint32_t)b;
+    w[2 * q + 1] = (uint32_t)(b >> 32);
+  }
+  state_hash(w, 12, h0, h1);
+}
+
+// mode bits: 1 push, 2 collide, 4 move, 8 deposit
+__global__ void __launch_bounds__(kBlock) k_particles64(PartK k, int mode, int64_t np,
+                                                        double *__restrict__ px,
+                                                        double *__restrict__ py,
+                                                        double *__restrict__ pz,
+                                                        double *__restrict__ vxa,
+                                                        double *__restrict__ vya,
+                                                        double *__restrict__ vza,
+                                                        const double4_32a *__restrict__ E,
+                                                        long long *__restrict__ acc,
+                                                        EcsDevStatus *st) {
+  const int64_t lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += stride) {
+    const int64_t ip = base + lane;
+    const bool active = ip < np;
+    double x = 0, y = 0, z = 0, vx = 0, vy = 0, vz = 0;
+    if (active) {
+      x = px[ip]; y = py[ip]; z = pz[ip];
+      vx = vxa[ip]; vy = vya[ip]; vz = vza[ip];
+    }
+    bool ok = true;
+    if ((mode & 1) && active) {
+      push64(k, E, x, y, z, vx, vy, vz, ok);
+      if (!ok) atomicOr(&st->flags, ECS_FLAG_RANGE);
+    }
+    unsigned int nacc = 0, nref = 0;
+    float sample = 0.f;
+    if ((mode & 2) && k.collide) {
+      if (active) {
+        uint32_t h0, h1;
+        hash64(x, y, z, vx, vy, vz, h0, h1);
+        sample = collide_ion<double>(k, h0, h1, vx, vy, vz, nacc, nref);
+      }
+      flush_counts(st, nacc, nref, sample, active, true);
+    }
+    if ((mode & 4) && active) {
+      move64(k, x, vx, 0);
+      move64(k, y, vy, 1);
+      move64(k, z, vz, 2);
+    }
+    if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
+    if (mode & 8) deposit64(acc, k, active, x, y, z, vx, vy, vz);
+    if (active) {
+      if (mode & 4) { px[ip] = x; py[ip] = y; pz[ip] = z; }
+      if (mode & 7) { vxa[ip] = vx; vya[ip] = vy; vza[ip] = vz; }
+    }
+  }
+}
+
+// ==========================================================================
+// Mixed path
+// ==========================================================================
+__device__ __forceinline__ void unpack_cell(int32_t c, int &i, int &j, int &kk) {
+  i = c & 1023;
+  j = (c >> 10) & 1023;
+  kk = (c >> 20) & 1023;
+}
+
+__device__ __forceinline__ void gather32(const float4 *__restrict__ E, const PartK &k, int i,
+                                         int j, int kk, float wx, float wy, float wz, float f[3]) {
+  const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
+  const int base = kk * sxy + j * sx + i;
+  float4 D[8];
+  D[0] = __ldg(&E[base]);
+  D[1] = __ldg(&E[base + 1]);
+  D[2] = __ldg(&E[base + sx]);
+  D[3] = __ldg(&E[base + sx + 1]);
+  D[4] = __ldg(&E[base + sxy]);
+  D[5] = __ldg(&E[base + sxy + 1]);
+  D[6] = __ldg(&E[base + sxy + sx]);
+  D[7] = __ldg(&E[base + sxy + sx + 1]);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float v[8];
+#pragma unroll
+    for (int b = 0; b < 8; b++) v[b] = c == 0 ? D[b].x : (c == 1 ? D[b].y : D[b].z);
+    float a00 = v[0] + wy * (v[2] - v[0]);
+    float a01 = v[1] + wy * (v[3] - v[1]);
+    float a10 = v[4] + wy * (v[6] - v[4]);
+    float a11 = v[5] + wy * (v[7] - v[5]);
+    float c0 = a00 + wx * (a10 - a00);
+    float c1 = a01 + wx * (a11 - a01);
+    f[c] = c0 + wz * (c1 - c0);
+  }
+}
+
+// Advance an in-cell offset by du (cell units); returns the cell shift.
+__device__ __forceinline__ int advance(float &o, float du) {
+  float q = o + du;
+  float fl = floorf(q);
+  int sh = (int)fl;
+  q = q - fl;
+  if (q >= 1.0f) {  // q - floor(q) rounded up to 1 for tiny negative q
+    q = 0.0f;
+    sh += 1;
+  }
+  o = q;
+  return sh;
+}
+
+// Apply the boundary condition to an integer cell coordinate along one axis.
+__device__ __forceinline__ bool bound_axis(int bc, int N, int &c, float &o, float &v) {
+  if (c >= 0 && c < N) return true;
+  if (bc == ECS_BC_PERIODIC) {
+    c %= N;
+    if (c < 0) c += N;
+    return true;
+  }
+  // specular reflection: position c + o mirrored about 0 or N
+  if (c < 0) {
+    c = -c - 1;
+    o = 1.0f - o;
+  } else {
+    c = 2 * N - c - 1;
+    o = 1.0f - o;
+  }
+  if (o >= 1.0f) { o = 0.0f; c += 1; }
+  v = -v;
+  return c >= 0 && c < N;
+}
+
+__device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, float vx,
+                                       float vy, float vz, uint32_t &h0, uint32_t &h1) {
+  uint32_t w[7] = {(uint32_t)c, __float_as_uint(ox), __float_as_uint(oy), __float_as_uint(oz),
+                   __float_as_uint(vx), __float_as_uint(vy), __float_as_uint(vz)};
+  state_hash(w, 7, h0, h1);
+}
+
+__global__ void __launch_bounds__(kBlock) k_particles32(
+    PartK k, int mode, int64_t np, int32_t *__restrict__ cella, float *__restrict__ oxa,
+    float *__restrict__ oya, float *__restrict__ oza, float *__restrict__ uxa,
+    float *__restrict__ uya, float *__restrict__ uza, const float4 *__restrict__ E,
+    long long *__restrict__ acc, EcsDevStatus *st) {
+  const int64_t lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += stride) {
+    const int64_t ip = base + lane;
+    const bool active = ip < np;
+    int32_t c = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+    if (active) {
+      c = cella[ip];
+      ox = oxa[ip]; oy = oya[ip]; oz = oza[ip];
+      vx = uxa[ip]; vy = uya[ip]; vz = uza[ip];
+    }
+    int i, j, kk;
+    unpack_cell(c, i, j, kk);
+    if ((mode & 1) && active) {
+      float f[3];
+      gather32(E, k, i, j, kk, ox, oy, oz, f);
+      float vxm = vx + k.escf[0] * f[0];
+      float vym = vy + k.escf[1] * f[1];
+      float vzm = vz + k.escf[2] * f[2];
+      float vxt = vxm + vym * k.tf;
+      float vyp = vym - vxt * k.sf;
+      float vxp = vxt + vyp * k.tf;
+      vx = vxp;
+      vy = vyp;
+      vz = vzm;
+    }
+    unsigned int nacc = 0, nref = 0;
+    float sample = 0.f;
+    if ((mode & 2) && k.collide) {
+      if (active) {
+        uint32_t h0, h1;
+        hash32(c, ox, oy, oz, vx, vy, vz, h0, h1);
+        sample = collide_ion<float>(k, h0, h1, vx, vy, vz, nacc, nref);
+      }
+      flush_counts(st, nacc, nref, sample, active, true);
+    }
+    bool inside = true;
+    if ((mode & 4) && active) {
+      i += advance(ox, vx * k.dtc[0]);
+      j += advance(oy, vy * k.dtc[1]);
+      kk += advance(oz, vz * k.dtc[2]);
+      inside = bound_axis(k.bc[0], k.Nx, i, ox, vx) & bound_axis(k.bc[1], k.Ny, j, oy, vy) &
+               bound_axis(k.bc[2], k.Nz, kk, oz, vz);
+      if (!inside) {
+        atomicOr(&st->flags, ECS_FLAG_RANGE);
+        i = min(max(i, 0), k.Nx - 1);
+        j = min(max(j, 0), k.Ny - 1);
+        kk = min(max(kk, 0), k.Nz - 1);
+      }
+      c = i | (j << 10) | (kk << 20);
+    }
+    if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
+    if (mode & 8) deposit_warp<float>(acc, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fix32);
+    if (active) {
+      if (mode & 4) { cella[ip] = c; oxa[ip] = ox; oya[ip] = oy; oza[ip] = oz; }
+      if (mode & 7) { uxa[ip] = vx; uya[ip] = vy; uza[ip] = vz; }
+    }
+  }
+}
+
+// ---- upload / download conversions ---------------------------------------------
+__global__ void k_aos_to_soa64(int64_t n, const double *__restrict__ pos,
+                               const double *__restrict__ vel, double *px, double *py,
+                               double *pz, double *vx, double *vy, double *vz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    px[i] = pos[3 * i]; py[i] = pos[3 * i + 1]; pz[i] = pos[3 * i + 2];
+    vx[i] = vel[3 * i]; vy[i] = vel[3 * i + 1]; vz[i] = vel[3 * i + 2];
+  }
+}
+__global__ void k_soa_to_aos64(int64_t n, double *__restrict__ pos, double *__restrict__ vel,
+                               const double *px, const double *py, const double *pz,
+                               const double *vx, const double *vy, const double *vz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    pos[3 * i] = px[i]; pos[3 * i + 1] = py[i]; pos[3 * i + 2] = pz[i];
+    vel[3 * i] = vx[i]; vel[3 * i + 1] = vy[i]; vel[3 * i + 2] = vz[i];
+  }
+}
+
+// Absolute FP64 coordinate -> (cell, FP32 offset) along one axis.
+__device__ __forceinline__ int to_cell(double pos, double d, int N, float &o) {
+  double x = pos / d;
+  double fl = floor(x);
+  int c = (int)fl;
+  float of = (float)(x - fl);
+  if (of >= 1.0f) { of = 0.0f; c += 1; }
+  c %= N;
+  if (c < 0) c += N;
+  o = of;
+  return c;
+}
+
+__global__ void k_aos_to_mixed(int64_t n, PartK k, const double *__restrict__ pos,
+                               const double *__restrict__ vel, int32_t *cell, float *ox,
+                               float *oy, float *oz, float *ux, float *uy, float *uz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float a, b, c;
+    int ci = to_cell(pos[3 * i], k.dx, k.Nx, a);
+    int cj = to_cell(pos[3 * i + 1], k.dy, k.Ny, b);
+    int ck = to_cell(pos[3 * i + 2], k.dz, k.Nz, c);
+    cell[i] = ci | (cj << 10) | (ck << 20);
+    ox[i] = a; oy[i] = b; oz[i] = c;
+    ux[i] = (float)vel[3 * i]; uy[i] = (float)vel[3 * i + 1]; uz[i] = (float)vel[3 * i + 2];
+  }
+}
+
+__global__ void k_mixed_to_aos(int64_t n, PartK k, double *__restrict__ pos,
+                               double *__restrict__ vel, const int32_t *cell, const float *ox,
+                               const float *oy, const float *oz, const float *ux,
+                               const float *uy, const float *uz) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int ci, cj, ck;
+    unpack_cell(cell[i], ci, cj, ck);
+    pos[3 * i] = ((double)ci + (double)ox[i]) * k.dx;
+    pos[3 * i + 1] = ((double)cj + (double)oy[i]) * k.dy;
+    pos[3 * i + 2] = ((double)ck + (double)oz[i]) * k.dz;
+    vel[3 * i] = ux[i]; vel[3 * i + 1] = uy[i]; vel[3 * i + 2] = uz[i];
+  }
+}
+
+// ---- counting sort by cell (mixed path) ------------------------------------------
+__device__ __forceinline__ int lin_cell(int32_t c, int Nx, int Ny) {
+  return (((c >> 20) & 1023) * Ny + ((c >> 10) & 1023)) * Nx + (c & 1023);
+}
+
+__global__ void k_sort_count(int64_t np, int Nx, int Ny, const int32_t *__restrict__ cell,
+                             int32_t *__restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ip = base + lane;
+    int key = ip < np ? lin_cell(cell[ip], Nx, Ny) : -1;
+    unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
+  }
+}
+
+// Exclusive scan of count[0..n) into off[0..n], three phases.
+constexpr int kScanBlock = 1024;
+constexpr int kScanItems = 4;
+__global__ void k_scan_local(int n, const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                             int32_t *__restrict__ sums) {
+  __shared__ int32_t warp_tot[32];
+  const int tile = kScanBlock * kScanItems;
+  const int base = blockIdx.x * tile + threadIdx.x * kScanItems;
+  int32_t v[kScanItems];
+  int32_t t = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    v[q] = (base + q < n) ? in[base + q] : 0;
+    t += v[q];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t incl = t;
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    int32_t y = __shfl_up_sync(ECS_FULL_MASK, incl, s);
+    if (lane >= s) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int32_t w = warp_tot[lane];
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+      int32_t y = __shfl_up_sync(ECS_FULL_MASK, w, s);
+      if (lane >= s) w += y;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  int32_t run = incl - t + (warp > 0 ? warp_tot[warp - 1] : 0);
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    if (base + q < n) out[base + q] = run;
+    run += v[q];
+  }
+  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = run;
+}
+__global__ void k_scan_sums(int nb, int32_t *sums) {
+  // single block: serial over chunks of 1024 with a carry
+  __shared__ int32_t buf[1024];
+  __shared__ int32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int off = 0; off < nb; off += 1024) {
+    int i = off + threadIdx.x;
+    int32_t v = i < nb ? sums[i] : 0;
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = 1; s < 1024; s <<= 1) {
+      int32_t y = threadIdx.x >= s ? buf[threadIdx.x - s] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += y;
+      __syncthreads();
+    }
+    if (i < nb) sums[i] = carry + buf[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += buf[1023];
+    __syncthreads();
+  }
+}
+__global__ void k_scan_add(int n, int32_t *__restrict__ out, const int32_t *__restrict__ sums,
+                           int32_t *__restrict__ total_out) {
+  const int tile = kScanBlock * kScanItems;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / tile];
+  if (i == n - 1 && total_out) *total_out = out[i];
+}
+
+__global__ void k_sort_scatter(int64_t np, int Nx, int Ny, const int32_t *__restrict__ off,
+                               int32_t *__restrict__ cursor, const int32_t *__restrict__ c0,
+                               const float *__restrict__ a0, const float *__restrict__ b0,
+                               const float *__restrict__ d0, const float *__restrict__ e0,
+                               const float *__restrict__ f0, const float *__restrict__ g0,
+                               int32_t *__restrict__ c1, float *__restrict__ a1,
+                               float *__restrict__ b1, float *__restrict__ d1,
+                               float *__restrict__ e1, float *__restrict__ f1,
+                               float *__restrict__ g1) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ip = base + lane;
+    int32_t c = ip < np ? c0[ip] : 0;
+    int key = ip < np ? lin_cell(c, Nx, Ny) : -1;
+    unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+    int leader = __ffs(peers) - 1;
+    int slot = 0;
+    if (key >= 0 && lane == leader) slot = atomicAdd(&cursor[key], __popc(peers));
+    slot = __shfl_sync(ECS_FULL_MASK, slot, leader);
+    if (key >= 0) {
+      int64_t dst = (int64_t)off[key] + slot + __popc(peers & ((1u << lane) - 1u));
+      c1[dst] = c;
+      a1[dst] = a0[ip]; b1[dst] = b0[ip]; d1[dst] = d0[ip];
+      e1[dst] = e0[ip]; f1[dst] = f0[ip]; g1[dst] = g0[ip];
+    }
+  }
+}
+
+// ---- collision-rate estimate (first pass only) -------------------------------------
+__global__ void k_estimate64(PartK k, int64_t np, const double *px, const double *py,
+                             const double *pz, const double *vxa, const double *vya,
+                             const double *vza, EcsDevStatus *st) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ip = base + lane;
+    bool active = ip < np;
+    float sample = 0.f;
+    if (active) {
+      double vx = vxa[ip], vy = vya[ip], vz = vza[ip];
+      uint32_t h0, h1;
+      hash64(px[ip], py[ip], pz[ip], vx, vy, vz, h0, h1);
+      PartK kk = k;
+      kk.rate = 0.0;
+      kk.p0 = 1.0;
+      unsigned int a = 0, r = 0;
+      sample = collide_ion<double>(kk, h0, h1, vx, vy, vz, a, r);
+    }
+    flush_counts(st, 0, 0, sample, active, true);
+  }
+}
+__global__ void k_estimate32(PartK k, int64_t np, const int32_t *cella, const float *oxa,
+                             const float *oya, const float *oza, const float *uxa,
+                             const float *uya, const float *uza, EcsDevStatus *st) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ip = base + lane;
+    bool active = ip < np;
+    float sample = 0.f;
+    if (active) {
+      float vx = uxa[ip], vy = uya[ip], vz = uza[ip];
+      uint32_t h0, h1;
+      hash32(cella[ip], oxa[ip], oya[ip], oza[ip], vx, vy, vz, h0, h1);
+      PartK kk = k;
+      kk.rate = 0.0;
+      kk.p0 = 1.0;
+      unsigned int a = 0, r = 0;
+      sample = collide_ion<float>(kk, h0, h1, vx, vy, vz, a, r);
+    }
+    flush_counts(st, 0, 0, sample, active, true);
+  }
+}
+
+// ---- host helpers -----------------------------------------------------------------
+PartK make_k(const EcsCtx *ctx, double dt) {
+  const EcsParams &p = ctx->p;
+  PartK k;
+  memset(&k, 0, sizeof k);
+  k.Nx = p.Nx; k.Ny = p.Ny; k.Nz = p.Nz;
+  for (int d = 0; d < 3; d++) k.bc[d] = p.bc[d] == ECS_BC_PERIODIC ? ECS_BC_PERIODIC : ECS_BC_INJECT_REFLECT;
+  k.ncell = ctx->ncell;
+  k.dx = p.dx; k.dy = p.dy; k.dz = p.dz;
+  k.lo[0] = p.x0; k.lo[1] = p.y0; k.lo[2] = p.z0;
+  k.hi[0] = p.x1; k.hi[1] = p.y1; k.hi[2] = p.z1;
+  k.L[0] = p.Lx; k.L[1] = p.Ly; k.L[2] = p.Lz;
+  // src/velocities.c:307-320, same operation order
+  double tscale = 0.5 * (p.qi / p.mi) * dt;
+  k.t = tscale * p.B0;
+  k.s = 2.0 * k.t / (1 + k.t * k.t);
+  double h[3] = {1.0 / p.dx, 1.0 / p.dy, 1.0 / p.dz};
+  for (int d = 0; d < 3; d++) {
+    k.esc[d] = -0.5 * h[d] * tscale;
+    k.escf[d] = (float)k.esc[d];
+  }
+  k.tf = (float)k.t;
+  k.sf = (float)k.s;
+  k.dt = dt;
+  k.dtc[0] = (float)(dt / p.dx);
+  k.dtc[1] = (float)(dt / p.dy);
+  k.dtc[2] = (float)(dt / p.dz);
+  // src/collisions.c:18-52
+  k.collide = p.mn > 0.0 ? 1 : 0;
+  double tmp = (p.vi0x - p.vn0x) * (p.vi0x - p.vn0x) + (p.vi0y - p.vn0y) * (p.vi0y - p.vn0y) +
+               (p.vi0z - p.vn0z) * (p.vi0z - p.vn0z);
+  double vrm = 4.0 * p.viT + sqrt(tmp);
+  k.vrm2 = vrm * vrm;
+  k.viT = p.viT;
+  k.vnT = p.vnT;
+  k.vn0[0] = p.vn0x; k.vn0[1] = p.vn0y; k.vn0[2] = p.vn0z;
+  k.mi = p.mi; k.mn = p.mn; k.M = p.mn + p.mi;
+  k.key0 = (uint32_t)ctx->seed;
+  k.key1 = (uint32_t)(ctx->seed >> 32);
+  k.step = (uint32_t)ctx->step_index;
+  k.fix64 = ldexp(1.0, ECS_FIX_SHIFT_FP64);
+  k.fix32 = ldexpf(1.0f, ECS_FIX_SHIFT_MIXED);
+  return k;
+}
+
+// Reference collision count Nc (src/collisions.c:58-63).
+int64_t collision_target(const EcsCtx *ctx, double dt) {
+  const EcsParams &p = ctx->p;
+  double tmp = (p.vi0x - p.vn0x) * (p.vi0x - p.vn0x) + (p.vi0y - p.vn0y) * (p.vi0y - p.vn0y) +
+               (p.vi0z - p.vn0z) * (p.vi0z - p.vn0z);
+  double vrm = 4.0 * p.viT + sqrt(tmp);
+  double fc = p.nui * dt;
+  double nc = ((double)ctx->np * fc * vrm) / ((p.vnT + p.vn0) * sqrt(p.mn / p.mi));
+  int64_t Nc = (int64_t)nc;
+  if (Nc > ctx->np) Nc = ctx->np;
+  if (Nc < 0) Nc = 0;
+  return Nc;
+}
+
+unsigned int grid_blocks(const EcsCtx *ctx, int64_t n, int per_sm) {
+  int64_t want = (n + kBlock - 1) / kBlock;
+  int64_t cap = (int64_t)ctx->nsm * per_sm;
+  if (want > cap) want = cap;
+  if (want < 1) want = 1;
+  return (unsigned int)want;
+}
+
+}  // namespace
+
+// ============================================================================
+// entry points used by ecs_api.cu
+// ============================================================================
+int ecs_particles_alloc(EcsCtx *ctx) {
+  size_t n = (size_t)ctx->cap;
+  if (n == 0) n = 1;
+  if (ctx->prec == ECS_PREC_FP64) {
+    double **arr[6] = {&ctx->px, &ctx->py, &ctx->pz, &ctx->vx, &ctx->vy, &ctx->vz};
+    for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(double)));
+  } else {
+    for (int b = 0; b < 2; b++) {
+      ECS_CUDA(ctx, cudaMalloc((void **)&ctx->cell[b], n * sizeof(int32_t)));
+      float **arr[6] = {&ctx->ox[b], &ctx->oy[b], &ctx->oz[b], &ctx->ux[b], &ctx->uy[b], &ctx->uz[b]};
+      for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(float)));
+    }
+    size_t nb = ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_count, ctx->ncell * sizeof(int32_t)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_offset, (ctx->ncell + 1) * sizeof(int32_t)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->scan_blocks, (nb + 1) * sizeof(int32_t)));
+  }
+  return ECS_OK;
+}
+
+int ecs_particles_free(EcsCtx *ctx) {
+  void *ptrs[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz,
+                  ctx->cell[0], ctx->cell[1], ctx->ox[0], ctx->ox[1], ctx->oy[0], ctx->oy[1],
+                  ctx->oz[0], ctx->oz[1], ctx->ux[0], ctx->ux[1], ctx->uy[0], ctx->uy[1],
+                  ctx->uz[0], ctx->uz[1], ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  return ECS_OK;
+}
+
+// Host AoS FP64 -> device, in chunks through a device staging buffer.
+int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np) {
+  if (np < 0 || np > ctx->cap) return ecs_fail(ctx, ECS_ERR_INVALID, "np %lld exceeds capacity %lld", (long long)np, (long long)ctx->cap);
+  const int64_t chunk = 1 << 22;
+  double *stage = nullptr;
+  int64_t cn = np < chunk ? (np > 0 ? np : 1) : chunk;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, (size_t)cn * 6 * sizeof(double), ctx->stream));
+  PartK k = make_k(ctx, 0.0);
+  for (int64_t off = 0; off < np; off += chunk) {
+    int64_t n = np - off < chunk ? np - off : chunk;
+    ECS_CUDA(ctx, cudaMemcpyAsync(stage, pos + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    ECS_CUDA(ctx, cudaMemcpyAsync(stage + 3 * n, vel + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    unsigned int g = grid_blocks(ctx, n, 8);
+    if (ctx->prec == ECS_PREC_FP64) {
+      k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
+                                                   ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
+    } else {
+      int b = ctx->cur;
+      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->cell[b] + off, ctx->ox[b] + off,
+                                                   ctx->oy[b] + off, ctx->oz[b] + off, ctx->ux[b] + off,
+                                                   ctx->uy[b] + off, ctx->uz[b] + off);
+    }
+    ECS_LAUNCHED(ctx);
+  }
+  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+  ctx->np = np;
+  ctx->attempt_rate = -1.0;
+  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
+    int rc = ecs_part_sort(ctx);
+    if (rc) return rc;
+  }
+  return ECS_OK;
+}
+
+int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
+  const int64_t chunk = 1 << 22;
+  int64_t np = ctx->np;
+  double *stage = nullptr;
+  int64_t cn = np < chunk ? (np > 0 ? np : 1) : chunk;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, (size_t)cn * 6 * sizeof(double), ctx->stream));
+  PartK k = make_k(ctx, 0.0);
+  for (int64_t off = 0; off < np; off += chunk) {
+    int64_t n = np - off < chunk ? np - off : chunk;
+    unsigned int g = grid_blocks(ctx, n, 8);
+    if (ctx->prec == ECS_PREC_FP64) {
+      k_soa_to_aos64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
+                                                   ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
+    } else {
+      int b = ctx->cur;
+      k_mixed_to_aos<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->cell[b] + off, ctx->ox[b] + off,
+                                                   ctx->oy[b] + off, ctx->oz[b] + off, ctx->ux[b] + off,
+                                                   ctx->uy[b] + off, ctx->uz[b] + off);
+    }
+    ECS_LAUNCHED(ctx);
+    if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + 3 * off, stage, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (vel) ECS_CUDA(ctx, cudaMemcpyAsync(vel + 3 * off, stage + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
+}
+
+static int launch_particles(EcsCtx *ctx, double dt, int mode) {
+  if (ctx->np == 0) return ECS_OK;
+  PartK k = make_k(ctx, dt);
+  if ((mode & 2) && k.collide) {
+    if (ctx->attempt_rate < 0) {
+      int rc = ecs_part_estimate_rate(ctx, dt);
+      if (rc) return rc;
+    }
+    k.rate = ctx->attempt_rate;
+    k.p0 = exp(-k.rate);
+    ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  }
+  if (!k.collide) mode &= ~2;
+  unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  if (ctx->prec == ECS_PREC_FP64) {
+    k_particles64<<<g, kBlock, 0, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
+                                                ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
+  } else {
+    int b = ctx->cur;
+    k_particles32<<<g, kBlock, 0, ctx->stream>>>(k, mode, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b],
+                                                ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b],
+                                                ctx->eext32, ctx->acc, ctx->dstat);
+  }
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// After a collision pass: read the counters, update the next pass's rate.
+static int finish_collisions(EcsCtx *ctx, double dt) {
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const EcsDevStatus &s = *ctx->hstat;
+  if (s.acc_count > 0) {
+    double mean = (double)s.acc_fix / 16777216.0 / (double)s.acc_count;
+    int64_t Nc = collision_target(ctx, dt);
+    ctx->attempt_rate = (mean > 0 && ctx->np > 0) ? (double)Nc / ((double)ctx->np * mean) : 0.0;
+  }
+  if (s.refused >= 10) return ecs_fail(ctx, ECS_ERR_COLLISION, "%llu collisions refused (final speed > 10 viT)", s.refused);
+  return ECS_OK;
+}
+
+int ecs_part_estimate_rate(EcsCtx *ctx, double dt) {
+  PartK k = make_k(ctx, dt);
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  if (ctx->prec == ECS_PREC_FP64) {
+    k_estimate64<<<g, kBlock, 0, ctx->stream>>>(k, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy,
+                                               ctx->vz, ctx->dstat);
+  } else {
+    int b = ctx->cur;
+    k_estimate32<<<g, kBlock, 0, ctx->stream>>>(k, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b], ctx->oz[b],
+                                               ctx->ux[b], ctx->uy[b], ctx->uz[b], ctx->dstat);
+  }
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double mean = ctx->hstat->acc_count ? (double)ctx->hstat->acc_fix / 16777216.0 / (double)ctx->hstat->acc_count : 0.0;
+  int64_t Nc = collision_target(ctx, dt);
+  ctx->attempt_rate = (mean > 0 && ctx->np > 0) ? (double)Nc / ((double)ctx->np * mean) : 0.0;
+  return ECS_OK;
+}
+
+int ecs_part_push(EcsCtx *ctx, double dt) { return launch_particles(ctx, dt, 1); }
+int ecs_part_collide(EcsCtx *ctx, double dt) {
+  if (ctx->p.mn <= 0.0) return ECS_OK;
+  int rc = launch_particles(ctx, dt, 2);
+  if (rc) return rc;
+  rc = finish_collisions(ctx, dt);
+  ctx->step_index++;
+  return rc;
+}
+int ecs_part_move(EcsCtx *ctx, double dt) { return launch_particles(ctx, dt, 4); }
+int ecs_part_collect(EcsCtx *ctx) {
+  int rc = ecs_grid_clear_acc(ctx);
+  if (rc) return rc;
+  return launch_particles(ctx, 0.0, 8);
+}
+int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide) {
+  int rc = ecs_grid_clear_acc(ctx);
+  if (rc) return rc;
+  int collide = do_collide && ctx->p.mn > 0.0;
+  rc = launch_particles(ctx, dt, 1 | (collide ? 2 : 0) | 4 | 8);
+  if (rc) return rc;
+  if (collide) {
+    rc = finish_collisions(ctx, dt);
+    ctx->step_index++;
+  }
+  return rc;
+}
+
+int ecs_part_sort(EcsCtx *ctx) {
+  if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0) return ECS_OK;
+  const int n = (int)ctx->ncell;
+  const int nb = (int)ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
+  int a = ctx->cur, b = 1 - ctx->cur;
+  unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+  k_sort_count<<<g, kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->cell[a], ctx->sort_count);
+  ECS_LAUNCHED(ctx);
+  k_scan_local<<<nb, kScanBlock, 0, ctx->stream>>>(n, ctx->sort_count, ctx->sort_offset, ctx->scan_blocks);
+  ECS_LAUNCHED(ctx);
+  k_scan_sums<<<1, 1024, 0, ctx->stream>>>(nb, ctx->scan_blocks);
+  ECS_LAUNCHED(ctx);
+  k_scan_add<<<ecs_div_up(ctx->ncell, 256), 256, 0, ctx->stream>>>(n, ctx->sort_offset, ctx->scan_blocks, nullptr);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+  k_sort_scatter<<<g, kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->sort_offset, ctx->sort_count,
+                                               ctx->cell[a], ctx->ox[a], ctx->oy[a], ctx->oz[a], ctx->ux[a],
+                                               ctx->uy[a], ctx->uz[a], ctx->cell[b], ctx->ox[b], ctx->oy[b],
+                                               ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b]);
+  ECS_LAUNCHED(ctx);
+  ctx->cur = b;
+  ctx->steps_since_sort = 0;
+  return ECS_OK;
+}
