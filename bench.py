@@ -1,0 +1,367 @@
+"""Benchmark of the ECSPRT per-timestep hot path on GB300.
+
+Workload (N=1): 128^3 periodic grid, dx = 1 (normalised), 64 ions per cell
+(134,217,728 ions), initial density 1 + 0.05 sin(2 pi x / Lx), Maxwellian ions
+(per-component thermal speed 1) drifting at 1.0 along x, B along z with ion
+gyrofrequency 0.1, ion-neutral collision frequency 0.02 (Maxwellian neutrals
+at the ion temperature), kappa_e ~ 2, dt = 0.1, variable-coefficient
+potential solve to 1e-8 relative residual.  Mixed path: FP32 cell-sorted
+particles (sorted every 4 steps), FP32 multigrid-FGMRES inside FP64
+iterative refinement.  Synthetic seeded data (no dataset exists for this
+benchmark).
+
+A step is one pass of src/pic.c:244-258: push + collide + move/BC + deposit
++ RHS + operator set-up + solve.  value = ions x steps / device time of the
+timed steps (particles resident in HBM, 7.5 GB >> L2, so no flush is needed).
+e2e = the same metric through the host-buffer C-ABI call ecs_step_host
+(particles copied in and out of pinned host memory every step, plus the
+moments and potential out).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {
+    "name": "128^3 periodic, 64 ions/cell, drift 1.0, nu 0.02, density 1+0.05 sin(2 pi x/Lx)",
+    "n": 128, "ppc": 64, "dt": 0.1, "drift": 1.0, "nu": 0.02, "seed": 20261205,
+}
+ALGO_BYTES_MIXED = 56   # per particle-step: (int32 cell + 3 FP32 offset + 3 FP32 v) read + written
+ALGO_BYTES_FP64 = 96    # per particle-step: 6 FP64 read + written
+
+
+def options(w):
+    n = w["n"]
+    return (f"-Nx {n} -Ny {n} -Nz {n} -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x {w['drift']} "
+            f"-nui {w['nu']} -nue 8.79e9 -Te 11604.5 -E0 0 -Np -{w['ppc']} -dt {w['dt']}")
+
+
+def make_particles(w, count=None):
+    """Seeded synthetic ions: x by rejection on 1 + 0.05 sin(2 pi x/L),
+    y, z uniform, Maxwellian velocities plus the drift along x."""
+    n = w["n"]
+    N = count or n ** 3 * w["ppc"]
+    rng = np.random.default_rng(w["seed"])
+    L = float(n)
+    pos = np.empty((N, 3))
+    got = 0
+    while got < N:
+        m = int((N - got) * 1.06) + 1024
+        x = rng.uniform(0.0, L, m)
+        keep = x[rng.uniform(0.0, 1.05, m) < 1.0 + 0.05 * np.sin(2 * np.pi * x / L)]
+        take = min(keep.size, N - got)
+        pos[got:got + take, 0] = keep[:take]
+        got += take
+    pos[:, 1] = rng.uniform(0.0, L, N)
+    pos[:, 2] = rng.uniform(0.0, L, N)
+    vel = rng.standard_normal((N, 3))
+    vel[:, 0] += w["drift"]
+    return pos, vel
+
+
+def measured_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
+    """The oracle port of the reference's particle phase (push, collide,
+    move + BC, deposit in FP64), timed on the host cores on a bounded sample
+    of the same workload; the potential solve is not included, which only
+    raises the CPU rate."""
+    from oracle import oracle as orc
+    import ecsprt_gb300 as E
+
+    orc.build()
+    p = E.params_from_options(options(w))
+    O = orc.Oracle(p)
+    threads = orc.num_threads()
+    S = min(pos.shape[0], 1 << 21)
+    sp, sv = pos[:S].copy(), vel[:S].copy()
+    dt = w["dt"]
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        sv = O.push(sp, sv, phi, dt)
+        sv, _, _ = O.collide(sv, dt)
+        sp, sv = O.move(sp, sv, dt)
+        O.collect(sp, sv)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_target or steps >= 50:
+            break
+    rate = S * steps / el
+    return {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{S} ions of the workload x {steps} steps of push+collide+move+deposit (FP64, "
+                      f"{threads} OpenMP threads for push/move; serial collide and deposit as in the "
+                      f"reference); the potential solve is excluded"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    w = WORKLOAD
+    pos, vel = make_particles(w, count=1 << 21)
+    phi = np.zeros((w["n"],) * 3)
+    per = []
+    for _ in range(args.warmup):
+        cpu_baseline(w, pos, vel, phi, seconds_target=0.0)
+    for _ in range(args.steps):
+        per.append(cpu_baseline(w, pos, vel, phi, seconds_target=0.0))
+    value = float(np.mean([c["value"] for c in per]))
+    c = dict(per[0])
+    c["value"] = value
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (1 << 21) / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w["name"], "sample_ions": 1 << 21},
+        "cpu_baseline": c,
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import ecsprt_gb300 as E
+
+    w = WORKLOAD
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    p = E.params_from_options(options(w))
+    pos, vel = make_particles(w)
+    N = pos.shape[0]
+    dt = w["dt"]
+    rtol = 1e-8
+
+    # ---------------- device-resident mixed path -----------------------
+    ctx = E.Context(p, E.ECS_PREC_MIXED, np_capacity=N, stream=stream.cuda_stream)
+    ctx.set_sort_every(4)
+    ctx.upload_particles(pos, vel)
+    ctx.collect()
+    ctx.compute_potential(rtol=rtol, max_it=400)
+    for _ in range(args.warmup):
+        ctx.step(dt, rtol, 400)
+    stats = []
+    launches0 = ctx.launches
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            stats.append(ctx.step(dt, rtol, 400))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    el = e0.elapsed_time(e1) * 1e-3
+    el_max = max_over_ranks(el, world)
+    value = N * args.steps * world / el_max
+    part_s = np.array([s.particle_seconds for s in stats])
+    solve_s = np.array([s.solve.seconds for s in stats])
+    sort_s = np.array([s.sort_seconds for s in stats if s.sorted])
+    relres = max(s.solve.relres for s in stats)
+    its = [s.solve.iterations for s in stats]
+    collisions = float(np.mean([s.collisions for s in stats]))
+    peak, peak_kind = measured_peaks()
+    achieved = ALGO_BYTES_MIXED * N / part_s.mean() / 1e9
+    phi_now = ctx.phi
+
+    # ---------------- end to end through host buffers ------------------
+    e2e_steps = max(1, min(3, args.steps))
+    hpos = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hvel = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hmom = torch.empty((p.Nz, p.Ny, p.Nx, 4), dtype=torch.float64, pin_memory=True).numpy()
+    hphi = torch.empty((p.Nz, p.Ny, p.Nx), dtype=torch.float64, pin_memory=True).numpy()
+    hpos[:] = pos
+    hvel[:] = vel
+    ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)  # warm-up
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)
+    e2e_el = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": N * e2e_steps * world / e2e_el, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": 48 * N, "d2h_bytes_per_step": 48 * N + 40 * p.Nx * p.Ny * p.Nz,
+           "steps": e2e_steps, "api": "ecs_step_host"}
+    ctx.close()
+    del hpos, hvel
+
+    # ---------------- plain FP64 GPU path, same workload ---------------
+    plain = None
+    if not args.skip_fp64:
+        ctx64 = E.Context(p, E.ECS_PREC_FP64, np_capacity=N, stream=stream.cuda_stream)
+        ctx64.upload_particles(pos, vel)
+        ctx64.collect()
+        ctx64.compute_potential(rtol=rtol, max_it=400)
+        ctx64.step(dt, rtol, 400)
+        k64 = max(1, min(3, args.steps))
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        st64 = [ctx64.step(dt, rtol, 400) for _ in range(k64)]
+        f1.record(stream)
+        torch.cuda.synchronize()
+        el64 = max_over_ranks(f0.elapsed_time(f1) * 1e-3, world)
+        plain = {"value": N * k64 * world / el64, "ms_per_step": 1e3 * el64 / k64, "steps": k64,
+                 "particle_ms": 1e3 * float(np.mean([s.particle_seconds for s in st64])),
+                 "solve_ms": 1e3 * float(np.mean([s.solve.seconds for s in st64]))}
+        ctx64.close()
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(w, pos, vel, phi_now) if not args.skip_cpu else None
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": w["name"], "grid": [w["n"]] * 3, "ions": N, "ppc": w["ppc"], "dt": dt,
+                   "precision": "mixed (FP32 particles + FP32 MG-FGMRES inside FP64 refinement)",
+                   "solve_rtol": rtol, "sort_every": 4,
+                   "l2": "inputs larger than L2 (7.5 GB of particles per step)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": "k_particles32 (fused push+collide+move+deposit)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": ALGO_BYTES_MIXED * N},
+        "solve_latency_ms": {"p50": 1e3 * float(np.percentile(solve_s, 50)),
+                             "p99": 1e3 * float(np.percentile(solve_s, 99)),
+                             "iterations": its, "max_relres": relres},
+        "phase_ms": {"particles": 1e3 * float(part_s.mean()), "solve": 1e3 * float(solve_s.mean()),
+                     "sort": 1e3 * float(sort_s.mean()) if sort_s.size else 0.0},
+        "collisions_per_step": collisions,
+        "plain_fp64": plain,
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup() if args.impl == "ours" else (
+        int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        from ecsprt_gb300 import build
+
+        build.build()
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -69,7 +69,8 @@ class EcsSolveStats(C.Structure):
 
 
 class EcsStepStats(C.Structure):
-    _fields_ = [("collisions", C.c_int64), ("refused", C.c_int64), ("sorted", C.c_int32), ("solve", EcsSolveStats)]
+    _fields_ = [("collisions", C.c_int64), ("refused", C.c_int64), ("sorted", C.c_int32), ("solve", EcsSolveStats),
+                ("particle_seconds", C.c_double), ("sort_seconds", C.c_double)]
 
 
 class EcsPicApp(C.Structure):

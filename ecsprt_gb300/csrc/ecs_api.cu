@@ -167,6 +167,7 @@ int ecs_ctx_create(const EcsParams *params, int precision, int64_t np_capacity, 
     ecs_ctx_destroy(ctx);
     return ECS_ERR_NOMEM;
   }
+  for (int q = 0; q < 4; q++) cudaEventCreate(&ctx->ev[q]);
   cudaMemsetAsync(ctx->phi, 0, ctx->ncell * sizeof(double), ctx->stream);
   cudaMemsetAsync(ctx->mom, 0, ctx->ncell * 4 * sizeof(double), ctx->stream);
   cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream);
@@ -195,6 +196,8 @@ int ecs_ctx_destroy(EcsCtx *ctx) {
   for (void *q : ptrs)
     if (q) cudaFree(q);
   if (ctx->hstat) cudaFreeHost(ctx->hstat);
+  for (int q = 0; q < 4; q++)
+    if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return ECS_OK;
@@ -372,6 +375,7 @@ int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stat
   int rc = ensure_eext(ctx, ctx->eext_ready);
   if (rc) return rc;
   int sorted = 0;
+  ctx->ev_particle = ctx->ev_sort = false;
   if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ctx->steps_since_sort >= ctx->sort_every) {
     if ((rc = ecs_part_sort(ctx))) return rc;
     sorted = 1;
@@ -394,6 +398,11 @@ int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stat
     stats->refused = (int64_t)coll.refused;
     stats->sorted = sorted;
     stats->solve = st;
+    float ms = 0.f;
+    cudaStreamSynchronize(ctx->stream);
+    stats->particle_seconds = (ctx->ev_particle && cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ? ms * 1e-3 : 0.0;
+    ms = 0.f;
+    stats->sort_seconds = (ctx->ev_sort && cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]) == cudaSuccess) ? ms * 1e-3 : 0.0;
   }
   return rc;
 }

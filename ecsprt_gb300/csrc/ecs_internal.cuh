@@ -118,6 +118,9 @@ struct EcsCtx {
 
   int64_t launches = 0;
   std::string err;
+  // events around the particle kernel [0,1] and the sort [2,3] of a step
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_particle = false, ev_sort = false;
 };
 
 // ---- error helpers -------------------------------------------------------

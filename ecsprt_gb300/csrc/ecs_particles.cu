@@ -176,27 +176,32 @@ __device__ __forceinline__ T accept_prob(T a) {
 }
 
 // One ion's collisions in one pass (src/collisions.c:70-157).  Returns the
-// acceptance probability sample used to estimate the next pass's rate.
+// acceptance-probability sample (or -1 when this ion is not in the 1/16
+// hash-selected subsample that estimates the next pass's rate).
 template <typename T>
 __device__ float collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &vy, T &vz,
                              unsigned int &nacc, unsigned int &nref) {
   typedef RMath<T> M;
-  // acceptance sample for the rate estimate (uses pre-collision velocity)
-  EcsU4 e = ecs_philox({h0, h1, 0xFFFFFFFEu, k.step}, k.key0, k.key1);
-  T r1 = M::sqrt_(T(-2) * M::log_(M::u01(e.x, e.y)));
-  T s1, c1, s2, c2;
-  M::sincospi_(T(2) * M::u01(e.z, e.w), &s1, &c1);
-  EcsU4 e2 = ecs_philox({h0, h1, 0xFFFFFFFDu, k.step}, k.key0, k.key1);
-  T r2 = M::sqrt_(T(-2) * M::log_(M::u01(e2.x, e2.y)));
-  M::sincospi_(T(2) * M::u01(e2.z, e2.w), &s2, &c2);
-  T wx = vx - (T(r1 * c1) * T(k.vnT) + T(k.vn0[0]));
-  T wy = vy - (T(r1 * s1) * T(k.vnT) + T(k.vn0[1]));
-  T wz = vz - (T(r2 * c2) * T(k.vnT) + T(k.vn0[2]));
-  float sample = (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
+  float sample = -1.0f;
+  if ((h0 & 15u) == 0u) {
+    // acceptance sample for the rate estimate (pre-collision velocity)
+    EcsU4 e = ecs_philox({h0, h1, 0xFFFFFFFEu, k.step}, k.key0, k.key1);
+    T r1 = M::sqrt_(T(-2) * M::log_(M::u01(e.x, e.y)));
+    T s1, c1, s2, c2;
+    M::sincospi_(T(2) * M::u01(e.z, e.w), &s1, &c1);
+    EcsU4 e2 = ecs_philox({h0, h1, 0xFFFFFFFDu, k.step}, k.key0, k.key1);
+    T r2 = M::sqrt_(T(-2) * M::log_(M::u01(e2.x, e2.y)));
+    M::sincospi_(T(2) * M::u01(e2.z, e2.w), &s2, &c2);
+    T wx = vx - (T(r1 * c1) * T(k.vnT) + T(k.vn0[0]));
+    T wy = vy - (T(r1 * s1) * T(k.vnT) + T(k.vn0[1]));
+    T wz = vz - (T(r2 * c2) * T(k.vnT) + T(k.vn0[2]));
+    sample = (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
+  }
 
-  // number of attempts ~ Poisson(rate), by inversion
-  EcsU4 pz = ecs_philox({h0, h1, 0xFFFFFFFFu, k.step}, k.key0, k.key1);
-  T u = M::u01(pz.x, pz.y);
+  // number of attempts ~ Poisson(rate), by inversion of a uniform drawn from
+  // the state hash mixed with the step and seed
+  uint32_t hu = ecs_mix32(h1 ^ ecs_mix32(k.step * 0x9E3779B9u ^ k.key0) ^ k.key1);
+  T u = M::u01(hu, ecs_mix32(hu ^ h0));
   T p = T(k.p0), cdf = p, rate = T(k.rate);
   int natt = 0;
   while (u > cdf && natt < 16) {
@@ -267,8 +272,9 @@ __device__ __forceinline__ void flush_counts(EcsDevStatus *st, unsigned int nacc
   if (!collide) return;
   unsigned int a = __reduce_add_sync(ECS_FULL_MASK, nacc);
   unsigned int r = __reduce_add_sync(ECS_FULL_MASK, nref);
-  unsigned int f = __reduce_add_sync(ECS_FULL_MASK, active ? (unsigned int)__float2uint_rn(sample * 16777216.0f) : 0u);
-  unsigned int n = __popc(__ballot_sync(ECS_FULL_MASK, active));
+  const bool has = active && sample >= 0.0f;
+  unsigned int f = __reduce_add_sync(ECS_FULL_MASK, has ? (unsigned int)__float2uint_rn(sample * 16777216.0f) : 0u);
+  unsigned int n = __popc(__ballot_sync(ECS_FULL_MASK, has));
   if ((threadIdx.x & 31) == 0) {
     if (a) atomicAdd(&st->collisions, (unsigned long long)a);
     if (r) atomicAdd(&st->refused, (unsigned long long)r);
@@ -993,6 +999,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode) {
   }
   if (!k.collide) mode &= ~2;
   unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
   if (ctx->prec == ECS_PREC_FP64) {
     k_particles64<<<g, kBlock, 0, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                                 ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
@@ -1003,6 +1010,10 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode) {
                                                 ctx->eext32, ctx->acc, ctx->dstat);
   }
   ECS_LAUNCHED(ctx);
+  if (ctx->ev[1]) {
+    cudaEventRecord(ctx->ev[1], ctx->stream);
+    ctx->ev_particle = true;
+  }
   return ECS_OK;
 }
 
@@ -1075,6 +1086,7 @@ int ecs_part_sort(EcsCtx *ctx) {
   const int nb = (int)ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
   int a = ctx->cur, b = 1 - ctx->cur;
   unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  if (ctx->ev[2]) cudaEventRecord(ctx->ev[2], ctx->stream);
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
   k_sort_count<<<g, kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->cell[a], ctx->sort_count);
   ECS_LAUNCHED(ctx);
@@ -1090,6 +1102,10 @@ int ecs_part_sort(EcsCtx *ctx) {
                                                ctx->uy[a], ctx->uz[a], ctx->cell[b], ctx->ox[b], ctx->oy[b],
                                                ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b]);
   ECS_LAUNCHED(ctx);
+  if (ctx->ev[3]) {
+    cudaEventRecord(ctx->ev[3], ctx->stream);
+    ctx->ev_sort = true;
+  }
   ctx->cur = b;
   ctx->steps_since_sort = 0;
   return ECS_OK;

@@ -97,6 +97,8 @@ typedef struct EcsStepStats {
   int64_t refused;        /* collisions refused (final speed > 10 viT) */
   int32_t sorted;         /* 1 if the particles were cell-sorted this step */
   EcsSolveStats solve;
+  double particle_seconds;/* device time of the fused particle kernel (CUDA events) */
+  double sort_seconds;    /* device time of the cell sort (0 if none) */
 } EcsStepStats;
 
 /* ---- library ------------------------------------------------------------ */

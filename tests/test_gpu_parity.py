@@ -1,0 +1,344 @@
+"""GPU parity: libecsgpu (through its C ABI) against the oracle and the
+reference's golden vectors.
+
+Tolerances:
+  FP64 plain path
+    push, move               bit-exact (same FP64 operations, no FMA)
+    deposit                  bit-exact against the oracle's fixed-point
+                             deposit (2^-44 grid); <= 1e-13 relative against
+                             the reference's FP64 particle-order sums
+    RHS                      <= 1e-14 relative (only the mean's summation
+                             order differs)
+    operator apply           <= 1e-13 relative
+    potential                relres <= requested rtol (FP64-measured);
+                             phi relative L2 <= 1e-8 against the oracle's
+                             1e-13 solve when solved to 1e-11
+  Mixed path (FP32 particles, FP32 multigrid inside FP64 refinement)
+    push velocities          <= 2e-6 * max|v|
+    positions                <= 2e-6 cell widths
+    density                  <= 1e-6 relative (L-infinity / max)
+    potential                relres <= 1e-8 (FP64-measured)
+"""
+import numpy as np
+import pytest
+
+import ecsprt_gb300 as E
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def params_for(golden_case):
+    return E.params_from_options(golden_case["opts"])
+
+
+def new_ctx(g, prec, np_=None, sort_every=0):
+    p = params_for(g)
+    n = np_ if np_ is not None else g["pos0"].shape[0]
+    ctx = E.Context(p, prec, np_capacity=max(n, 1))
+    ctx.set_sort_every(sort_every)
+    return ctx
+
+
+def rel_inf(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def bit_equal(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    bad = np.flatnonzero(a.ravel() != b.ravel())
+    assert bad.size == 0, f"{bad.size}/{a.size} differ, first {bad[:4]}: {a.ravel()[bad[:4]]} vs {b.ravel()[bad[:4]]}"
+
+
+CASES = ["c1", "edge", "fb"]
+
+
+# ---------------------------------------------------------------- FP64 plain
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_push_bit_exact(built, golden, case):
+    g = golden[case]
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        ctx.upload_particles(g["pos0"], g["vel0"])
+        ctx.phi = g["phi"]
+        ctx.push(float(g["dt"]))
+        pos, vel = ctx.download_particles()
+    bit_equal(pos, g["pos0"])
+    bit_equal(vel, g["vel_push"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_move_bit_exact(built, golden, case):
+    g = golden[case]
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        ctx.upload_particles(g["pos0"], g["vel_push"])
+        ctx.update_positions(float(g["dt"]))
+        pos, vel = ctx.download_particles()
+    bit_equal(pos, g["pos_move"])
+    bit_equal(vel, g["vel_move"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_deposit(built, golden, case):
+    g = golden[case]
+    O = orc.Oracle(g["params"])
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        ctx.upload_particles(g["pos_move"], g["vel_move"])
+        ctx.collect()
+        m = ctx.moments
+    fixed, _ = O.collect_fixed(g["pos_move"], g["vel_move"], 44)
+    bit_equal(m, fixed)
+    assert rel_inf(m, g["moments"]) <= 1e-13
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_rhs(built, golden, case):
+    g = golden[case]
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        ctx.moments = g["moments"]
+        ctx.compute_rhs()
+        b = ctx.rhs
+    assert rel_inf(b, g["rhs"]) <= 1e-14
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_operator_apply(built, golden, case):
+    g = golden[case]
+    O = orc.Oracle(g["params"])
+    x = np.random.RandomState(3).standard_normal(O.shape)
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        ctx.moments = g["moments"]
+        y = ctx.lhs_apply(x)
+    yo = O.lhs_apply(g["moments"][..., 0], x)
+    assert rel_inf(y, yo) <= 1e-13
+
+
+@pytest.mark.parametrize("prec", [E.ECS_PREC_FP64, E.ECS_PREC_MIXED])
+@pytest.mark.parametrize("case", ["c1", "fb"])
+def test_solve(built, golden, case, prec):
+    g = golden[case]
+    O = orc.Oracle(g["params"])
+    phi_o, its, rel = O.solve(g["moments"][..., 0], g["rhs"], rtol=1e-13)
+    assert rel <= 1e-13
+    rtol = 1e-11 if prec == E.ECS_PREC_FP64 else 1e-8
+    with new_ctx(g, prec) as ctx:
+        ctx.moments = g["moments"]
+        st = ctx.compute_potential(rtol=rtol, max_it=400)
+        phi = ctx.phi
+    assert st.relres <= rtol
+    # independent FP64 residual of the GPU potential with the oracle operator
+    r = g["rhs"] - O.lhs_apply(g["moments"][..., 0], phi)
+    assert np.linalg.norm(r) / np.linalg.norm(g["rhs"]) <= 2 * rtol
+    if prec == E.ECS_PREC_FP64:
+        assert np.linalg.norm(phi - phi_o) / np.linalg.norm(phi_o) <= 1e-8
+
+
+# ---------------------------------------------------------------- mixed path
+@pytest.mark.parametrize("case", CASES)
+def test_mixed_push(built, golden, case):
+    g = golden[case]
+    with new_ctx(g, E.ECS_PREC_MIXED) as ctx:
+        ctx.upload_particles(g["pos0"], g["vel0"])
+        ctx.phi = g["phi"]
+        ctx.push(float(g["dt"]))
+        _, vel = ctx.download_particles()
+    assert np.abs(vel - g["vel_push"]).max() <= 2e-6 * np.abs(g["vel_push"]).max()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mixed_move_and_deposit(built, golden, case):
+    g = golden[case]
+    p = g["params"]
+    with new_ctx(g, E.ECS_PREC_MIXED) as ctx:
+        ctx.upload_particles(g["pos0"], g["vel_push"])
+        ctx.update_positions(float(g["dt"]))
+        pos, vel = ctx.download_particles()
+        ctx.collect()
+        m = ctx.moments
+    L = np.array([p["Lx"], p["Ly"], p["Lz"]])
+    d = np.abs(pos - g["pos_move"])
+    d = np.minimum(d, L - d)  # periodic distance
+    assert (d / np.array([p["dx"], p["dy"], p["dz"]])).max() <= 2e-6
+    assert rel_inf(m[..., 0], g["moments"][..., 0]) <= 1e-6
+    assert rel_inf(m, g["moments"]) <= 1e-5
+
+
+# ---------------------------------------------------------------- full steps
+def c1_like(n=16, ppc=8, mn=True, seed=7):
+    opts = (f"-Nx {n} -Ny {n} -Nz {n} -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 0.5 "
+            f"-nui 0.05 -nue 8.79e9 -Te 11604.5 -E0 0 " + ("" if mn else "-mn 0 "))
+    p = E.params_from_options(opts)
+    rng = np.random.RandomState(seed)
+    npart = ppc * n ** 3
+    pos = rng.uniform(0, n, (npart, 3))
+    pos[:, 0] = (pos[:, 0] + 0.3 * np.sin(2 * np.pi * pos[:, 1] / n)) % n  # density structure
+    vel = rng.standard_normal((npart, 3)) + [0.5, 0, 0]
+    return opts, p, pos, vel
+
+
+def oracle_step(O, pos, vel, phi, dt):
+    vel = O.push(pos, vel, phi, dt)
+    pos, vel = O.move(pos, vel, dt)
+    m = O.collect(pos, vel)
+    b = O.rhs(m)
+    phi, _, rel = O.solve(m[..., 0], b, rtol=1e-13)
+    return pos, vel, m, phi
+
+
+def test_fp64_steps_track_oracle(built):
+    opts, p, pos, vel = c1_like(n=8, ppc=8, mn=False)
+    O = orc.Oracle(p)
+    dt = 0.1
+    op, ov = pos.copy(), vel.copy()
+    m0 = O.collect(op, ov)
+    ophi, _, _ = O.solve(m0[..., 0], O.rhs(m0), rtol=1e-13)
+    with E.Context(p, E.ECS_PREC_FP64, np_capacity=pos.shape[0]) as ctx:
+        ctx.upload_particles(pos, vel)
+        ctx.phi = ophi
+        for _ in range(5):
+            st = ctx.step(dt, rtol=1e-12, max_it=400)
+            assert st.solve.relres <= 1e-12
+            op, ov, om, ophi = oracle_step(O, op, ov, ophi, dt)
+        gp, gv = ctx.download_particles()
+        gm = ctx.moments
+        gphi = ctx.phi
+    assert rel_inf(gv, ov) <= 1e-10
+    L = p.Lx
+    d = np.abs(gp - op)
+    assert np.minimum(d, L - d).max() <= 1e-10 * L
+    assert rel_inf(gm, om) <= 1e-12
+    assert np.linalg.norm(gphi - ophi) / np.linalg.norm(ophi) <= 1e-8
+
+
+def test_mixed_step_matches_fp64(built):
+    opts, p, pos, vel = c1_like(n=16, ppc=8, mn=False)
+    res = {}
+    for prec in (E.ECS_PREC_FP64, E.ECS_PREC_MIXED):
+        with E.Context(p, prec, np_capacity=pos.shape[0]) as ctx:
+            ctx.upload_particles(pos, vel)
+            ctx.collect()
+            ctx.compute_potential(rtol=1e-10, max_it=400)
+            for _ in range(3):
+                st = ctx.step(0.1, rtol=1e-8, max_it=400)
+                assert st.solve.relres <= 1e-8
+            res[prec] = (ctx.moments, ctx.phi)
+    assert rel_inf(res[1][0][..., 0], res[0][0][..., 0]) <= 1e-5
+    assert np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1]) <= 1e-4
+
+
+def test_mixed_deterministic_with_collisions(built):
+    opts, p, pos, vel = c1_like(n=16, ppc=8, mn=True)
+    outs = []
+    for rep in range(2):
+        with E.Context(p, E.ECS_PREC_MIXED, np_capacity=pos.shape[0]) as ctx:
+            ctx.set_sort_every(2)
+            ctx.upload_particles(pos, vel)
+            ctx.collect()
+            ctx.compute_potential(rtol=1e-8, max_it=400)
+            for _ in range(4):
+                st = ctx.step(0.1, rtol=1e-8, max_it=400)
+                assert st.collisions > 0
+            outs.append((ctx.moments, ctx.phi))
+    bit_equal(outs[0][0], outs[1][0])
+    bit_equal(outs[0][1], outs[1][1])
+
+
+def test_deposit_order_independent(built):
+    opts, p, pos, vel = c1_like(n=16, ppc=8, mn=False)
+    perm = np.random.RandomState(1).permutation(pos.shape[0])
+    res = []
+    for prec in (E.ECS_PREC_FP64, E.ECS_PREC_MIXED):
+        ms = []
+        for order in (np.arange(pos.shape[0]), perm):
+            with E.Context(p, prec, np_capacity=pos.shape[0]) as ctx:
+                ctx.set_sort_every(0)
+                ctx.upload_particles(pos[order], vel[order])
+                ctx.collect()
+                ms.append(ctx.moments)
+        bit_equal(ms[0], ms[1])
+
+
+def test_sorting_preserves_particles(built):
+    opts, p, pos, vel = c1_like(n=16, ppc=8, mn=False)
+    got = []
+    for every in (0, 1):
+        with E.Context(p, E.ECS_PREC_MIXED, np_capacity=pos.shape[0]) as ctx:
+            ctx.set_sort_every(every)
+            ctx.upload_particles(pos, vel)
+            ctx.collect()
+            ctx.compute_potential(rtol=1e-8, max_it=400)
+            for _ in range(3):
+                ctx.step(0.1, rtol=1e-8, max_it=400)
+            gp, gv = ctx.download_particles()
+            got.append(np.c_[gp, gv])
+    a = got[0][np.lexsort(got[0].T[::-1])]
+    b = got[1][np.lexsort(got[1].T[::-1])]
+    bit_equal(a, b)
+
+
+# ---------------------------------------------------------------- collisions
+@pytest.mark.parametrize("prec", [E.ECS_PREC_FP64, E.ECS_PREC_MIXED])
+def test_collisions_statistics(built, prec):
+    """One ScatterElastic call on the GPU against the reference algorithm
+    (oracle) from the same velocities: number of collisions, velocity
+    moments, and two-sample KS tests of the velocity components."""
+    stats = pytest.importorskip("scipy.stats")
+    n = 16
+    opts = (f"-Nx {n} -Ny {n} -Nz {n} -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 0.5 "
+            f"-nui 2.0 -nue 8.79e9 -Te 11604.5 -E0 0")
+    p = E.params_from_options(opts)
+    rng = np.random.RandomState(11)
+    npart = 64 * n ** 3
+    pos = rng.uniform(0, n, (npart, 3))
+    vel = rng.standard_normal((npart, 3)) + [1.5, 0, 0]
+    dt = 0.1
+    O = orc.Oracle(p)
+    orc.rng_reset()
+    vo, ns, _ = O.collide(vel, dt)
+    Nc = O.collision_count(npart, dt)
+    with E.Context(p, prec, np_capacity=npart) as ctx:
+        ctx.set_sort_every(0)
+        ctx.upload_particles(pos, vel)
+        ctx.collide(dt)
+        _, vg = ctx.download_particles()
+    changed_g = np.any(vg != vel, axis=1).sum() if prec == E.ECS_PREC_FP64 else np.any(np.abs(vg - vel) > 1e-5, axis=1).sum()
+    changed_o = np.any(vo != vel, axis=1).sum()
+    # expected number of collisions Nc, Poisson-like fluctuation
+    assert abs(changed_g - changed_o) <= 6 * np.sqrt(Nc) + 0.02 * Nc
+    for d in range(3):
+        assert abs(vg[:, d].mean() - vo[:, d].mean()) <= 6 * vo[:, d].std() / np.sqrt(npart)
+        assert abs(vg[:, d].var() / vo[:, d].var() - 1) <= 0.01
+        assert stats.ks_2samp(vg[:, d], vo[:, d]).pvalue > 1e-3
+    sg = np.linalg.norm(vg, axis=1)
+    so = np.linalg.norm(vo, axis=1)
+    assert stats.ks_2samp(sg, so).pvalue > 1e-3
+
+
+# ---------------------------------------------------------------- status codes
+def test_error_status(built, golden):
+    g = golden["c1"]
+    p = params_for(g)
+    bad = E.EcsParams.from_buffer_copy(p)
+    bad.Nx = 2
+    with pytest.raises(E.EcsError) as ei:
+        E.Context(bad, E.ECS_PREC_FP64, 10)
+    assert ei.value.code == -1
+    with new_ctx(g, E.ECS_PREC_FP64) as ctx:
+        with pytest.raises(E.EcsError) as ei:
+            ctx.solve(1e-8, 10)
+        assert ei.value.code == -9
+        vel = g["vel0"].copy()
+        vel[3, 1] = np.nan
+        ctx.upload_particles(g["pos0"], vel)
+        ctx.phi = g["phi"]
+        with pytest.raises(E.EcsError) as ei:
+            ctx.push(0.1)
+        assert ei.value.code == -4
+        ctx.moments = g["moments"]
+        ctx.compute_rhs()
+        ctx.compute_lhs()
+        with pytest.raises(E.EcsError) as ei:
+            ctx.solve(1e-14, 1)
+        assert ei.value.code == -3
