@@ -155,7 +155,7 @@ def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
         sv = O.push(sp, sv, phi, dt)
         sv, _, _ = O.collide(sv, dt)
         sp, sv = O.move(sp, sv, dt)
-        O.collect(sp, sv)
+        O.collect_mt(sp, sv)
         steps += 1
         el = time.perf_counter() - t0
         if el > seconds_target or steps >= 50:
@@ -163,8 +163,8 @@ def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
     rate = S * steps / el
     return {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
             "sample": f"{S} ions of the workload x {steps} steps of push+collide+move+deposit (FP64, "
-                      f"{threads} OpenMP threads for push/move; serial collide and deposit as in the "
-                      f"reference); the potential solve is excluded"}
+                      f"{threads} OpenMP threads for push, move and deposit (per-thread grids as per-rank "
+                      f"local arrays); collide serial as in the reference); the potential solve is excluded"}
 
 
 def dist_setup():

@@ -37,6 +37,7 @@ CC_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-Wno-unused-param
 
 GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu"]
 HOST_SOURCES = ["ecs_options.c", "ecs_io.c"]
+GPU_HOST_SOURCES = ["ecs_ops.c"]  # host C linked into libecsgpu (operator slots)
 
 LIBGPU = OUT / "libecsgpu.so"
 LIBHOST = OUT / "libecshost.so"
@@ -82,6 +83,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict:
         gpu_objs.append(obj)
     host_objs = []
     cc = shutil.which("gcc") or "cc"
+    for src in GPU_HOST_SOURCES:
+        s = HOST / src
+        obj = OUT / (s.stem + ".gpuhost.o")
+        flags = CC_FLAGS + ["-c", str(s), "-o", str(obj)]
+        tasks.append(([cc] + flags, obj, OUT / (s.stem + ".gpuhost.stamp"), _digest([s] + headers, flags)))
+        gpu_objs.append(obj)
     for src in HOST_SOURCES:
         s = HOST / src
         obj = OUT / (s.stem + ".host.o")

@@ -55,6 +55,7 @@ def lib():
             "orc_move": (C.c_int, [P, C.c_int, vp, vp, C.c_double]),
             "orc_collect": (C.c_int, [P, C.c_int, vp, vp, vp]),
             "orc_collect_fixed": (C.c_int, [P, C.c_int, vp, vp, C.c_int, vp, vp]),
+            "orc_collect_mt": (C.c_int, [P, C.c_int, vp, vp, vp]),
             "orc_rhs": (C.c_int, [P, vp, vp]),
             "orc_lhs_dense": (C.c_int, [P, vp, vp]),
             "orc_lhs_apply": (C.c_int, [P, vp, vp, vp]),
@@ -141,6 +142,13 @@ class Oracle:
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         out = np.zeros(self.shape + (4,))
         self.L.orc_collect(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(out))
+        return out
+
+    def collect_mt(self, pos, vel):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        out = np.zeros(self.shape + (4,))
+        self.L.orc_collect_mt(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(out))
         return out
 
     def collect_fixed(self, pos, vel, shift):
