@@ -273,24 +273,26 @@ def run_ours(args, world, rank, local):
     phi_now = ctx.phi
 
     # ---------------- end to end through host buffers ------------------
-    e2e_steps = max(1, min(3, args.steps))
-    hpos = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
-    hvel = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
-    hmom = torch.empty((p.Nz, p.Ny, p.Nx, 4), dtype=torch.float64, pin_memory=True).numpy()
-    hphi = torch.empty((p.Nz, p.Ny, p.Nx), dtype=torch.float64, pin_memory=True).numpy()
-    hpos[:] = pos
-    hvel[:] = vel
-    ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)  # warm-up
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)
-    e2e_el = max_over_ranks(time.perf_counter() - t0, world)
-    e2e = {"value": N * e2e_steps * world / e2e_el, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": 48 * N, "d2h_bytes_per_step": 48 * N + 40 * p.Nx * p.Ny * p.Nz,
-           "steps": e2e_steps, "api": "ecs_step_host"}
+    e2e = None
+    e2e_steps = 0 if args.no_e2e else max(1, min(3, args.steps))
+    if e2e_steps:
+        hpos = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+        hvel = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
+        hmom = torch.empty((p.Nz, p.Ny, p.Nx, 4), dtype=torch.float64, pin_memory=True).numpy()
+        hphi = torch.empty((p.Nz, p.Ny, p.Nx), dtype=torch.float64, pin_memory=True).numpy()
+        hpos[:] = pos
+        hvel[:] = vel
+        ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)  # warm-up
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)
+        e2e_el = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": N * e2e_steps * world / e2e_el, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 48 * N, "d2h_bytes_per_step": 48 * N + 40 * p.Nx * p.Ny * p.Nz,
+               "steps": e2e_steps, "api": "ecs_step_host"}
+        del hpos, hvel
     ctx.close()
-    del hpos, hvel
 
     # ---------------- plain FP64 GPU path, same workload ---------------
     plain = None
@@ -351,7 +353,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--grid", type=int, default=None, help="profiling only: smaller cube edge")
+    ap.add_argument("--ppc", type=int, default=None, help="profiling only: ions per cell")
     args = ap.parse_args()
+    if args.grid:
+        WORKLOAD["n"] = args.grid
+        WORKLOAD["name"] = WORKLOAD["name"].replace("128^3", f"{args.grid}^3")
+    if args.ppc:
+        WORKLOAD["ppc"] = args.ppc
+        WORKLOAD["name"] = WORKLOAD["name"].replace("64 ions/cell", f"{args.ppc} ions/cell")
     world, rank, local = dist_setup() if args.impl == "ours" else (
         int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
     if args.impl == "reference":

@@ -239,10 +239,17 @@ __device__ float collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T 
     T sphi, cphi;
     M::sincospi_(T(2) * M::u01(q2.w, q2.w), &sphi, &cphi);
     T u0x = uperp * cphi, u0y = uperp * sphi;
+    // frame of the incident relative velocity; when it lies along z (where
+    // the reference divides 0 by 0) any azimuth is valid for an isotropic
+    // scattering vector, so phi = 0 is used
     T costht = vr[2] / vrr;
-    T sintht = M::sqrt_(T(1) - costht * costht);
-    T cosphi = vr[0] / (vrr * sintht);
-    T sinphi = vr[1] / (vrr * sintht);
+    T s2 = T(1) - costht * costht;
+    T sintht = s2 > T(0) ? M::sqrt_(s2) : T(0);
+    T cosphi = T(1), sinphi = T(0);
+    if (sintht > T(0)) {
+      cosphi = vr[0] / (vrr * sintht);
+      sinphi = vr[1] / (vrr * sintht);
+    }
     T u1x = u0z * sintht + u0x * costht;
     T u1y = u0y;
     T u1z = u0z * costht - u0x * sintht;

@@ -312,8 +312,10 @@ def test_collisions_statistics(built, prec):
     (isotropic centre-of-mass scattering) the call."""
     stats = pytest.importorskip("scipy.stats")
     vel, vo, vg, co, cg, Nc = _collide_both(prec, nui=0.05, drift=1.0)
-    assert abs(cg.sum() - Nc) <= 5 * np.sqrt(Nc) + 0.01 * Nc, (cg.sum(), co.sum(), Nc)
-    assert abs(co.sum() - Nc) <= 0.01 * Nc + 3
+    assert abs(cg.sum() - co.sum()) <= 5 * np.sqrt(Nc) + 0.01 * Nc, (cg.sum(), co.sum(), Nc)
+    # the reference samples ions with replacement: ~Nc^2/(2 np) ions are hit twice
+    dup = Nc * Nc / (2.0 * vel.shape[0])
+    assert Nc - 3 * dup - 5 * np.sqrt(dup) - 3 <= co.sum() <= Nc
     for d in range(3):
         assert stats.ks_2samp(vel[cg, d], vel[co, d]).pvalue > 1e-3, ("selection", d)
         assert stats.ks_2samp(vg[cg, d], vo[co, d]).pvalue > 1e-3, ("scattered", d)
