@@ -113,6 +113,7 @@ GPU_API = [
     ("ecs_lhs", C.c_int, [_vp]),
     ("ecs_solve", C.c_int, [_vp, C.c_double, C.c_int, C.c_int, C.POINTER(EcsSolveStats)]),
     ("ecs_lhs_apply_host", C.c_int, [_vp, _vp, _vp]),
+    ("ecs_rhs_noalloc", C.c_int, [C.POINTER(EcsParams), _vp, _vp, _vp]),
     ("ecs_step", C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.POINTER(EcsStepStats)]),
     ("ecs_step_host", C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_double, C.c_int, _vp, _vp,
                                 C.POINTER(EcsStepStats)]),

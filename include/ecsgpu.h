@@ -153,6 +153,22 @@ int ecs_solve(EcsCtx *ctx, double rtol, int max_it, int warm_start, EcsSolveStat
 /* y = A x with the current operator, host FP64 arrays (test hook). */
 int ecs_lhs_apply_host(EcsCtx *ctx, const double *x, double *y);
 
+/* RHS for callers that cannot allocate device memory (no counterpart in the
+   reference; it computes what ecs_rhs computes).  For code that owns all of
+   its device memory in its own pool and may not call cudaMalloc inside its
+   step loop, or cannot accept the device synchronisation an allocation may
+   cause: no allocation of any kind is made.  d_moments (device, FluidNode
+   {n,Gx,Gy,Gz} per node, [Nz][Ny][Nx][4]) and d_rhs (device, [Nz][Ny][Nx])
+   belong to the caller; the work is queued on `stream` (a cudaStream_t,
+   NULL for the default stream).  Its reduction scratch is a fixed 32 KiB
+   __device__ array held by every device that loads the library, so grids of
+   more than 8,388,608 nodes (256 x 256 x 128) are rejected with
+   ECS_ERR_INVALID.  The first call on a device looks up the array's device
+   address (cudaGetSymbolAddress); make that first call before any stream
+   capture.  Calls share the scratch: calls that overlap on the GPU race.
+   Errors are reported by ecs_last_error(NULL). */
+int ecs_rhs_noalloc(const EcsParams *params, const double *d_moments, double *d_rhs, void *stream);
+
 /* One time step of src/pic.c:244-258: push, collide (if mn > 0), move + BC,
    collect, rhs, lhs, solve.  In the mixed path push..collect run as one fused
    kernel over the cell-sorted particles. */
