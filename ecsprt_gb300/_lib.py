@@ -118,6 +118,7 @@ GPU_API = [
     ("ecs_step_host", C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_double, C.c_double, C.c_int, _vp, _vp,
                                 C.POINTER(EcsStepStats)]),
     ("ecs_launch_count", C.c_int64, [_vp]),
+    ("ecs_fix_shifts", C.c_int, [C.POINTER(EcsParams), C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 ]
 
 HOST_API = [

@@ -131,6 +131,7 @@ int ecs_ctx_create(const EcsParams *params, int precision, int64_t np_capacity, 
   ctx->cap = np_capacity;
   ctx->ncell = (size_t)params->Nx * params->Ny * params->Nz;
   ctx->next = (size_t)(params->Nx + 1) * (params->Ny + 1) * (params->Nz + 1);
+  ecs_fix_shifts(params, precision, &ctx->shift_n, &ctx->shift_f);
   cudaError_t ce = cudaGetDevice(&ctx->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device);
   if (ce != cudaSuccess) {
@@ -423,5 +424,19 @@ int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, 
 }
 
 int64_t ecs_launch_count(const EcsCtx *ctx) { return ctx ? ctx->launches : -1; }
+
+// Velocity bound 2^e_v: sixteen times the thermal speed plus drift,
+// rounded up to a power of two; the flux quantum is 2^-(S - e_v).
+int ecs_fix_shifts(const EcsParams *p, int precision, int32_t *shift_density, int32_t *shift_flux) {
+  if (!p || !shift_density || !shift_flux) return ECS_ERR_INVALID;
+  int S = precision == ECS_PREC_FP64 ? ECS_FIX_SHIFT_FP64 : ECS_FIX_SHIFT_MIXED;
+  double vmax = 16.0 * (p->viT + p->vi0);
+  int ev = vmax > 0.0 ? (int)ceil(log2(vmax)) : 0;
+  if (ev < -8) ev = -8;
+  if (ev > 40) ev = 40;
+  *shift_density = S;
+  *shift_flux = S - ev;
+  return ECS_OK;
+}
 
 }  // extern "C"

@@ -81,12 +81,12 @@ __global__ void k_eext(GridG g, const double *__restrict__ phi, double4_32a *__r
 }
 
 // ---- moments -----------------------------------------------------------------
-__global__ void k_moments(size_t n4, const long long *__restrict__ acc, double *__restrict__ mom,
-                          double iscale, EcsDevStatus *st) {
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += (size_t)gridDim.x * blockDim.x) {
+__global__ void k_moments(size_t n, const long long *__restrict__ acc, double *__restrict__ mom,
+                          double iscale_n, double iscale_f, EcsDevStatus *st) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 4 * n; e += (size_t)gridDim.x * blockDim.x) {
     long long a = acc[e];
     if (a > (1ll << 62) || a < -(1ll << 62)) atomicOr(&st->flags, ECS_FLAG_RANGE);
-    mom[e] = __ll2double_rn(a) * iscale;
+    mom[e] = __ll2double_rn(a) * (e < n ? iscale_n : iscale_f);
   }
 }
 
@@ -278,48 +278,173 @@ __global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z) {
   }
 }
 
-// One damped z-line Jacobi sweep: xn = (1-w) xo + w * Tz^{-1} (b - Axy xo).
-// xo == nullptr means a zero previous iterate.
+// Right-hand side of the z-line systems: r = b - A_xy xo, where A_xy holds
+// the 8 in-plane entries of each row (x+-, y+-, the four xy corners).
 template <typename T>
-__global__ void k_zline_sweep(OpK o, const T *__restrict__ n, ZlP<T> z, const T *__restrict__ b,
-                              const T *__restrict__ xo, T *__restrict__ xn, T omega) {
+__global__ void k_zline_rhs(OpK o, const T *__restrict__ n, const T *__restrict__ b,
+                            const T *__restrict__ xo, T *__restrict__ r) {
   const GridG &g = o.g;
-  const int ncol = g.nx * g.ny;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  const int i = col % g.nx, j = col / g.nx;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cell_ijk(c, g, i, j, k);
+    T v[11];
+    row11(n, o, i, j, k, v);
+    T s = b[c];
+#pragma unroll
+    for (int e = 0; e < 10; e++) {
+      if (e == 4 || e == 5) continue;
+      s -= v[e] * gval(xo, g, k, j + c_off[e][1], i + c_off[e][0]);
+    }
+    r[c] = s;
+  }
+}
+
+constexpr int kZChunk = 8;
+
+// Thomas solve of one column with the precomputed factors (a, cp, minv) and
+// the Sherman-Morrison closure (q, a0g, qden), then damping against xo
+// (nullptr: zero).  Loads of chunk c+1 are issued before chunk c is used.
+template <typename T>
+__device__ __forceinline__ void zline_column(const GridG &g, const ZlP<T> &z, const T *__restrict__ r,
+                                             const T *__restrict__ xo, T *__restrict__ xn, T omega, int col) {
   const size_t plane = (size_t)g.nx * g.ny;
   const int N = g.nz;
-  T dp_prev = T(0);
-  for (int k = 0; k < N; k++) {
-    size_t c = (size_t)k * plane + col;
-    T r = b[c];
-    if (xo) {
-      T v[11];
-      row11(n, o, i, j, k, v);
+  T ra[kZChunk], aa[kZChunk], ma[kZChunk];
+  T rb[kZChunk], ab[kZChunk], mb[kZChunk];
 #pragma unroll
-      for (int e = 0; e < 10; e++) {
-        if (e == 4 || e == 5) continue;
-        r -= v[e] * gval(xo, g, k + c_off[e][2], j + c_off[e][1], i + c_off[e][0]);
+  for (int q = 0; q < kZChunk; q++) {
+    size_t c = (size_t)q * plane + col;
+    bool in = q < N;
+    ra[q] = in ? r[c] : T(0);
+    aa[q] = in ? z.a[c] : T(0);
+    ma[q] = in ? z.minv[c] : T(0);
+  }
+  T dp = T(0);
+  for (int k0 = 0; k0 < N; k0 += kZChunk) {
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {  // prefetch next chunk
+      int k = k0 + kZChunk + q;
+      size_t c = (size_t)k * plane + col;
+      bool in = k < N;
+      rb[q] = in ? r[c] : T(0);
+      ab[q] = in ? z.a[c] : T(0);
+      mb[q] = in ? z.minv[c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      if (k < N) {
+        dp = (ra[q] - aa[q] * dp) * ma[q];
+        z.dp[(size_t)k * plane + col] = dp;
       }
     }
-    T dp = (r - z.a[c] * dp_prev) * z.minv[c];
-    z.dp[c] = dp;
-    dp_prev = dp;
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      ra[q] = rb[q];
+      aa[q] = ab[q];
+      ma[q] = mb[q];
+    }
   }
-  T y = z.dp[(size_t)(N - 1) * plane + col];
-  const T yN = y;
-  for (int k = N - 2; k >= 0; k--) {
+  // backward substitution, chunks from the top
+  T y = T(0);
+  const T yN = z.dp[(size_t)(N - 1) * plane + col];
+  const int last0 = ((N - 1) / kZChunk) * kZChunk;
+  T da[kZChunk], ca[kZChunk], db[kZChunk], cb[kZChunk];
+#pragma unroll
+  for (int q = 0; q < kZChunk; q++) {
+    int k = last0 + q;
     size_t c = (size_t)k * plane + col;
-    y = z.dp[c] - z.cp[c] * y;
-    z.dp[c] = y;
+    bool in = k < N;
+    da[q] = in ? z.dp[c] : T(0);
+    ca[q] = in ? z.cp[c] : T(0);
+  }
+  for (int k0 = last0; k0 >= 0; k0 -= kZChunk) {
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 - kZChunk + q;
+      size_t c = (size_t)(k < 0 ? 0 : k) * plane + col;
+      bool in = k >= 0;
+      db[q] = in ? z.dp[c] : T(0);
+      cb[q] = in ? z.cp[c] : T(0);
+    }
+#pragma unroll
+    for (int q = kZChunk - 1; q >= 0; q--) {
+      int k = k0 + q;
+      if (k < N) {
+        y = (k == N - 1) ? da[q] : da[q] - ca[q] * y;
+        z.dp[(size_t)k * plane + col] = y;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      da[q] = db[q];
+      ca[q] = cb[q];
+    }
   }
   const T s = (y + z.a0g[col] * yN) * z.qden[col];
-  for (int k = 0; k < N; k++) {
-    size_t c = (size_t)k * plane + col;
-    T sol = z.dp[c] - s * z.q[c];
-    T old = xo ? xo[c] : T(0);
-    xn[c] = old + omega * (sol - old);
+  for (int k0 = 0; k0 < N; k0 += kZChunk) {
+    T yv[kZChunk], qv[kZChunk], ov[kZChunk];
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      size_t c = (size_t)k * plane + col;
+      bool in = k < N;
+      yv[q] = in ? z.dp[c] : T(0);
+      qv[q] = in ? z.q[c] : T(0);
+      ov[q] = (in && xo) ? xo[c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      if (k < N) xn[(size_t)k * plane + col] = ov[q] + omega * ((yv[q] - s * qv[q]) - ov[q]);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_zline_solve(GridG g, ZlP<T> z, const T *__restrict__ r, const T *__restrict__ xo,
+                              T *__restrict__ xn, T omega) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= g.nx * g.ny) return;
+  zline_column<T>(g, z, r, xo, xn, omega, col);
+}
+
+// All sweeps of a small level in one block: each sweep forms r in `rbuf`,
+// solves every column, and alternates between x and t; the result ends in x.
+template <typename T>
+__global__ void k_zline_block(OpK o, const T *__restrict__ n, ZlP<T> z, const T *__restrict__ b,
+                              T *__restrict__ x, T *__restrict__ t, T *__restrict__ rbuf, int nsweeps,
+                              T omega) {
+  const GridG &g = o.g;
+  const int ncol = g.nx * g.ny;
+  T *cur = x, *nxt = t;
+  for (int sw = 0; sw < nsweeps; sw++) {
+    const T *xo = sw == 0 ? nullptr : cur;
+    if (xo) {
+      for (size_t c = threadIdx.x; c < g.n; c += blockDim.x) {
+        int i, j, k;
+        cell_ijk(c, g, i, j, k);
+        T v[11];
+        row11(n, o, i, j, k, v);
+        T s = b[c];
+#pragma unroll
+        for (int e = 0; e < 10; e++) {
+          if (e == 4 || e == 5) continue;
+          s -= v[e] * gval(xo, g, k, j + c_off[e][1], i + c_off[e][0]);
+        }
+        rbuf[c] = s;
+      }
+      __syncthreads();
+    }
+    for (int col = threadIdx.x; col < ncol; col += blockDim.x)
+      zline_column<T>(g, z, xo ? rbuf : b, xo, nxt, omega, col);
+    __syncthreads();
+    T *tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  if (cur != x) {
+    for (size_t c = threadIdx.x; c < g.n; c += blockDim.x) x[c] = cur[c];
   }
 }
 
@@ -584,9 +709,15 @@ int mg_setup(EcsCtx *ctx) {
 
 template <typename T>
 int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
+  const OpK o = op_level(ctx, L);
+  const T *r = b;
+  if (xo) {
+    k_zline_rhs<T><<<blocks_for(ctx, L.n), kB, 0, ctx->stream>>>(o, L.dens, b, xo, L.r);
+    ECS_LAUNCHED(ctx);
+    r = L.r;
+  }
   int ncol = L.nx * L.ny;
-  k_zline_sweep<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L), b,
-                                                                             xo, xn, kOmega<T>());
+  k_zline_solve<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -598,6 +729,12 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
   MgLevel<T> &L = mg.lv[l];
   int rc;
   if (l + 1 == mg.lv.size()) {
+    if (L.n <= 8192) {
+      k_zline_block<T><<<1, 256, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L), b, xout, L.t, L.r,
+                                                    kCoarseSweeps, kOmega<T>());
+      ECS_LAUNCHED(ctx);
+      return ECS_OK;
+    }
     if ((rc = sweep<T>(ctx, L, b, nullptr, xout))) return rc;
     for (int s = 0; s < (kCoarseSweeps - 1) / 2; s++) {
       if ((rc = sweep<T>(ctx, L, b, xout, L.t))) return rc;
@@ -802,9 +939,9 @@ int ecs_grid_clear_acc(EcsCtx *ctx) {
 }
 
 int ecs_grid_moments(EcsCtx *ctx) {
-  int shift = ctx->prec == ECS_PREC_FP64 ? ECS_FIX_SHIFT_FP64 : ECS_FIX_SHIFT_MIXED;
-  k_moments<<<blocks_for(ctx, ctx->ncell * 4), kB, 0, ctx->stream>>>(ctx->ncell * 4, ctx->acc, ctx->mom,
-                                                                    ldexp(1.0, -shift), ctx->dstat);
+  k_moments<<<blocks_for(ctx, ctx->ncell * 4), kB, 0, ctx->stream>>>(ctx->ncell, ctx->acc, ctx->mom,
+                                                                    ldexp(1.0, -ctx->shift_n),
+                                                                    ldexp(1.0, -ctx->shift_f), ctx->dstat);
   ECS_LAUNCHED(ctx);
   ctx->moments_ready = true;
   return ECS_OK;

@@ -13,8 +13,10 @@
 
 // Fixed-point scales of the deposit accumulators: contributions are rounded
 // to integer multiples of 2^-S and summed exactly in int64, which makes the
-// moments independent of the order in which particles are processed.
-#define ECS_FIX_SHIFT_FP64 44
+// moments independent of the order in which particles are processed.  The
+// density uses S = ECS_FIX_SHIFT_*; the flux uses S - e_v, where 2^e_v bounds
+// |v| (ecs_fix_shifts), so every contribution is at most 2^S in magnitude.
+#define ECS_FIX_SHIFT_FP64 48
 #define ECS_FIX_SHIFT_MIXED 40
 
 // Device status word bits (EcsDevStatus::flags).
@@ -116,6 +118,7 @@ struct EcsCtx {
   EcsDevStatus *dstat = nullptr;
   EcsDevStatus *hstat = nullptr;    // pinned
 
+  int shift_n = 48, shift_f = 48;   // deposit fixed-point shifts (density, flux)
   int64_t launches = 0;
   std::string err;
   // events around the particle kernel [0,1] and the sort [2,3] of a step
@@ -200,3 +203,4 @@ int ecs_part_collect(EcsCtx *ctx);
 int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide);
 int ecs_part_sort(EcsCtx *ctx);
 int ecs_part_estimate_rate(EcsCtx *ctx, double dt);
+extern "C" int ecs_fix_shifts(const EcsParams *p, int precision, int32_t *shift_density, int32_t *shift_flux);

@@ -63,8 +63,11 @@ struct PartK {
   int collide;
   double rate, p0, vrm2, viT, vnT, vn0[3], mi, mn, M;  // p0 = exp(-rate)
   uint32_t key0, key1, step;
-  double fix64;
-  float fix32;
+  // fixed-point scales of the deposit: density 2^Sn, flux 2^Sf (Sf = Sn - e_v
+  // for the velocity bound 2^e_v), and the bound itself
+  double fixn64, fixf64;
+  float fixn32, fixf32;
+  double vmax;
 };
 
 // ---- deposit ---------------------------------------------------------------
@@ -82,61 +85,59 @@ __device__ __forceinline__ long long corner_node(const PartK &k, int i, int j, i
 }
 
 // Deposit one particle's CIC contributions (src/moments.c:162-205): weights
-// w_b = wz*wy*wx over the 8 corners, density += w_b, flux_d += v_d*w_b.
-// All lanes of the warp must call this together.
+// w_b = wz*wy*wx over the 8 corners (the reference's product order),
+// density += w_b, flux_d += v_d*w_b, each rounded to an integer multiple of
+// the field's fixed-point quantum.
+//
+// Warp aggregation: every lane writes its 32 values (slot = b + 8*field) to
+// the warp's shared-memory tile, transposed so that lane l then reads slot l
+// of all 32 lanes.  Lanes are grouped by cell (__match_any_sync); for each
+// group lane l adds slot l over the group's lanes (exact int64) and issues
+// one atomic for that node and field.  Any mix of cells in a warp is handled;
+// cell-sorted ions give few groups and so few atomics.  `tile` is this warp's
+// 32 x 33 int64 scratch (padded against bank conflicts).  All lanes of the
+// warp must call this together.
+constexpr int kTileStride = 33;
+
 template <typename T>
-__device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, const PartK &k,
+__device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long long *tile, const PartK &k,
                                              bool active, int i, int j, int kk, T wxh, T wyh,
-                                             T wzh, T v0, T v1, T v2, T scale) {
+                                             T wzh, T v0, T v1, T v2, T sn, T sf) {
   const int lane = threadIdx.x & 31;
-  T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
-  T w[8];
-  w[0] = wzl * wyl * wxl;
-  w[1] = wzl * wyl * wxh;
-  w[2] = wzl * wyh * wxl;
-  w[3] = wzl * wyh * wxh;
-  w[4] = wzh * wyl * wxl;
-  w[5] = wzh * wyl * wxh;
-  w[6] = wzh * wyh * wxl;
-  w[7] = wzh * wyh * wxh;
-  long long c[32];
+  const T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
 #pragma unroll
   for (int b = 0; b < 8; b++) {
-    c[b] = active ? fix_rn(w[b], scale) : 0;
-    c[8 + b] = active ? fix_rn(v0 * w[b], scale) : 0;
-    c[16 + b] = active ? fix_rn(v1 * w[b], scale) : 0;
-    c[24 + b] = active ? fix_rn(v2 * w[b], scale) : 0;
+    const T wz = (b & 4) ? wzh : wzl, wy = (b & 2) ? wyh : wyl, wx = (b & 1) ? wxh : wxl;
+    const T w = wz * wy * wx;
+    tile[(b + 0) * kTileStride + lane] = active ? fix_rn(w, sn) : 0ll;
+    tile[(b + 8) * kTileStride + lane] = active ? fix_rn(v0 * w, sf) : 0ll;
+    tile[(b + 16) * kTileStride + lane] = active ? fix_rn(v1 * w, sf) : 0ll;
+    tile[(b + 24) * kTileStride + lane] = active ? fix_rn(v2 * w, sf) : 0ll;
   }
-  int key = active ? (i | (j << 10) | (kk << 20)) : -1;
-  unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
-  if (peers == ECS_FULL_MASK && key >= 0) {
-    // Register reduce-scatter: afterwards lane l holds the warp sum of slot l.
-#pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) {
-      const bool upper = (lane & s) != 0;
-#pragma unroll
-      for (int q = 0; q < s; q++) {
-        long long send = upper ? c[q] : c[q + s];
-        long long keep = upper ? c[q + s] : c[q];
-        c[q] = keep + __shfl_xor_sync(ECS_FULL_MASK, send, s);
-      }
+  const int key = active ? (i | (j << 10) | (kk << 20)) : -1;
+  const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+  __syncwarp();
+  const long long *row = tile + lane * kTileStride;
+  unsigned rem = __ballot_sync(ECS_FULL_MASK, active);
+  while (rem) {
+    const int lead = __ffs(rem) - 1;
+    const unsigned grp = __shfl_sync(ECS_FULL_MASK, peers, lead);
+    const int gi = __shfl_sync(ECS_FULL_MASK, i, lead);
+    const int gj = __shfl_sync(ECS_FULL_MASK, j, lead);
+    const int gk = __shfl_sync(ECS_FULL_MASK, kk, lead);
+    rem &= ~grp;
+    long long sum = 0;
+    unsigned m = grp;
+    while (m) {
+      const int q = __ffs(m) - 1;
+      m &= m - 1;
+      sum += row[q];
     }
-    long long node = corner_node(k, i, j, kk, lane & 7);
-    if (node >= 0 && c[0] != 0)
-      atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node],
-                (unsigned long long)c[0]);
-  } else if (active) {
-#pragma unroll
-    for (int b = 0; b < 8; b++) {
-      long long node = corner_node(k, i, j, kk, b);
-      if (node < 0) continue;
-#pragma unroll
-      for (int d = 0; d < 4; d++)
-        if (c[8 * d + b] != 0)
-          atomicAdd((unsigned long long *)&acc[(size_t)d * k.ncell + node],
-                    (unsigned long long)c[8 * d + b]);
-    }
+    const long long node = corner_node(k, gi, gj, gk, lane & 7);
+    if (node >= 0 && sum != 0)
+      atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
   }
+  __syncwarp();
 }
 
 // ---- collisions --------------------------------------------------------------
@@ -376,7 +377,7 @@ __device__ __forceinline__ void move64(const PartK &k, double &p, double &v, int
   p = r.v;
 }
 
-__device__ __forceinline__ void deposit64(long long *acc, const PartK &k, bool active, double px,
+__device__ __forceinline__ void deposit64(long long *acc, long long *tile, const PartK &k, bool active, double px,
                                           double py, double pz, double vx, double vy, double vz) {
   rd x{0}, y{0}, z{0};
   int i = 0, j = 0, kk = 0;
@@ -387,7 +388,7 @@ __device__ __forceinline__ void deposit64(long long *acc, const PartK &k, bool a
   double wx = ok ? (x - rd{(double)i}).v : 0.0;
   double wy = ok ? (y - rd{(double)j}).v : 0.0;
   double wz = ok ? (z - rd{(double)kk}).v : 0.0;
-  deposit_warp<double>(acc, k, ok, i, j, kk, wx, wy, wz, vx, vy, vz, k.fix64);
+  deposit_warp<double>(acc, tile, k, ok, i, j, kk, wx, wy, wz, vx, vy, vz, k.fixn64, k.fixf64);
 }
 
 __device__ __forceinline__ void hash64(double px, double py, double pz, double vx, double vy,
@@ -414,6 +415,8 @@ __global__ void __launch_bounds__(kBlock) k_particles64(PartK k, int mode, int64
                                                         const double4_32a *__restrict__ E,
                                                         long long *__restrict__ acc,
                                                         EcsDevStatus *st) {
+  extern __shared__ long long shm_tiles[];
+  long long *tile = shm_tiles + (threadIdx.x >> 5) * 32 * kTileStride;
   const int64_t lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
@@ -446,7 +449,11 @@ __global__ void __launch_bounds__(kBlock) k_particles64(PartK k, int mode, int64
       move64(k, z, vz, 2);
     }
     if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
-    if (mode & 8) deposit64(acc, k, active, x, y, z, vx, vy, vz);
+    if (mode & 8) {
+      if (active && !(fabs(vx) <= k.vmax && fabs(vy) <= k.vmax && fabs(vz) <= k.vmax))
+        atomicOr(&st->flags, ECS_FLAG_RANGE);
+      deposit64(acc, tile, k, active, x, y, z, vx, vy, vz);
+    }
     if (active) {
       if (mode & 4) { px[ip] = x; py[ip] = y; pz[ip] = z; }
       if (mode & 7) { vxa[ip] = vx; vya[ip] = vy; vza[ip] = vz; }
@@ -533,11 +540,13 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
   state_hash(w, 7, h0, h1);
 }
 
-__global__ void __launch_bounds__(kBlock) k_particles32(
+__global__ void __launch_bounds__(kBlock, 3) k_particles32(
     PartK k, int mode, int64_t np, int32_t *__restrict__ cella, float *__restrict__ oxa,
     float *__restrict__ oya, float *__restrict__ oza, float *__restrict__ uxa,
     float *__restrict__ uya, float *__restrict__ uza, const float4 *__restrict__ E,
     long long *__restrict__ acc, EcsDevStatus *st) {
+  extern __shared__ long long shm_tiles[];
+  long long *tile = shm_tiles + (threadIdx.x >> 5) * 32 * kTileStride;
   const int64_t lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
@@ -592,7 +601,11 @@ __global__ void __launch_bounds__(kBlock) k_particles32(
       c = i | (j << 10) | (kk << 20);
     }
     if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
-    if (mode & 8) deposit_warp<float>(acc, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fix32);
+    if (mode & 8) {
+      if (active && !(fabsf(vx) <= (float)k.vmax && fabsf(vy) <= (float)k.vmax && fabsf(vz) <= (float)k.vmax))
+        atomicOr(&st->flags, ECS_FLAG_RANGE);
+      deposit_warp<float>(acc, tile, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fixn32, k.fixf32);
+    }
     if (active) {
       if (mode & 4) { cella[ip] = c; oxa[ip] = ox; oya[ip] = oy; oza[ip] = oz; }
       if (mode & 7) { uxa[ip] = vx; uya[ip] = vy; uza[ip] = vz; }
@@ -868,8 +881,11 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   k.key0 = (uint32_t)ctx->seed;
   k.key1 = (uint32_t)(ctx->seed >> 32);
   k.step = (uint32_t)ctx->step_index;
-  k.fix64 = ldexp(1.0, ECS_FIX_SHIFT_FP64);
-  k.fix32 = ldexpf(1.0f, ECS_FIX_SHIFT_MIXED);
+  k.fixn64 = ldexp(1.0, ctx->shift_n);
+  k.fixf64 = ldexp(1.0, ctx->shift_f);
+  k.fixn32 = ldexpf(1.0f, ctx->shift_n);
+  k.fixf32 = ldexpf(1.0f, ctx->shift_f);
+  k.vmax = ldexp(1.0, ctx->shift_n - ctx->shift_f);
   return k;
 }
 
@@ -1005,14 +1021,21 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode) {
     ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   }
   if (!k.collide) mode &= ~2;
-  unsigned int g = grid_blocks(ctx, ctx->np, 8);
+  const size_t shm = (size_t)(kBlock / 32) * 32 * kTileStride * sizeof(long long);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_particles64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    cudaFuncSetAttribute(k_particles32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    attr_set = true;
+  }
+  unsigned int g = grid_blocks(ctx, ctx->np, 3);
   if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
   if (ctx->prec == ECS_PREC_FP64) {
-    k_particles64<<<g, kBlock, 0, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
+    k_particles64<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                                 ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
   } else {
     int b = ctx->cur;
-    k_particles32<<<g, kBlock, 0, ctx->stream>>>(k, mode, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b],
+    k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b],
                                                 ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b],
                                                 ctx->eext32, ctx->acc, ctx->dstat);
   }

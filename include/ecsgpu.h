@@ -185,6 +185,12 @@ int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, 
    kernels; used to report launch counts). */
 int64_t ecs_launch_count(const EcsCtx *ctx);
 
+/* Fixed-point shifts of the deposition for these parameters: density
+   contributions are rounded to multiples of 2^-shift_density and flux
+   contributions to multiples of 2^-shift_flux; |v| above
+   2^(shift_density - shift_flux) makes a deposit report ECS_ERR_RANGE. */
+int ecs_fix_shifts(const EcsParams *params, int precision, int32_t *shift_density, int32_t *shift_flux);
+
 #ifdef __cplusplus
 }
 #endif

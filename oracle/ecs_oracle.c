@@ -248,18 +248,19 @@ int orc_collect(const OrcParams *p, int np, const double *pos, const double *vel
   return 0;
 }
 
-/* Fixed-point CIC deposit: the same weights as orc_collect, each
-   contribution rounded to an integer multiple of 2^-S (round to nearest
-   even) and summed exactly in int64, then converted once to FP64.  This is
-   the order-independent deposition the GPU library performs; it is exact
-   integer work, so the GPU must reproduce it bit for bit.  out is
-   [Nz][Ny][Nx][4] FP64; acc (optional) receives the raw int64 sums. */
+/* Fixed-point CIC deposit: the same weights as orc_collect, each density
+   contribution rounded to an integer multiple of 2^-Sn and each flux
+   contribution to a multiple of 2^-Sf (round to nearest even), summed exactly
+   in int64, then converted once to FP64.  This is the order-independent
+   deposition the GPU library performs; it is exact integer work, so the GPU
+   must reproduce it bit for bit.  out is [Nz][Ny][Nx][4] FP64; acc (optional)
+   receives the raw int64 sums. */
 int orc_collect_fixed(const OrcParams *p, int np, const double *pos, const double *vel,
-                      int S, double *out, int64_t *acc_out) {
+                      int Sn, int Sf, double *out, int64_t *acc_out) {
   size_t ncell = (size_t)p->Nx * p->Ny * p->Nz;
   int64_t *acc = calloc(ncell * 4, sizeof(int64_t));
   if (!acc) return -1;
-  double sc = ldexp(1.0, S);
+  double sc = ldexp(1.0, Sn), scf = ldexp(1.0, Sf);
   for (int ip = 0; ip < np; ip++) {
     int idx[3];
     double w[8];
@@ -272,11 +273,11 @@ int orc_collect_fixed(const OrcParams *p, int np, const double *pos, const doubl
       if (k < 0 || k >= p->Nz) { if (p->bc[2]) continue; k = wrapi(k, p->Nz); }
       int64_t *node = acc + (((size_t)k * p->Ny + j) * p->Nx + i) * 4;
       node[0] += (int64_t)llrint(w[b] * sc);
-      for (int d = 0; d < 3; d++) node[1 + d] += (int64_t)llrint((vel[ip * 3 + d] * w[b]) * sc);
+      for (int d = 0; d < 3; d++) node[1 + d] += (int64_t)llrint((vel[ip * 3 + d] * w[b]) * scf);
     }
   }
-  double isc = ldexp(1.0, -S);
-  for (size_t e = 0; e < ncell * 4; e++) out[e] = (double)acc[e] * isc;
+  double isc = ldexp(1.0, -Sn), iscf = ldexp(1.0, -Sf);
+  for (size_t e = 0; e < ncell * 4; e++) out[e] = (double)acc[e] * ((e % 4) == 0 ? isc : iscf);
   if (acc_out) memcpy(acc_out, acc, sizeof(int64_t) * ncell * 4);
   free(acc);
   return 0;

@@ -54,7 +54,7 @@ def lib():
             "orc_push": (C.c_int, [P, C.c_int, vp, vp, vp, C.c_double]),
             "orc_move": (C.c_int, [P, C.c_int, vp, vp, C.c_double]),
             "orc_collect": (C.c_int, [P, C.c_int, vp, vp, vp]),
-            "orc_collect_fixed": (C.c_int, [P, C.c_int, vp, vp, C.c_int, vp, vp]),
+            "orc_collect_fixed": (C.c_int, [P, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp]),
             "orc_collect_mt": (C.c_int, [P, C.c_int, vp, vp, vp]),
             "orc_rhs": (C.c_int, [P, vp, vp]),
             "orc_lhs_dense": (C.c_int, [P, vp, vp]),
@@ -151,12 +151,12 @@ class Oracle:
         self.L.orc_collect_mt(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(out))
         return out
 
-    def collect_fixed(self, pos, vel, shift):
+    def collect_fixed(self, pos, vel, shift_n, shift_f):
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         out = np.zeros(self.shape + (4,))
         acc = np.zeros(self.shape + (4,), dtype=np.int64)
-        self.L.orc_collect_fixed(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), shift, _p(out), _p(acc))
+        self.L.orc_collect_fixed(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), shift_n, shift_f, _p(out), _p(acc))
         return out, acc
 
     def rhs(self, moments):
