@@ -451,42 +451,141 @@ __global__ void k_zline_block(OpK o, const T *__restrict__ n, ZlP<T> z, const T 
 // ---- inter-grid transfer ---------------------------------------------------------
 // Full weighting (1/4,1/2,1/4 per axis) from fine (2I+a) to coarse I.
 template <typename T>
-__global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < gc.n; e += (size_t)gridDim.x * blockDim.x) {
-    int I, J, K;
-    cell_ijk(e, gc, I, J, K);
-    T s = T(0);
+__device__ __forceinline__ T restrict_at(const GridG &gf, const GridG &gc, const T *__restrict__ f, size_t e) {
+  int I, J, K;
+  cell_ijk(e, gc, I, J, K);
+  T s = T(0);
 #pragma unroll
-    for (int dk = -1; dk <= 1; dk++) {
-      T wk = dk == 0 ? T(0.5) : T(0.25);
+  for (int dk = -1; dk <= 1; dk++) {
+    T wk = dk == 0 ? T(0.5) : T(0.25);
 #pragma unroll
-      for (int dj = -1; dj <= 1; dj++) {
-        T wj = dj == 0 ? T(0.5) : T(0.25);
+    for (int dj = -1; dj <= 1; dj++) {
+      T wj = dj == 0 ? T(0.5) : T(0.25);
 #pragma unroll
-        for (int di = -1; di <= 1; di++) {
-          T wi = di == 0 ? T(0.5) : T(0.25);
-          s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
-        }
+      for (int di = -1; di <= 1; di++) {
+        T wi = di == 0 ? T(0.5) : T(0.25);
+        s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
       }
     }
-    c[e] = s;
   }
+  return s;
+}
+template <typename T>
+__global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < gc.n; e += (size_t)gridDim.x * blockDim.x)
+    c[e] = restrict_at(gf, gc, f, e);
 }
 
-// Trilinear prolongation, added: f += P c.
+// Trilinear prolongation value at fine cell e.
+template <typename T>
+__device__ __forceinline__ T prolong_at(const GridG &gf, const GridG &gc, const T *__restrict__ c, size_t e) {
+  int i, j, k;
+  cell_ijk(e, gf, i, j, k);
+  int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
+  int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+  T wi = ni == 2 ? T(0.5) : T(1), wj = nj == 2 ? T(0.5) : T(1), wk = nk == 2 ? T(0.5) : T(1);
+  T s = T(0);
+  for (int a = 0; a < nk; a++)
+    for (int bq = 0; bq < nj; bq++)
+      for (int q = 0; q < ni; q++) s += gval(c, gc, k0 + a, j0 + bq, i0 + q);
+  return wi * wj * wk * s;
+}
+// f += P c.
 template <typename T>
 __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__restrict__ f) {
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < gf.n; e += (size_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    cell_ijk(e, gf, i, j, k);
-    int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
-    int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
-    T wi = ni == 2 ? T(0.5) : T(1), wj = nj == 2 ? T(0.5) : T(1), wk = nk == 2 ? T(0.5) : T(1);
-    T s = T(0);
-    for (int a = 0; a < nk; a++)
-      for (int bq = 0; bq < nj; bq++)
-        for (int q = 0; q < ni; q++) s += gval(c, gc, k0 + a, j0 + bq, i0 + q);
-    f[e] += wi * wj * wk * s;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < gf.n; e += (size_t)gridDim.x * blockDim.x)
+    f[e] += prolong_at(gf, gc, c, e);
+}
+
+// ---- whole V-cycle of the small levels in one thread block -------------------
+template <typename T>
+struct SmallLevel {
+  OpK o;
+  T *dens, *x, *b, *r, *t;
+  ZlP<T> z;
+};
+constexpr int kMaxSmall = 8;
+template <typename T>
+struct SmallCycle {
+  int nl;
+  SmallLevel<T> lv[kMaxSmall];
+};
+
+template <typename T>
+__device__ void blk_sweep(const SmallLevel<T> &L, const T *b, const T *xo, T *xn, T omega) {
+  const GridG &g = L.o.g;
+  if (xo) {
+    for (size_t c = threadIdx.x; c < g.n; c += blockDim.x) {
+      int i, j, k;
+      cell_ijk(c, g, i, j, k);
+      T v[11];
+      row11(L.dens, L.o, i, j, k, v);
+      T s = b[c];
+#pragma unroll
+      for (int e = 0; e < 10; e++) {
+        if (e == 4 || e == 5) continue;
+        s -= v[e] * gval(xo, g, k, j + c_off[e][1], i + c_off[e][0]);
+      }
+      L.r[c] = s;
+    }
+    __syncthreads();
+  }
+  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x)
+    zline_column<T>(g, L.z, xo ? L.r : b, xo, xn, omega, col);
+  __syncthreads();
+}
+
+// x_out = M(l0) b_in: V(1,1) over levels l0..l0+nl-1, all in this block.
+template <typename T>
+__global__ void __launch_bounds__(512) k_vcycle_small(SmallCycle<T> sc, const T *__restrict__ b_in,
+                                                      T *__restrict__ x_out, int coarse_sweeps, T omega) {
+  const int nl = sc.nl;
+  // down
+  for (int l = 0; l < nl - 1; l++) {
+    const SmallLevel<T> &L = sc.lv[l];
+    const T *b = l == 0 ? b_in : L.b;
+    blk_sweep(L, b, (const T *)nullptr, L.t, omega);
+    const GridG &g = L.o.g;
+    for (size_t c = threadIdx.x; c < g.n; c += blockDim.x) {
+      int i, j, k;
+      cell_ijk(c, g, i, j, k);
+      T v[11];
+      row11(L.dens, L.o, i, j, k, v);
+      T s = T(0);
+#pragma unroll
+      for (int e = 0; e < 11; e++) s += v[e] * gval(L.t, g, k + c_off[e][2], j + c_off[e][1], i + c_off[e][0]);
+      L.r[c] = b[c] - s;
+    }
+    __syncthreads();
+    const SmallLevel<T> &C = sc.lv[l + 1];
+    for (size_t c = threadIdx.x; c < C.o.g.n; c += blockDim.x) C.b[c] = restrict_at(g, C.o.g, L.r, c);
+    __syncthreads();
+  }
+  // coarsest: damped z-line Jacobi sweeps, result in its x (or x_out if nl == 1)
+  {
+    const SmallLevel<T> &L = sc.lv[nl - 1];
+    const T *b = nl == 1 ? b_in : L.b;
+    T *dst = nl == 1 ? x_out : L.x;
+    T *cur = dst, *nxt = L.t;
+    for (int sw = 0; sw < coarse_sweeps; sw++) {
+      blk_sweep(L, b, sw == 0 ? (const T *)nullptr : cur, nxt, omega);
+      T *tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+    }
+    if (cur != dst) {
+      for (size_t c = threadIdx.x; c < L.o.g.n; c += blockDim.x) dst[c] = cur[c];
+      __syncthreads();
+    }
+  }
+  // up
+  for (int l = nl - 2; l >= 0; l--) {
+    const SmallLevel<T> &L = sc.lv[l], &C = sc.lv[l + 1];
+    const GridG &g = L.o.g;
+    for (size_t c = threadIdx.x; c < g.n; c += blockDim.x) L.t[c] += prolong_at(g, C.o.g, C.x, c);
+    __syncthreads();
+    const T *b = l == 0 ? b_in : L.b;
+    blk_sweep(L, b, L.t, l == 0 ? x_out : L.x, omega);
   }
 }
 
@@ -507,23 +606,33 @@ __global__ void k_axpy64(size_t n, double a, const T *__restrict__ e, double *__
     x[q] += a * (double)e[q];
 }
 
-// partial[v*nb + block] = sum_k V_v[k] * w[k] for v < nv; slot nv holds w.w
+// partial[v*nb + block] = sum_k V_v[k] * w[k] for v < nv; slot nv holds w.w.
+// Products and sums over runs of 8 consecutive elements are formed in the
+// vectors' own precision T; the runs are accumulated in FP64.
 template <typename T>
 __global__ void k_mdot_partial(size_t n, int nv, const T *__restrict__ V, size_t ld, const T *__restrict__ w,
                                int with_ww, double *__restrict__ partial) {
   extern __shared__ double shm[];  // [nwarps][nv+1]
   const int nwarp = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nslot = nv + (with_ww ? 1 : 0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (int v0 = 0; v0 < nslot; v0 += 8) {
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-      double we = (double)w[e];
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    while (e < n) {
+      T run[8] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll 1
+      for (int r = 0; r < 8 && e < n; r++, e += stride) {
+        const T we = w[e];
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        int v = v0 + q;
-        if (v < nv) acc[q] += (double)V[(size_t)v * ld + e] * we;
-        else if (v == nv && with_ww) acc[q] += we * we;
+        for (int q = 0; q < 8; q++) {
+          const int v = v0 + q;
+          if (v < nv) run[q] += V[(size_t)v * ld + e] * we;
+          else if (v == nv && with_ww) run[q] += we * we;
+        }
       }
+#pragma unroll
+      for (int q = 0; q < 8; q++) acc[q] += (double)run[q];
     }
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -560,9 +669,9 @@ template <typename T>
 __global__ void k_maxpy(size_t n, int nv, const double *__restrict__ h, const T *__restrict__ V, size_t ld,
                         T *__restrict__ w) {
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    double s = (double)w[e];
-    for (int v = 0; v < nv; v++) s -= h[v] * (double)V[(size_t)v * ld + e];
-    w[e] = (T)s;
+    T s = w[e];
+    for (int v = 0; v < nv; v++) s -= (T)h[v] * V[(size_t)v * ld + e];
+    w[e] = s;
   }
 }
 // x += sum_v y[v] Z_v
@@ -570,9 +679,9 @@ template <typename T>
 __global__ void k_combine(size_t n, int nv, const double *__restrict__ y, const T *__restrict__ Z, size_t ld,
                           T *__restrict__ x) {
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    double s = (double)x[e];
-    for (int v = 0; v < nv; v++) s += y[v] * (double)Z[(size_t)v * ld + e];
-    x[e] = (T)s;
+    T s = x[e];
+    for (int v = 0; v < nv; v++) s += (T)y[v] * Z[(size_t)v * ld + e];
+    x[e] = s;
   }
 }
 // v -= mean(v) using a precomputed sum
@@ -722,19 +831,29 @@ int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
   return ECS_OK;
 }
 
-// One V(1,1) cycle on level l: xout = M(l) b, zero initial guess.
+constexpr size_t kSmallCells = 4096;
+
+// One V(1,1) cycle on level l: xout = M(l) b, zero initial guess.  Levels of
+// at most kSmallCells cells run as one single-block kernel.
 template <typename T>
 int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
   Multigrid<T> &mg = mg_of<T>(ctx);
   MgLevel<T> &L = mg.lv[l];
   int rc;
-  if (l + 1 == mg.lv.size()) {
-    if (L.n <= 8192) {
-      k_zline_block<T><<<1, 256, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L), b, xout, L.t, L.r,
-                                                    kCoarseSweeps, kOmega<T>());
-      ECS_LAUNCHED(ctx);
-      return ECS_OK;
+  if (L.n <= kSmallCells && mg.lv.size() - l <= (size_t)kMaxSmall) {
+    SmallCycle<T> sc;
+    sc.nl = (int)(mg.lv.size() - l);
+    for (int q = 0; q < sc.nl; q++) {
+      MgLevel<T> &M = mg.lv[l + q];
+      sc.lv[q].o = op_level(ctx, M);
+      sc.lv[q].dens = M.dens; sc.lv[q].x = M.x; sc.lv[q].b = M.b; sc.lv[q].r = M.r; sc.lv[q].t = M.t;
+      sc.lv[q].z = zl_of(M);
     }
+    k_vcycle_small<T><<<1, 512, 0, ctx->stream>>>(sc, b, xout, kCoarseSweeps, kOmega<T>());
+    ECS_LAUNCHED(ctx);
+    return ECS_OK;
+  }
+  if (l + 1 == mg.lv.size()) {
     if ((rc = sweep<T>(ctx, L, b, nullptr, xout))) return rc;
     for (int s = 0; s < (kCoarseSweeps - 1) / 2; s++) {
       if ((rc = sweep<T>(ctx, L, b, xout, L.t))) return rc;

@@ -61,7 +61,9 @@ struct PartK {
   float dtc[3];  // dt / cell width, FP32 (mixed move)
   // collisions, src/collisions.c:18-63
   int collide;
-  double rate, p0, vrm2, viT, vnT, vn0[3], mi, mn, M;  // p0 = exp(-rate)
+  double rate, vrm2, viT, vnT, vn0[3], mi, mn, M;
+  float p0f;          // exp(-rate)
+  uint32_t stepmix;   // step and seed mixed for the attempt uniform
   uint32_t key0, key1, step;
   // fixed-point scales of the deposit: density 2^Sn, flux 2^Sf (Sf = Sn - e_v
   // for the velocity bound 2^e_v), and the bound itself
@@ -119,6 +121,16 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
   __syncwarp();
   const long long *row = tile + lane * kTileStride;
   unsigned rem = __ballot_sync(ECS_FULL_MASK, active);
+  if (rem == ECS_FULL_MASK && peers == ECS_FULL_MASK) {
+    // the whole warp deposits into one cell: plain 32-term sums
+    long long sum = 0;
+#pragma unroll
+    for (int q = 0; q < 32; q++) sum += row[q];
+    const long long node = corner_node(k, i, j, kk, lane & 7);
+    if (node >= 0 && sum != 0)
+      atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
+    rem = 0;
+  }
   while (rem) {
     const int lead = __ffs(rem) - 1;
     const unsigned grp = __shfl_sync(ECS_FULL_MASK, peers, lead);
@@ -142,13 +154,14 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
 
 // ---- collisions --------------------------------------------------------------
 __device__ __forceinline__ void state_hash(const uint32_t *w, int n, uint32_t &h0, uint32_t &h1) {
+  // two multiply-xor chains over the state words, finalised by mixing
   uint32_t a = 0x811C9DC5u, b = 0x27D4EB2Fu;
   for (int q = 0; q < n; q++) {
-    a = ecs_mix32(a ^ w[q]);
-    b = ecs_mix32(b + w[q] * 0x9E3779B1u);
+    a = (a ^ w[q]) * 0x01000193u;
+    b = b * 0x9E3779B1u + w[q];
   }
-  h0 = a;
-  h1 = ecs_mix32(b ^ a);
+  h0 = ecs_mix32(a);
+  h1 = ecs_mix32(b ^ h0);
 }
 
 template <typename T>
@@ -176,50 +189,60 @@ __device__ __forceinline__ T accept_prob(T a) {
   return a * (T(1) - RMath<T>::log_(a));
 }
 
-// One ion's collisions in one pass (src/collisions.c:70-157).  Returns the
-// acceptance-probability sample (or -1 when this ion is not in the 1/16
-// hash-selected subsample that estimates the next pass's rate).
+// Acceptance-probability sample of one ion against one neutral drawn from
+// its own stream (used only to seed the attempt rate before the first pass).
 template <typename T>
-__device__ float collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &vy, T &vz,
-                             unsigned int &nacc, unsigned int &nref) {
+__device__ float accept_sample(const PartK &k, uint32_t h0, uint32_t h1, T vx, T vy, T vz) {
   typedef RMath<T> M;
-  float sample = -1.0f;
-  if ((h0 & 15u) == 0u) {
-    // acceptance sample for the rate estimate (pre-collision velocity)
-    EcsU4 e = ecs_philox({h0, h1, 0xFFFFFFFEu, k.step}, k.key0, k.key1);
-    T r1 = M::sqrt_(T(-2) * M::log_(M::u01(e.x, e.y)));
-    T s1, c1, s2, c2;
-    M::sincospi_(T(2) * M::u01(e.z, e.w), &s1, &c1);
-    EcsU4 e2 = ecs_philox({h0, h1, 0xFFFFFFFDu, k.step}, k.key0, k.key1);
-    T r2 = M::sqrt_(T(-2) * M::log_(M::u01(e2.x, e2.y)));
-    M::sincospi_(T(2) * M::u01(e2.z, e2.w), &s2, &c2);
-    T wx = vx - (T(r1 * c1) * T(k.vnT) + T(k.vn0[0]));
-    T wy = vy - (T(r1 * s1) * T(k.vnT) + T(k.vn0[1]));
-    T wz = vz - (T(r2 * c2) * T(k.vnT) + T(k.vn0[2]));
-    sample = (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
-  }
+  EcsU4 e = ecs_philox({h0, h1, 0xFFFFFFFEu, k.step}, k.key0, k.key1);
+  T r1 = M::sqrt_(T(-2) * M::log_(M::u01(e.x, e.x)));
+  T r2 = M::sqrt_(T(-2) * M::log_(M::u01(e.z, e.z)));
+  T s1, c1, s2, c2;
+  M::sincospi_(T(2) * M::u01(e.y, e.y), &s1, &c1);
+  M::sincospi_(T(2) * M::u01(e.w, e.w), &s2, &c2);
+  T wx = vx - (r1 * c1 * T(k.vnT) + T(k.vn0[0]));
+  T wy = vy - (r1 * s1 * T(k.vnT) + T(k.vn0[1]));
+  T wz = vz - (r2 * c2 * T(k.vnT) + T(k.vn0[2]));
+  return (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
+}
 
-  // number of attempts ~ Poisson(rate), by inversion of a uniform drawn from
-  // the state hash mixed with the step and seed
-  uint32_t hu = ecs_mix32(h1 ^ ecs_mix32(k.step * 0x9E3779B9u ^ k.key0) ^ k.key1);
-  T u = M::u01(hu, ecs_mix32(hu ^ h0));
-  T p = T(k.p0), cdf = p, rate = T(k.rate);
+// One ion's collisions in one pass (src/collisions.c:70-157): a Poisson
+// number of attempts (rate k.rate) by inversion of a uniform drawn from the
+// state hash mixed with the step and seed; each attempt draws a Maxwellian
+// neutral, accepts with U1*U2 < |vr|^2/vrm^2, and scatters isotropically in
+// the centre-of-mass frame.
+template <typename T>
+__device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &vy, T &vz,
+                            unsigned int &nacc, unsigned int &nref) {
+  typedef RMath<T> M;
+  const uint32_t hu = ecs_mix32(h1 ^ k.stepmix);
+  const float u = ecs_u01f(hu);
+  if (u <= k.p0f) return;  // no attempt (the common case)
+  float p = k.p0f, cdf = p;
+  const float rate = (float)k.rate;
   int natt = 0;
   while (u > cdf && natt < 16) {
     natt++;
-    p *= rate / T(natt);
+    p *= rate / (float)natt;
     cdf += p;
   }
   for (int a = 0; a < natt; a++) {
+    // neutral velocity: three normal deviates by Box-Muller
     EcsU4 q1 = ecs_philox({h0, h1, 2u * a, k.step}, k.key0, k.key1);
     EcsU4 q2 = ecs_philox({h0, h1, 2u * a + 1u, k.step}, k.key0, k.key1);
-    T ra = M::sqrt_(T(-2) * M::log_(M::u01(q1.x, q1.y)));
-    T sa, ca;
-    M::sincospi_(T(2) * M::u01(q1.z, q1.w), &sa, &ca);
-    EcsU4 q3 = ecs_philox({h0, h1, 0x40000000u + a, k.step}, k.key0, k.key1);
-    T rb = M::sqrt_(T(-2) * M::log_(M::u01(q3.x, q3.y)));
-    T sb, cb;
-    M::sincospi_(T(2) * M::u01(q3.z, q3.w), &sb, &cb);
+    T ra, rb, sa, ca, sb, cb;
+    if (sizeof(T) == 4) {
+      ra = M::sqrt_(T(-2) * M::log_(M::u01(q1.x, q1.x)));
+      rb = M::sqrt_(T(-2) * M::log_(M::u01(q1.z, q1.z)));
+      M::sincospi_(T(2) * M::u01(q1.y, q1.y), &sa, &ca);
+      M::sincospi_(T(2) * M::u01(q1.w, q1.w), &sb, &cb);
+    } else {
+      EcsU4 q3 = ecs_philox({h0, h1, 0x40000000u + a, k.step}, k.key0, k.key1);
+      ra = M::sqrt_(T(-2) * M::log_(M::u01(q1.x, q1.y)));
+      rb = M::sqrt_(T(-2) * M::log_(M::u01(q3.x, q3.y)));
+      M::sincospi_(T(2) * M::u01(q1.z, q1.w), &sa, &ca);
+      M::sincospi_(T(2) * M::u01(q3.z, q3.w), &sb, &cb);
+    }
     T vn[3] = {ra * ca * T(k.vnT) + T(k.vn0[0]), ra * sa * T(k.vnT) + T(k.vn0[1]),
                rb * cb * T(k.vnT) + T(k.vn0[2])};
     T vi[3] = {vx, vy, vz};
@@ -270,26 +293,23 @@ __device__ float collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T 
       nacc++;
     }
   }
-  return sample;
 }
 
 // Warp-aggregated status counters.
-__device__ __forceinline__ void flush_counts(EcsDevStatus *st, unsigned int nacc,
-                                             unsigned int nref, float sample, bool active,
-                                             bool collide) {
-  if (!collide) return;
+__device__ __forceinline__ void flush_counts(EcsDevStatus *st, unsigned int nacc, unsigned int nref) {
   unsigned int a = __reduce_add_sync(ECS_FULL_MASK, nacc);
   unsigned int r = __reduce_add_sync(ECS_FULL_MASK, nref);
-  const bool has = active && sample >= 0.0f;
-  unsigned int f = __reduce_add_sync(ECS_FULL_MASK, has ? (unsigned int)__float2uint_rn(sample * 16777216.0f) : 0u);
-  unsigned int n = __popc(__ballot_sync(ECS_FULL_MASK, has));
   if ((threadIdx.x & 31) == 0) {
     if (a) atomicAdd(&st->collisions, (unsigned long long)a);
     if (r) atomicAdd(&st->refused, (unsigned long long)r);
-    if (n) {
-      atomicAdd(&st->acc_fix, (unsigned long long)f);
-      atomicAdd(&st->acc_count, (unsigned long long)n);
-    }
+  }
+}
+__device__ __forceinline__ void flush_samples(EcsDevStatus *st, float sample, bool has) {
+  unsigned int f = __reduce_add_sync(ECS_FULL_MASK, has ? (unsigned int)__float2uint_rn(sample * 16777216.0f) : 0u);
+  unsigned int n = __popc(__ballot_sync(ECS_FULL_MASK, has));
+  if ((threadIdx.x & 31) == 0 && n) {
+    atomicAdd(&st->acc_fix, (unsigned long long)f);
+    atomicAdd(&st->acc_count, (unsigned long long)n);
   }
 }
 
@@ -434,14 +454,13 @@ __global__ void __launch_bounds__(kBlock) k_particles64(PartK k, int mode, int64
       if (!ok) atomicOr(&st->flags, ECS_FLAG_RANGE);
     }
     unsigned int nacc = 0, nref = 0;
-    float sample = 0.f;
     if ((mode & 2) && k.collide) {
       if (active) {
         uint32_t h0, h1;
         hash64(x, y, z, vx, vy, vz, h0, h1);
-        sample = collide_ion<double>(k, h0, h1, vx, vy, vz, nacc, nref);
+        collide_ion<double>(k, h0, h1, vx, vy, vz, nacc, nref);
       }
-      flush_counts(st, nacc, nref, sample, active, true);
+      flush_counts(st, nacc, nref);
     }
     if ((mode & 4) && active) {
       move64(k, x, vx, 0);
@@ -576,14 +595,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(
       vz = vzm;
     }
     unsigned int nacc = 0, nref = 0;
-    float sample = 0.f;
     if ((mode & 2) && k.collide) {
       if (active) {
         uint32_t h0, h1;
         hash32(c, ox, oy, oz, vx, vy, vz, h0, h1);
-        sample = collide_ion<float>(k, h0, h1, vx, vy, vz, nacc, nref);
+        collide_ion<float>(k, h0, h1, vx, vy, vz, nacc, nref);
       }
-      flush_counts(st, nacc, nref, sample, active, true);
+      flush_counts(st, nacc, nref);
     }
     bool inside = true;
     if ((mode & 4) && active) {
@@ -809,13 +827,9 @@ __global__ void k_estimate64(PartK k, int64_t np, const double *px, const double
       double vx = vxa[ip], vy = vya[ip], vz = vza[ip];
       uint32_t h0, h1;
       hash64(px[ip], py[ip], pz[ip], vx, vy, vz, h0, h1);
-      PartK kk = k;
-      kk.rate = 0.0;
-      kk.p0 = 1.0;
-      unsigned int a = 0, r = 0;
-      sample = collide_ion<double>(kk, h0, h1, vx, vy, vz, a, r);
+      sample = accept_sample<double>(k, h0, h1, vx, vy, vz);
     }
-    flush_counts(st, 0, 0, sample, active, true);
+    flush_samples(st, sample, active);
   }
 }
 __global__ void k_estimate32(PartK k, int64_t np, const int32_t *cella, const float *oxa,
@@ -831,13 +845,9 @@ __global__ void k_estimate32(PartK k, int64_t np, const int32_t *cella, const fl
       float vx = uxa[ip], vy = uya[ip], vz = uza[ip];
       uint32_t h0, h1;
       hash32(cella[ip], oxa[ip], oya[ip], oza[ip], vx, vy, vz, h0, h1);
-      PartK kk = k;
-      kk.rate = 0.0;
-      kk.p0 = 1.0;
-      unsigned int a = 0, r = 0;
-      sample = collide_ion<float>(kk, h0, h1, vx, vy, vz, a, r);
+      sample = accept_sample<float>(k, h0, h1, vx, vy, vz);
     }
-    flush_counts(st, 0, 0, sample, active, true);
+    flush_samples(st, sample, active);
   }
 }
 
@@ -881,6 +891,11 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   k.key0 = (uint32_t)ctx->seed;
   k.key1 = (uint32_t)(ctx->seed >> 32);
   k.step = (uint32_t)ctx->step_index;
+  {
+    uint32_t m = (uint32_t)ctx->step_index * 0x9E3779B9u ^ k.key0;
+    m ^= m >> 16; m *= 0x7feb352du; m ^= m >> 15; m *= 0x846ca68bu; m ^= m >> 16;
+    k.stepmix = m ^ k.key1;
+  }
   k.fixn64 = ldexp(1.0, ctx->shift_n);
   k.fixf64 = ldexp(1.0, ctx->shift_f);
   k.fixn32 = ldexpf(1.0f, ctx->shift_n);
@@ -1017,7 +1032,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode) {
       if (rc) return rc;
     }
     k.rate = ctx->attempt_rate;
-    k.p0 = exp(-k.rate);
+    k.p0f = (float)exp(-k.rate);
     ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   }
   if (!k.collide) mode &= ~2;
@@ -1052,10 +1067,18 @@ static int finish_collisions(EcsCtx *ctx, double dt) {
   ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const EcsDevStatus &s = *ctx->hstat;
-  if (s.acc_count > 0) {
-    double mean = (double)s.acc_fix / 16777216.0 / (double)s.acc_count;
-    int64_t Nc = collision_target(ctx, dt);
-    ctx->attempt_rate = (mean > 0 && ctx->np > 0) ? (double)Nc / ((double)ctx->np * mean) : 0.0;
+  // Attempt rate of the next pass: the expected number of accepted
+  // collisions is rate * sum_i P_accept(v_i), so scale the rate by
+  // Nc / accepted (damped by a square root against Poisson noise).  The
+  // accepted count is a sum over ions, independent of their order.
+  int64_t Nc = collision_target(ctx, dt);
+  if (s.collisions > 0 && Nc > 0) {
+    double f = sqrt((double)Nc / (double)s.collisions);
+    if (f > 2.0) f = 2.0;
+    if (f < 0.5) f = 0.5;
+    ctx->attempt_rate *= f;
+  } else if (Nc > 0 && ctx->attempt_rate > 0) {
+    ctx->attempt_rate *= 2.0;
   }
   if (s.refused >= 10) return ecs_fail(ctx, ECS_ERR_COLLISION, "%llu collisions refused (final speed > 10 viT)", s.refused);
   return ECS_OK;
