@@ -16,10 +16,9 @@
 //
 // Deposition: every contribution is rounded to an integer multiple of 2^-S and
 // added into int64 accumulators, so moments do not depend on the order of
-// particles or atomics (bit-reproducible run to run).  Warps whose 32 lanes
-// share one cell (the common case for cell-sorted particles) combine their
-// 32 values per lane with a register reduce-scatter and issue one atomic per
-// lane; other warps issue per-lane atomics.
+// particles or atomics (bit-reproducible run to run).  A warp transposes its
+// 32 x 32 contributions through shared memory and sums them per cell group, so
+// cell-sorted particles issue about one atomic per node and field per warp.
 //
 // Collisions: the reference picks Nc random ions with replacement and accepts
 // each attempt with the product of two uniforms below |vr|^2/vrm^2
@@ -48,6 +47,82 @@ __device__ __forceinline__ rd operator/(rd a, rd b) { return {__ddiv_rn(a.v, b.v
 
 constexpr int kBlock = 256;
 
+// ---- deposit fixed point ---------------------------------------------------
+// FP64: rint(v 2^S) by the FP64 conversion.
+struct FixScale64 {
+  double s;
+  __device__ __forceinline__ long long put(double v) const { return __double2ll_rn(v * s); }
+};
+
+// FP32: the same integer, rint(v 2^S) with |v 2^S| <= 2^42, from FP32 adds and
+// multiply-adds only (on sm_103 a float-to-int64 conversion issues on the
+// narrow FP64 pipe).  With H = rint(v 2^(S-20)):
+//   v 2^S = H 2^20 + r,  |r| <= 2^19, r exact in FP32,
+//   rint(v 2^S) = H 2^20 + rint(r)   (2^20 H is even, so ties round alike).
+// Both integers come from adding the bias B = 1.5 * 2^23: for |t| <= 2^22,
+// fl(t + B) lies in [2^23, 2^24], where the spacing of floats is 1, so the
+// addition rounds t to the nearest integer (ties to even) and the bit pattern
+// of the sum is bits(B) + rint(t).  The two biased words are stored as one
+// 64-bit tile entry (low word H, high word rint(r)); sums over a group of n
+// lanes remove the bias n * bits(B) from each word (wrap-around int32
+// arithmetic) before recombining in int64.
+constexpr float kFixBias = 12582912.0f;  // 1.5 * 2^23
+constexpr unsigned kFixBiasBits = 0x4B400000u;
+struct FixScale32 {
+  float s, s_hi, s_back;  // 2^S, 2^(S-20), -2^(20-S)
+  __device__ __forceinline__ long long put(float v) const {
+    const float h = __fmaf_rn(v, s_hi, kFixBias);
+    const float r = __fmaf_rn(__fsub_rn(h, kFixBias), s_back, v);
+    const float l = __fmaf_rn(r, s, kFixBias);
+    return (long long)(((unsigned long long)__float_as_uint(l) << 32) | __float_as_uint(h));
+  }
+};
+__device__ __forceinline__ long long fix_unbias(unsigned hi_sum, unsigned lo_sum, int n) {
+  const int hi = (int)(hi_sum - (unsigned)n * kFixBiasBits);
+  const int lo = (int)(lo_sum - (unsigned)n * kFixBiasBits);
+  return (long long)hi * 1048576ll + lo;
+}
+
+// Exact sum of the tile entries q in `m` (bit mask of lanes).
+__device__ __forceinline__ long long group_sum(const long long *row, unsigned m, const FixScale64 &) {
+  long long sum = 0;
+  while (m) {
+    const int q = __ffs(m) - 1;
+    m &= m - 1;
+    sum += row[q];
+  }
+  return sum;
+}
+__device__ __forceinline__ long long group_sum(const long long *row, unsigned m, const FixScale32 &) {
+  const int n = __popc(m);
+  unsigned hs = 0, ls = 0;
+  while (m) {
+    const int q = __ffs(m) - 1;
+    m &= m - 1;
+    const unsigned long long e = (unsigned long long)row[q];
+    hs += (unsigned)e;
+    ls += (unsigned)(e >> 32);
+  }
+  return fix_unbias(hs, ls, n);
+}
+__device__ __forceinline__ long long full_sum(const long long *row, const FixScale64 &) {
+  long long sum = 0;
+#pragma unroll
+  for (int q = 0; q < 32; q++) sum += row[q];
+  return sum;
+}
+__device__ __forceinline__ long long full_sum(const long long *row, const FixScale32 &) {
+  unsigned hs = 0, ls = 0;
+#pragma unroll
+  for (int q = 0; q < 32; q++) {
+    const unsigned long long e = (unsigned long long)row[q];
+    hs += (unsigned)e;
+    ls += (unsigned)(e >> 32);
+  }
+  return fix_unbias(hs, ls, 32);
+}
+
+
 struct PartK {
   int Nx, Ny, Nz;
   int bc[3];
@@ -68,14 +143,12 @@ struct PartK {
   // fixed-point scales of the deposit: density 2^Sn, flux 2^Sf (Sf = Sn - e_v
   // for the velocity bound 2^e_v), and the bound itself
   double fixn64, fixf64;
-  float fixn32, fixf32;
+  FixScale32 fixn32, fixf32;
   double vmax;
+  float vmaxf;
 };
 
 // ---- deposit ---------------------------------------------------------------
-__device__ __forceinline__ long long fix_rn(double v, double s) { return __double2ll_rn(v * s); }
-__device__ __forceinline__ long long fix_rn(float v, float s) { return __float2ll_rn(v * s); }
-
 // Linear node index of corner b (xb = b&1, yb = b>>1&1, zb = b>>2) of cell
 // (i,j,k), or -1 when it falls outside a non-periodic dimension.
 __device__ __forceinline__ long long corner_node(const PartK &k, int i, int j, int kk, int b) {
@@ -101,20 +174,22 @@ __device__ __forceinline__ long long corner_node(const PartK &k, int i, int j, i
 // warp must call this together.
 constexpr int kTileStride = 33;
 
-template <typename T>
+template <typename T, typename Fix>
 __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long long *tile, const PartK &k,
                                              bool active, int i, int j, int kk, T wxh, T wyh,
-                                             T wzh, T v0, T v1, T v2, T sn, T sf) {
+                                             T wzh, T v0, T v1, T v2, const Fix &fn, const Fix &ff) {
   const int lane = threadIdx.x & 31;
   const T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
+  // inactive lanes contribute the zero entry (bias included for FP32)
+  const long long zero = fn.put(T(0));
 #pragma unroll
   for (int b = 0; b < 8; b++) {
     const T wz = (b & 4) ? wzh : wzl, wy = (b & 2) ? wyh : wyl, wx = (b & 1) ? wxh : wxl;
     const T w = wz * wy * wx;
-    tile[(b + 0) * kTileStride + lane] = active ? fix_rn(w, sn) : 0ll;
-    tile[(b + 8) * kTileStride + lane] = active ? fix_rn(v0 * w, sf) : 0ll;
-    tile[(b + 16) * kTileStride + lane] = active ? fix_rn(v1 * w, sf) : 0ll;
-    tile[(b + 24) * kTileStride + lane] = active ? fix_rn(v2 * w, sf) : 0ll;
+    tile[(b + 0) * kTileStride + lane] = active ? fn.put(w) : zero;
+    tile[(b + 8) * kTileStride + lane] = active ? ff.put(v0 * w) : zero;
+    tile[(b + 16) * kTileStride + lane] = active ? ff.put(v1 * w) : zero;
+    tile[(b + 24) * kTileStride + lane] = active ? ff.put(v2 * w) : zero;
   }
   const int key = active ? (i | (j << 10) | (kk << 20)) : -1;
   const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
@@ -123,9 +198,7 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
   unsigned rem = __ballot_sync(ECS_FULL_MASK, active);
   if (rem == ECS_FULL_MASK && peers == ECS_FULL_MASK) {
     // the whole warp deposits into one cell: plain 32-term sums
-    long long sum = 0;
-#pragma unroll
-    for (int q = 0; q < 32; q++) sum += row[q];
+    const long long sum = full_sum(row, fn);
     const long long node = corner_node(k, i, j, kk, lane & 7);
     if (node >= 0 && sum != 0)
       atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
@@ -138,13 +211,7 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
     const int gj = __shfl_sync(ECS_FULL_MASK, j, lead);
     const int gk = __shfl_sync(ECS_FULL_MASK, kk, lead);
     rem &= ~grp;
-    long long sum = 0;
-    unsigned m = grp;
-    while (m) {
-      const int q = __ffs(m) - 1;
-      m &= m - 1;
-      sum += row[q];
-    }
+    const long long sum = group_sum(row, grp, fn);
     const long long node = corner_node(k, gi, gj, gk, lane & 7);
     if (node >= 0 && sum != 0)
       atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
@@ -408,7 +475,8 @@ __device__ __forceinline__ void deposit64(long long *acc, long long *tile, const
   double wx = ok ? (x - rd{(double)i}).v : 0.0;
   double wy = ok ? (y - rd{(double)j}).v : 0.0;
   double wz = ok ? (z - rd{(double)kk}).v : 0.0;
-  deposit_warp<double>(acc, tile, k, ok, i, j, kk, wx, wy, wz, vx, vy, vz, k.fixn64, k.fixf64);
+  deposit_warp<double>(acc, tile, k, ok, i, j, kk, wx, wy, wz, vx, vy, vz, FixScale64{k.fixn64},
+                       FixScale64{k.fixf64});
 }
 
 __device__ __forceinline__ void hash64(double px, double py, double pz, double vx, double vy,
@@ -620,7 +688,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(
     }
     if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
     if (mode & 8) {
-      if (active && !(fabsf(vx) <= (float)k.vmax && fabsf(vy) <= (float)k.vmax && fabsf(vz) <= (float)k.vmax))
+      if (active && !(fabsf(vx) <= k.vmaxf && fabsf(vy) <= k.vmaxf && fabsf(vz) <= k.vmaxf))
         atomicOr(&st->flags, ECS_FLAG_RANGE);
       deposit_warp<float>(acc, tile, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fixn32, k.fixf32);
     }
@@ -898,9 +966,10 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   }
   k.fixn64 = ldexp(1.0, ctx->shift_n);
   k.fixf64 = ldexp(1.0, ctx->shift_f);
-  k.fixn32 = ldexpf(1.0f, ctx->shift_n);
-  k.fixf32 = ldexpf(1.0f, ctx->shift_f);
+  k.fixn32 = {ldexpf(1.0f, ctx->shift_n), ldexpf(1.0f, ctx->shift_n - 20), -ldexpf(1.0f, 20 - ctx->shift_n)};
+  k.fixf32 = {ldexpf(1.0f, ctx->shift_f), ldexpf(1.0f, ctx->shift_f - 20), -ldexpf(1.0f, 20 - ctx->shift_f)};
   k.vmax = ldexp(1.0, ctx->shift_n - ctx->shift_f);
+  k.vmaxf = (float)k.vmax;
   return k;
 }
 
