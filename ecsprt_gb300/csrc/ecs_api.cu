@@ -111,7 +111,7 @@ int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
     b += cap * 48 + ne * 32;
     b += (2 * m + 1) * n * 8 + (int64_t)(n * 8 * 10 * 8 / 7);  // Krylov + multigrid levels
   } else {
-    b += cap * 56 + ne * 16 + n * 4 * 2 + n / 1024 * 4;
+    b += cap * 64 + ne * 16 + n * 4 * 2 + n / 1024 * 4;
     b += (2 * m + 3) * n * 4 + (int64_t)(n * 4 * 10 * 8 / 7);
   }
   return b;
@@ -312,11 +312,8 @@ int ecs_collide(EcsCtx *ctx, double dt) {
 int ecs_move(EcsCtx *ctx, double dt) {
   if (!ctx) return ECS_ERR_INVALID;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
-  int rc = ecs_part_move(ctx, dt);
+  int rc = ecs_part_move(ctx, dt);  // sorts the ions by cell when due
   if (rc) return rc;
-  // DMSwarmMigrate analogue (src/boundaries.c:92): keep particles cell-sorted
-  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ++ctx->steps_since_sort >= ctx->sort_every)
-    if ((rc = ecs_part_sort(ctx))) return rc;
   return read_status(ctx);
 }
 
@@ -377,15 +374,10 @@ int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stat
   if (rc) return rc;
   int sorted = 0;
   ctx->ev_particle = ctx->ev_sort = false;
-  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ctx->steps_since_sort >= ctx->sort_every) {
-    if ((rc = ecs_part_sort(ctx))) return rc;
-    sorted = 1;
-  }
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
-  if ((rc = ecs_part_fused(ctx, dt, 1))) return rc;
+  if ((rc = ecs_part_fused(ctx, dt, 1, &sorted))) return rc;
   EcsDevStatus coll = *ctx->hstat;
   if (ctx->p.mn <= 0.0) memset(&coll, 0, sizeof coll);
-  ctx->steps_since_sort++;
   if ((rc = ecs_grid_moments(ctx))) return rc;
   if ((rc = read_status(ctx))) return rc;
   if ((rc = ecs_grid_rhs(ctx))) return rc;

@@ -72,11 +72,10 @@ struct EcsCtx {
   double *px = nullptr, *py = nullptr, *pz = nullptr;
   double *vx = nullptr, *vy = nullptr, *vz = nullptr;
 
-  // Mixed particles: int32 cell + FP32 in-cell offset + FP32 velocity, SoA,
+  // Mixed particles: one 32-byte record per ion (a DRAM sector), two float4:
+  //   (int32 cell bits, FP32 in-cell offsets ox, oy, oz), (FP32 vx, vy, vz, 0),
   // double-buffered for the counting sort.
-  int32_t *cell[2] = {nullptr, nullptr};
-  float *ox[2] = {nullptr, nullptr}, *oy[2] = {nullptr, nullptr}, *oz[2] = {nullptr, nullptr};
-  float *ux[2] = {nullptr, nullptr}, *uy[2] = {nullptr, nullptr}, *uz[2] = {nullptr, nullptr};
+  float4 *ions[2] = {nullptr, nullptr};
   int cur = 0;
   int32_t *sort_count = nullptr;   // [ncell]
   int32_t *sort_offset = nullptr;  // [ncell+1]
@@ -200,7 +199,7 @@ int ecs_part_push(EcsCtx *ctx, double dt);
 int ecs_part_collide(EcsCtx *ctx, double dt);
 int ecs_part_move(EcsCtx *ctx, double dt);
 int ecs_part_collect(EcsCtx *ctx);
-int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide);
+int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted);
 int ecs_part_sort(EcsCtx *ctx);
 int ecs_part_estimate_rate(EcsCtx *ctx, double dt);
 extern "C" int ecs_fix_shifts(const EcsParams *p, int precision, int32_t *shift_density, int32_t *shift_flux);

@@ -12,7 +12,10 @@
 //     arithmetic operand for operand (separately rounded, no FMA), so push and
 //     move agree bit for bit with the reference.
 //   Mixed: packed int32 cell (i | j<<10 | k<<20) + FP32 in-cell offset in
-//     [0,1) + FP32 velocity, SoA, counting-sorted by cell every few steps.
+//     [0,1) + FP32 velocity in one 32-byte record per ion (a DRAM sector, so
+//     the sort's scattered writes never leave a sector half written),
+//     counting-sorted by cell every few steps; the cells are counted by the
+//     particle pass that precedes the sort.
 //
 // Deposition: every contribution is rounded to an integer multiple of 2^-S and
 // added into int64 accumulators, so moments do not depend on the order of
@@ -557,6 +560,34 @@ __device__ __forceinline__ void unpack_cell(int32_t c, int &i, int &j, int &kk) 
   kk = (c >> 20) & 1023;
 }
 
+// Ion record ip: two float4 at ions[2 ip], ions[2 ip + 1].  The particle
+// arrays are far larger than L2, so they are streamed (evict-first).
+struct Ion {
+  int32_t c;
+  float ox, oy, oz, vx, vy, vz;
+};
+__device__ __forceinline__ Ion load_ion(const float4 *ions, int64_t ip) {
+  const float4 a = __ldcs(ions + 2 * ip), b = __ldcs(ions + 2 * ip + 1);
+  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z};
+}
+__device__ __forceinline__ void store_ion(float4 *ions, int64_t ip, const Ion &q) {
+  __stcs(ions + 2 * ip, make_float4(__int_as_float(q.c), q.ox, q.oy, q.oz));
+  __stcs(ions + 2 * ip + 1, make_float4(q.vx, q.vy, q.vz, 0.f));
+}
+__device__ __forceinline__ int32_t ion_cell(const float4 *ions, int64_t ip) {
+  return __ldcs(reinterpret_cast<const int32_t *>(ions) + 8 * ip);
+}
+__device__ __forceinline__ int lin_cell(int32_t c, int Nx, int Ny) {
+  return (((c >> 20) & 1023) * Ny + ((c >> 10) & 1023)) * Nx + (c & 1023);
+}
+
+// Warp-aggregated count of the lanes' cells (inactive lanes pass key < 0).
+__device__ __forceinline__ void count_cells(int32_t *__restrict__ count, int key) {
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+  if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
+}
+
 __device__ __forceinline__ void gather32(const float4 *__restrict__ E, const PartK &k, int i,
                                          int j, int kk, float wx, float wy, float wz, float f[3]) {
   const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
@@ -627,11 +658,10 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
   state_hash(w, 7, h0, h1);
 }
 
-__global__ void __launch_bounds__(kBlock, 3) k_particles32(
-    PartK k, int mode, int64_t np, int32_t *__restrict__ cella, float *__restrict__ oxa,
-    float *__restrict__ oya, float *__restrict__ oza, float *__restrict__ uxa,
-    float *__restrict__ uya, float *__restrict__ uza, const float4 *__restrict__ E,
-    long long *__restrict__ acc, EcsDevStatus *st) {
+__global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, int64_t np, float4 *ions,
+                                                         const float4 *__restrict__ E,
+                                                         long long *__restrict__ acc,
+                                                         int32_t *__restrict__ count, EcsDevStatus *st) {
   extern __shared__ long long shm_tiles[];
   long long *tile = shm_tiles + (threadIdx.x >> 5) * 32 * kTileStride;
   const int64_t lane = threadIdx.x & 31;
@@ -640,13 +670,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(
        base += stride) {
     const int64_t ip = base + lane;
     const bool active = ip < np;
-    int32_t c = 0;
-    float ox = 0.f, oy = 0.f, oz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
-    if (active) {
-      c = cella[ip];
-      ox = oxa[ip]; oy = oya[ip]; oz = oza[ip];
-      vx = uxa[ip]; vy = uya[ip]; vz = uza[ip];
-    }
+    Ion q = {0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (active) q = load_ion(ions, ip);
+    float ox = q.ox, oy = q.oy, oz = q.oz, vx = q.vx, vy = q.vy, vz = q.vz;
+    int32_t c = q.c;
     int i, j, kk;
     unpack_cell(c, i, j, kk);
     if ((mode & 1) && active) {
@@ -686,16 +713,14 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(
       }
       c = i | (j << 10) | (kk << 20);
     }
+    if (count) count_cells(count, active ? (kk * k.Ny + j) * k.Nx + i : -1);
     if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
     if (mode & 8) {
       if (active && !(fabsf(vx) <= k.vmaxf && fabsf(vy) <= k.vmaxf && fabsf(vz) <= k.vmaxf))
         atomicOr(&st->flags, ECS_FLAG_RANGE);
       deposit_warp<float>(acc, tile, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fixn32, k.fixf32);
     }
-    if (active) {
-      if (mode & 4) { cella[ip] = c; oxa[ip] = ox; oya[ip] = oy; oza[ip] = oz; }
-      if (mode & 7) { uxa[ip] = vx; uya[ip] = vy; uza[ip] = vz; }
-    }
+    if (active && (mode & 7)) store_ion(ions, ip, {c, ox, oy, oz, vx, vy, vz});
   }
 }
 
@@ -733,49 +758,40 @@ __device__ __forceinline__ int to_cell(double pos, double d, int N, float &o) {
 }
 
 __global__ void k_aos_to_mixed(int64_t n, PartK k, const double *__restrict__ pos,
-                               const double *__restrict__ vel, int32_t *cell, float *ox,
-                               float *oy, float *oz, float *ux, float *uy, float *uz) {
+                               const double *__restrict__ vel, float4 *__restrict__ ions) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float a, b, c;
     int ci = to_cell(pos[3 * i], k.dx, k.Nx, a);
     int cj = to_cell(pos[3 * i + 1], k.dy, k.Ny, b);
     int ck = to_cell(pos[3 * i + 2], k.dz, k.Nz, c);
-    cell[i] = ci | (cj << 10) | (ck << 20);
-    ox[i] = a; oy[i] = b; oz[i] = c;
-    ux[i] = (float)vel[3 * i]; uy[i] = (float)vel[3 * i + 1]; uz[i] = (float)vel[3 * i + 2];
+    store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[3 * i], (float)vel[3 * i + 1],
+                        (float)vel[3 * i + 2]});
   }
 }
 
 __global__ void k_mixed_to_aos(int64_t n, PartK k, double *__restrict__ pos,
-                               double *__restrict__ vel, const int32_t *cell, const float *ox,
-                               const float *oy, const float *oz, const float *ux,
-                               const float *uy, const float *uz) {
+                               double *__restrict__ vel, const float4 *__restrict__ ions) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
+    const Ion q = load_ion(ions, i);
     int ci, cj, ck;
-    unpack_cell(cell[i], ci, cj, ck);
-    pos[3 * i] = ((double)ci + (double)ox[i]) * k.dx;
-    pos[3 * i + 1] = ((double)cj + (double)oy[i]) * k.dy;
-    pos[3 * i + 2] = ((double)ck + (double)oz[i]) * k.dz;
-    vel[3 * i] = ux[i]; vel[3 * i + 1] = uy[i]; vel[3 * i + 2] = uz[i];
+    unpack_cell(q.c, ci, cj, ck);
+    pos[3 * i] = ((double)ci + (double)q.ox) * k.dx;
+    pos[3 * i + 1] = ((double)cj + (double)q.oy) * k.dy;
+    pos[3 * i + 2] = ((double)ck + (double)q.oz) * k.dz;
+    vel[3 * i] = q.vx; vel[3 * i + 1] = q.vy; vel[3 * i + 2] = q.vz;
   }
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
-__device__ __forceinline__ int lin_cell(int32_t c, int Nx, int Ny) {
-  return (((c >> 20) & 1023) * Ny + ((c >> 10) & 1023)) * Nx + (c & 1023);
-}
-
-__global__ void k_sort_count(int64_t np, int Nx, int Ny, const int32_t *__restrict__ cell,
+__global__ void k_sort_count(int64_t np, int Nx, int Ny, const float4 *__restrict__ ions,
                              int32_t *__restrict__ count) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
-    int64_t ip = base + lane;
-    int key = ip < np ? lin_cell(cell[ip], Nx, Ny) : -1;
-    unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
-    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
+    const int64_t ip = base + lane;
+    count_cells(count, ip < np ? lin_cell(ion_cell(ions, ip), Nx, Ny) : -1);
   }
 }
 
@@ -852,31 +868,31 @@ __global__ void k_scan_add(int n, int32_t *__restrict__ out, const int32_t *__re
   if (i == n - 1 && total_out) *total_out = out[i];
 }
 
+// Every ion record moves whole (32 bytes, one sector) to slot
+// off[cell] + (its rank among the ions of its cell), ranks handed out by a
+// warp-aggregated atomic cursor per cell.
 __global__ void k_sort_scatter(int64_t np, int Nx, int Ny, const int32_t *__restrict__ off,
-                               int32_t *__restrict__ cursor, const int32_t *__restrict__ c0,
-                               const float *__restrict__ a0, const float *__restrict__ b0,
-                               const float *__restrict__ d0, const float *__restrict__ e0,
-                               const float *__restrict__ f0, const float *__restrict__ g0,
-                               int32_t *__restrict__ c1, float *__restrict__ a1,
-                               float *__restrict__ b1, float *__restrict__ d1,
-                               float *__restrict__ e1, float *__restrict__ f1,
-                               float *__restrict__ g1) {
+                               int32_t *__restrict__ cursor, const float4 *__restrict__ src,
+                               float4 *__restrict__ dst) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
-    int64_t ip = base + lane;
-    int32_t c = ip < np ? c0[ip] : 0;
-    int key = ip < np ? lin_cell(c, Nx, Ny) : -1;
-    unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
-    int leader = __ffs(peers) - 1;
+    const int64_t ip = base + lane;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (ip < np) {
+      a = __ldcs(src + 2 * ip);
+      b = __ldcs(src + 2 * ip + 1);
+    }
+    const int key = ip < np ? lin_cell(__float_as_int(a.x), Nx, Ny) : -1;
+    const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
+    const int leader = __ffs(peers) - 1;
     int slot = 0;
     if (key >= 0 && lane == leader) slot = atomicAdd(&cursor[key], __popc(peers));
     slot = __shfl_sync(ECS_FULL_MASK, slot, leader);
     if (key >= 0) {
-      int64_t dst = (int64_t)off[key] + slot + __popc(peers & ((1u << lane) - 1u));
-      c1[dst] = c;
-      a1[dst] = a0[ip]; b1[dst] = b0[ip]; d1[dst] = d0[ip];
-      e1[dst] = e0[ip]; f1[dst] = f0[ip]; g1[dst] = g0[ip];
+      const int64_t d = (int64_t)off[key] + slot + __popc(peers & ((1u << lane) - 1u));
+      __stcs(dst + 2 * d, a);
+      __stcs(dst + 2 * d + 1, b);
     }
   }
 }
@@ -900,9 +916,7 @@ __global__ void k_estimate64(PartK k, int64_t np, const double *px, const double
     flush_samples(st, sample, active);
   }
 }
-__global__ void k_estimate32(PartK k, int64_t np, const int32_t *cella, const float *oxa,
-                             const float *oya, const float *oza, const float *uxa,
-                             const float *uya, const float *uza, EcsDevStatus *st) {
+__global__ void k_estimate32(PartK k, int64_t np, const float4 *__restrict__ ions, EcsDevStatus *st) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -910,10 +924,10 @@ __global__ void k_estimate32(PartK k, int64_t np, const int32_t *cella, const fl
     bool active = ip < np;
     float sample = 0.f;
     if (active) {
-      float vx = uxa[ip], vy = uya[ip], vz = uza[ip];
+      const Ion q = load_ion(ions, ip);
       uint32_t h0, h1;
-      hash32(cella[ip], oxa[ip], oya[ip], oza[ip], vx, vy, vz, h0, h1);
-      sample = accept_sample<float>(k, h0, h1, vx, vy, vz);
+      hash32(q.c, q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, h0, h1);
+      sample = accept_sample<float>(k, h0, h1, q.vx, q.vy, q.vz);
     }
     flush_samples(st, sample, active);
   }
@@ -1007,11 +1021,7 @@ int ecs_particles_alloc(EcsCtx *ctx) {
     double **arr[6] = {&ctx->px, &ctx->py, &ctx->pz, &ctx->vx, &ctx->vy, &ctx->vz};
     for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(double)));
   } else {
-    for (int b = 0; b < 2; b++) {
-      ECS_CUDA(ctx, cudaMalloc((void **)&ctx->cell[b], n * sizeof(int32_t)));
-      float **arr[6] = {&ctx->ox[b], &ctx->oy[b], &ctx->oz[b], &ctx->ux[b], &ctx->uy[b], &ctx->uz[b]};
-      for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(float)));
-    }
+    for (int b = 0; b < 2; b++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->ions[b], n * 2 * sizeof(float4)));
     size_t nb = ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
     ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_count, ctx->ncell * sizeof(int32_t)));
     ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_offset, (ctx->ncell + 1) * sizeof(int32_t)));
@@ -1021,10 +1031,8 @@ int ecs_particles_alloc(EcsCtx *ctx) {
 }
 
 int ecs_particles_free(EcsCtx *ctx) {
-  void *ptrs[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz,
-                  ctx->cell[0], ctx->cell[1], ctx->ox[0], ctx->ox[1], ctx->oy[0], ctx->oy[1],
-                  ctx->oz[0], ctx->oz[1], ctx->ux[0], ctx->ux[1], ctx->uy[0], ctx->uy[1],
-                  ctx->uz[0], ctx->uz[1], ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
+  void *ptrs[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ions[0], ctx->ions[1],
+                  ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   return ECS_OK;
@@ -1047,10 +1055,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
       k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
                                                    ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      int b = ctx->cur;
-      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->cell[b] + off, ctx->ox[b] + off,
-                                                   ctx->oy[b] + off, ctx->oz[b] + off, ctx->ux[b] + off,
-                                                   ctx->uy[b] + off, ctx->uz[b] + off);
+      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->ions[ctx->cur] + 2 * off);
     }
     ECS_LAUNCHED(ctx);
   }
@@ -1078,10 +1083,7 @@ int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
       k_soa_to_aos64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
                                                    ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      int b = ctx->cur;
-      k_mixed_to_aos<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->cell[b] + off, ctx->ox[b] + off,
-                                                   ctx->oy[b] + off, ctx->oz[b] + off, ctx->ux[b] + off,
-                                                   ctx->uy[b] + off, ctx->uz[b] + off);
+      k_mixed_to_aos<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->ions[ctx->cur] + 2 * off);
     }
     ECS_LAUNCHED(ctx);
     if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + 3 * off, stage, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1092,7 +1094,9 @@ int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
   return ECS_OK;
 }
 
-static int launch_particles(EcsCtx *ctx, double dt, int mode) {
+// One pass of the particle kernel over all ions.  With `count_for_sort` the
+// pass also counts the ions' (new) cells for the counting sort that follows.
+static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sort = false) {
   if (ctx->np == 0) return ECS_OK;
   PartK k = make_k(ctx, dt);
   if ((mode & 2) && k.collide) {
@@ -1112,16 +1116,19 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode) {
     cudaFuncSetAttribute(k_particles32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     attr_set = true;
   }
+  int32_t *count = nullptr;
+  if (count_for_sort && ctx->prec == ECS_PREC_MIXED) {
+    ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+    count = ctx->sort_count;
+  }
   unsigned int g = grid_blocks(ctx, ctx->np, 3);
   if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
   if (ctx->prec == ECS_PREC_FP64) {
     k_particles64<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                                 ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
   } else {
-    int b = ctx->cur;
-    k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b],
-                                                ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b],
-                                                ctx->eext32, ctx->acc, ctx->dstat);
+    k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
+                                                count, ctx->dstat);
   }
   ECS_LAUNCHED(ctx);
   if (ctx->ev[1]) {
@@ -1161,9 +1168,7 @@ int ecs_part_estimate_rate(EcsCtx *ctx, double dt) {
     k_estimate64<<<g, kBlock, 0, ctx->stream>>>(k, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy,
                                                ctx->vz, ctx->dstat);
   } else {
-    int b = ctx->cur;
-    k_estimate32<<<g, kBlock, 0, ctx->stream>>>(k, ctx->np, ctx->cell[b], ctx->ox[b], ctx->oy[b], ctx->oz[b],
-                                               ctx->ux[b], ctx->uy[b], ctx->uz[b], ctx->dstat);
+    k_estimate32<<<g, kBlock, 0, ctx->stream>>>(k, ctx->np, ctx->ions[ctx->cur], ctx->dstat);
   }
   ECS_LAUNCHED(ctx);
   ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1183,35 +1188,17 @@ int ecs_part_collide(EcsCtx *ctx, double dt) {
   ctx->step_index++;
   return rc;
 }
-int ecs_part_move(EcsCtx *ctx, double dt) { return launch_particles(ctx, dt, 4); }
-int ecs_part_collect(EcsCtx *ctx) {
-  int rc = ecs_grid_clear_acc(ctx);
-  if (rc) return rc;
-  return launch_particles(ctx, 0.0, 8);
-}
-int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide) {
-  int rc = ecs_grid_clear_acc(ctx);
-  if (rc) return rc;
-  int collide = do_collide && ctx->p.mn > 0.0;
-  rc = launch_particles(ctx, dt, 1 | (collide ? 2 : 0) | 4 | 8);
-  if (rc) return rc;
-  if (collide) {
-    rc = finish_collisions(ctx, dt);
-    ctx->step_index++;
-  }
-  return rc;
+
+// Whether the pass that moves the ions now is followed by a cell sort.
+static bool sort_due(const EcsCtx *ctx) {
+  return ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ctx->steps_since_sort + 1 >= ctx->sort_every;
 }
 
-int ecs_part_sort(EcsCtx *ctx) {
-  if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0) return ECS_OK;
+// Scan of the cell counts and the scatter into the other buffer.
+static int sort_counted(EcsCtx *ctx) {
   const int n = (int)ctx->ncell;
   const int nb = (int)ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
-  int a = ctx->cur, b = 1 - ctx->cur;
-  unsigned int g = grid_blocks(ctx, ctx->np, 8);
-  if (ctx->ev[2]) cudaEventRecord(ctx->ev[2], ctx->stream);
-  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
-  k_sort_count<<<g, kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->cell[a], ctx->sort_count);
-  ECS_LAUNCHED(ctx);
+  const int a = ctx->cur, b = 1 - ctx->cur;
   k_scan_local<<<nb, kScanBlock, 0, ctx->stream>>>(n, ctx->sort_count, ctx->sort_offset, ctx->scan_blocks);
   ECS_LAUNCHED(ctx);
   k_scan_sums<<<1, 1024, 0, ctx->stream>>>(nb, ctx->scan_blocks);
@@ -1219,16 +1206,64 @@ int ecs_part_sort(EcsCtx *ctx) {
   k_scan_add<<<ecs_div_up(ctx->ncell, 256), 256, 0, ctx->stream>>>(n, ctx->sort_offset, ctx->scan_blocks, nullptr);
   ECS_LAUNCHED(ctx);
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
-  k_sort_scatter<<<g, kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->sort_offset, ctx->sort_count,
-                                               ctx->cell[a], ctx->ox[a], ctx->oy[a], ctx->oz[a], ctx->ux[a],
-                                               ctx->uy[a], ctx->uz[a], ctx->cell[b], ctx->ox[b], ctx->oy[b],
-                                               ctx->oz[b], ctx->ux[b], ctx->uy[b], ctx->uz[b]);
+  k_sort_scatter<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(
+      ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->sort_offset, ctx->sort_count, ctx->ions[a], ctx->ions[b]);
   ECS_LAUNCHED(ctx);
+  ctx->cur = b;
+  ctx->steps_since_sort = 0;
+  return ECS_OK;
+}
+
+static int sort_after_pass(EcsCtx *ctx, bool counted) {
+  if (!counted) {
+    ctx->steps_since_sort++;
+    return ECS_OK;
+  }
+  if (ctx->ev[2]) cudaEventRecord(ctx->ev[2], ctx->stream);
+  int rc = sort_counted(ctx);
+  if (rc) return rc;
   if (ctx->ev[3]) {
     cudaEventRecord(ctx->ev[3], ctx->stream);
     ctx->ev_sort = true;
   }
-  ctx->cur = b;
-  ctx->steps_since_sort = 0;
   return ECS_OK;
+}
+
+// UpdatePositions + ApplyBC, then (DMSwarmMigrate analogue,
+// src/boundaries.c:92) the cell sort when it is due.
+int ecs_part_move(EcsCtx *ctx, double dt) {
+  const bool counted = sort_due(ctx) && ctx->np > 0;
+  int rc = launch_particles(ctx, dt, 4, counted);
+  if (rc) return rc;
+  return sort_after_pass(ctx, counted);
+}
+int ecs_part_collect(EcsCtx *ctx) {
+  int rc = ecs_grid_clear_acc(ctx);
+  if (rc) return rc;
+  return launch_particles(ctx, 0.0, 8);
+}
+int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
+  int rc = ecs_grid_clear_acc(ctx);
+  if (rc) return rc;
+  int collide = do_collide && ctx->p.mn > 0.0;
+  const bool counted = sort_due(ctx) && ctx->np > 0;
+  rc = launch_particles(ctx, dt, 1 | (collide ? 2 : 0) | 4 | 8, counted);
+  if (rc) return rc;
+  if ((rc = sort_after_pass(ctx, counted))) return rc;
+  if (sorted) *sorted = counted ? 1 : 0;
+  if (collide) {
+    rc = finish_collisions(ctx, dt);
+    ctx->step_index++;
+  }
+  return rc;
+}
+
+// Full counting sort (count pass included), used after an upload.
+int ecs_part_sort(EcsCtx *ctx) {
+  if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0) return ECS_OK;
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+  k_sort_count<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny,
+                                                                        ctx->ions[ctx->cur], ctx->sort_count);
+  ECS_LAUNCHED(ctx);
+  return sort_counted(ctx);
 }
