@@ -171,6 +171,10 @@ class Context:
     def set_warm_start(self, warm: bool):
         self._check(self._lib.ecs_set_warm_start(self._h, 1 if warm else 0))
 
+    def set_solver_graphs(self, on: bool):
+        """Run each FGMRES cycle as one CUDA graph (default) or step by step."""
+        self._check(self._lib.ecs_set_solver_graphs(self._h, 1 if on else 0))
+
     # ---- data ----------------------------------------------------------
     def upload_particles(self, pos: np.ndarray, vel: np.ndarray):
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)

@@ -97,6 +97,7 @@ GPU_API = [
     ("ecs_set_sort_every", C.c_int, [_vp, C.c_int]),
     ("ecs_set_seed", C.c_int, [_vp, C.c_uint64]),
     ("ecs_set_warm_start", C.c_int, [_vp, C.c_int]),
+    ("ecs_set_solver_graphs", C.c_int, [_vp, C.c_int]),
     ("ecs_particles_upload", C.c_int, [_vp, _vp, _vp, C.c_int64]),
     ("ecs_particles_download", C.c_int, [_vp, _vp, _vp]),
     ("ecs_particles_count", C.c_int64, [_vp]),

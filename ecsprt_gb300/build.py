@@ -35,7 +35,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CC_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-Wno-unused-parameter", f"-I{INCLUDE}"]
 
-GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu", "ecs_noalloc.cu"]
+GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu", "ecs_solver.cu", "ecs_noalloc.cu"]
 HOST_SOURCES = ["ecs_options.c", "ecs_io.c"]
 GPU_HOST_SOURCES = ["ecs_ops.c"]  # host C linked into libecsgpu (operator slots)
 

@@ -228,6 +228,12 @@ int ecs_set_warm_start(EcsCtx *ctx, int warm) {
   return ECS_OK;
 }
 
+int ecs_set_solver_graphs(EcsCtx *ctx, int on) {
+  if (!ctx) return ECS_ERR_INVALID;
+  ctx->use_graphs = on ? 1 : 0;
+  return ECS_OK;
+}
+
 int ecs_particles_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np) {
   if (!ctx || (np > 0 && (!pos || !vel))) return ECS_ERR_INVALID;
   int rc = ecs_part_upload(ctx, pos, vel, np);

@@ -57,6 +57,14 @@ struct Multigrid {
   bool built = false;
 };
 
+// Instantiated graph of one FGMRES cycle (per arithmetic type).
+struct SolverGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t kernels_fixed = 0;  // kernels before and after the Arnoldi loop
+  int64_t kernels_step = 0;   // kernels of one Arnoldi step
+};
+
 struct EcsCtx {
   EcsParams p;
   int prec = ECS_PREC_FP64;
@@ -103,8 +111,15 @@ struct EcsCtx {
   float *kz32 = nullptr;
   double *w64 = nullptr;            // FP64 work vectors
   double *r64 = nullptr;
-  double *dots = nullptr;           // device dot results [m+2]
+  double *dots = nullptr;           // device scalars (norms, means) [m+2]
   double *h_dots = nullptr;         // pinned host copy
+  void *kdev = nullptr;             // device FGMRES control block
+  void *kdev_host = nullptr;        // pinned copy read back after a cycle
+  void *kctl_host = nullptr;        // pinned staging of the cycle's tolerance and step limit
+  SolverGraph graph64, graph32;     // one FGMRES cycle as a CUDA graph
+  int use_graphs = 1;               // 0: the host launches the Arnoldi steps one by one
+  void *graph_pending = nullptr;    // SolverGraph launched, kernels not yet counted
+  cudaEvent_t ev_solve[2] = {nullptr, nullptr};
   bool lhs_ready = false;
   bool moments_ready = false;
   bool eext_ready = false;          // difference numerators valid for the current phi
@@ -181,11 +196,12 @@ __device__ __forceinline__ uint32_t ecs_mix32(uint32_t h) {
 }
 
 // ---- kernels launched from several translation units --------------------
-// (defined in ecs_grid.cu)
+// (defined in ecs_grid.cu and ecs_solver.cu)
 int ecs_grid_eext(EcsCtx *ctx);          // difference numerators from phi
 int ecs_grid_moments(EcsCtx *ctx);       // fixed-point -> FP64 moments
 int ecs_grid_rhs(EcsCtx *ctx);           // RHS (+ mean removal) from moments
 int ecs_grid_clear_acc(EcsCtx *ctx);
+int ecs_solver_alloc(EcsCtx *ctx);       // reductions, Krylov bases, control block
 int ecs_solver_setup(EcsCtx *ctx);       // multigrid hierarchy from the density
 int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st);
 int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y);

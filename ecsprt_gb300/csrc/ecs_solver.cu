@@ -1,0 +1,1279 @@
+// Potential solve of the ECSPRT hot path on sm_103a: the matrix-free
+// 11-point operator of src/lhs.c:337-505 and the KSP solve of
+// src/potential.c:6-15.
+//
+// FGMRES(m) preconditioned by one geometric-multigrid V(1,1) cycle (full
+// coarsening, full-weighting restriction, trilinear prolongation, coarse
+// operators rediscretised from the full-weighted density, damped z-line
+// Jacobi smoothing: the z couplings carry (1+kappa^2) and dominate).
+//   ECS_PREC_FP64:  FGMRES and multigrid in FP64 to the requested rtol.
+//   ECS_PREC_MIXED: FP64 iterative refinement; each correction is an FP32
+//     FGMRES/multigrid solve; residuals, their norms, the update of phi and
+//     the mean projection are FP64.
+//
+// One FGMRES cycle runs entirely on the device: the Gram-Schmidt
+// coefficients, the Hessenberg matrix, the Givens rotations and the
+// convergence test live in a device control block (KrylovDev), and the
+// kernels that need the Arnoldi index read it from there.  The cycle is a
+// CUDA graph whose Arnoldi step is the body of a conditional WHILE node; the
+// step's last small kernel clears the condition once the residual estimate
+// meets the tolerance, so the host waits once per cycle.  Without graphs the
+// host launches the same kernels step by step and reads the stop flag after
+// each step.
+//
+// All reductions use fixed block partials summed in a fixed order, so every
+// result is reproducible run to run.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ecs_stencil.cuh"
+
+namespace {
+
+constexpr int kKrylovMax = 30;            // restart length m (upper bound)
+constexpr int kSlots = kKrylovMax + 2;    // dot-product slots per pass
+constexpr int kDotBlocks = 1024;          // block partials per dot pass
+constexpr int kB = 256;
+
+// Device control block of one FGMRES cycle.
+struct KrylovDev {
+  // set by the host before a cycle
+  double tol_rel;  // stop when the estimate <= tol_rel * beta
+  int maxit;       // Arnoldi steps allowed in this cycle (<= kKrylovMax)
+  int pad0;
+  // cycle state
+  int j;           // current Arnoldi index
+  int jprev;       // index of the step that just finished
+  int done;        // 1: converged, broke down or out of steps
+  int nits;        // Arnoldi steps taken
+  double beta, res, inv_scale, mean;
+  double h1[kSlots], h2[kSlots];
+  double H[(kKrylovMax + 1) * kKrylovMax];
+  double cs[kKrylovMax], sn[kKrylovMax], g[kKrylovMax + 1], y[kKrylovMax];
+};
+
+// ---- operator ------------------------------------------------------------------
+// y = A x   (mode 0)     or     y = b - A x   (mode 1)
+template <typename T>
+__global__ void k_apply(OpK o, const T *__restrict__ n, const T *__restrict__ x, const T *__restrict__ b,
+                        T *__restrict__ y, int mode) {
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const unsigned c = lin3(o.g, i, j, k);
+  const T s = apply_row(n, x, o, i, j, k);
+  y[c] = mode ? b[c] - s : s;
+}
+
+// ---- z-line smoother --------------------------------------------------------------
+// Column (i,j) carries the z-tridiagonal part of the rows: lo = z- entry,
+// diag = centre, up = z+ entry.  A periodic z closes the cycle, solved with
+// Sherman-Morrison around the Thomas factorisation of the modified matrix;
+// reflecting z drops the out-of-range couplings (Dirichlet-0 ghosts).
+template <typename T>
+struct ZlP {
+  T *a, *cp, *minv, *q, *dp;  // per cell
+  T *a0g, *qden;              // per column
+};
+
+template <typename T>
+__global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z) {
+  const GridG &g = o.g;
+  const int ncol = g.nx * g.ny;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int i = col % g.nx, j = col / g.nx;
+  const size_t plane = (size_t)g.nx * g.ny;
+  const bool cyc = g.bc[2] == 0;
+  const int N = g.nz;
+  T v[11];
+  row11(n, o, i, j, 0, v);
+  const T lo0 = cyc ? v[5] : T(0), d0 = v[10];
+  const T gamma = -d0;
+  T cp_prev = T(0), dq_prev = T(0);
+  // forward: factor T' and forward-substitute u = (gamma, 0, .., up_{N-1})
+  for (int k = 0; k < N; k++) {
+    row11(n, o, i, j, k, v);
+    T a = (k == 0) ? T(0) : v[5];
+    T up = (k == N - 1) ? T(0) : v[4];
+    T bb = v[10];
+    if (cyc && k == 0) bb = d0 - gamma;
+    if (cyc && k == N - 1) bb = v[10] - v[4] * lo0 / gamma;
+    T m = bb - a * cp_prev;
+    T minv = T(1) / m;
+    T cp = up * minv;
+    T u = cyc ? ((k == 0) ? gamma : ((k == N - 1) ? v[4] : T(0))) : T(0);
+    T dq = (u - a * dq_prev) * minv;
+    size_t c = (size_t)k * plane + col;
+    z.a[c] = a;
+    z.cp[c] = cp;
+    z.minv[c] = minv;
+    z.q[c] = dq;
+    cp_prev = cp;
+    dq_prev = dq;
+  }
+  // backward substitution for q
+  T qn = z.q[(size_t)(N - 1) * plane + col];
+  for (int k = N - 2; k >= 0; k--) {
+    size_t c = (size_t)k * plane + col;
+    qn = z.q[c] - z.cp[c] * qn;
+    z.q[c] = qn;
+  }
+  if (cyc) {
+    T a0g = lo0 / gamma;
+    T q0 = z.q[col], qN = z.q[(size_t)(N - 1) * plane + col];
+    z.a0g[col] = a0g;
+    z.qden[col] = T(1) / (T(1) + q0 + a0g * qN);
+  } else {
+    z.a0g[col] = T(0);
+    z.qden[col] = T(0);
+  }
+}
+
+// Right-hand side of the z-line systems: r = b - A_xy xo.
+template <typename T>
+__global__ void k_zline_rhs(OpK o, const T *__restrict__ n, const T *__restrict__ b, const T *__restrict__ xo,
+                            T *__restrict__ r) {
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const unsigned c = lin3(o.g, i, j, k);
+  r[c] = zline_rhs_at(n, b, xo, o, i, j, k, c);
+}
+
+constexpr int kZChunk = 8;
+
+// Thomas solve of one column with the precomputed factors (a, cp, minv) and
+// the Sherman-Morrison closure (q, a0g, qden), then damping against xo
+// (nullptr: zero).  Loads of chunk c+1 are issued before chunk c is used.
+template <typename T>
+__device__ __forceinline__ void zline_column(const GridG &g, const ZlP<T> &z, const T *__restrict__ r,
+                                             const T *__restrict__ xo, T *__restrict__ xn, T omega, int col) {
+  const size_t plane = (size_t)g.nx * g.ny;
+  const int N = g.nz;
+  T ra[kZChunk], aa[kZChunk], ma[kZChunk];
+  T rb[kZChunk], ab[kZChunk], mb[kZChunk];
+#pragma unroll
+  for (int q = 0; q < kZChunk; q++) {
+    size_t c = (size_t)q * plane + col;
+    bool in = q < N;
+    ra[q] = in ? r[c] : T(0);
+    aa[q] = in ? z.a[c] : T(0);
+    ma[q] = in ? z.minv[c] : T(0);
+  }
+  T dp = T(0);
+  for (int k0 = 0; k0 < N; k0 += kZChunk) {
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {  // prefetch next chunk
+      int k = k0 + kZChunk + q;
+      size_t c = (size_t)k * plane + col;
+      bool in = k < N;
+      rb[q] = in ? r[c] : T(0);
+      ab[q] = in ? z.a[c] : T(0);
+      mb[q] = in ? z.minv[c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      if (k < N) {
+        dp = (ra[q] - aa[q] * dp) * ma[q];
+        z.dp[(size_t)k * plane + col] = dp;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      ra[q] = rb[q];
+      aa[q] = ab[q];
+      ma[q] = mb[q];
+    }
+  }
+  // backward substitution, chunks from the top
+  T y = T(0);
+  const T yN = z.dp[(size_t)(N - 1) * plane + col];
+  const int last0 = ((N - 1) / kZChunk) * kZChunk;
+  T da[kZChunk], ca[kZChunk], db[kZChunk], cb[kZChunk];
+#pragma unroll
+  for (int q = 0; q < kZChunk; q++) {
+    int k = last0 + q;
+    size_t c = (size_t)k * plane + col;
+    bool in = k < N;
+    da[q] = in ? z.dp[c] : T(0);
+    ca[q] = in ? z.cp[c] : T(0);
+  }
+  for (int k0 = last0; k0 >= 0; k0 -= kZChunk) {
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 - kZChunk + q;
+      size_t c = (size_t)(k < 0 ? 0 : k) * plane + col;
+      bool in = k >= 0;
+      db[q] = in ? z.dp[c] : T(0);
+      cb[q] = in ? z.cp[c] : T(0);
+    }
+#pragma unroll
+    for (int q = kZChunk - 1; q >= 0; q--) {
+      int k = k0 + q;
+      if (k < N) {
+        y = (k == N - 1) ? da[q] : da[q] - ca[q] * y;
+        z.dp[(size_t)k * plane + col] = y;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      da[q] = db[q];
+      ca[q] = cb[q];
+    }
+  }
+  const T s = (y + z.a0g[col] * yN) * z.qden[col];
+  for (int k0 = 0; k0 < N; k0 += kZChunk) {
+    T yv[kZChunk], qv[kZChunk], ov[kZChunk];
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      size_t c = (size_t)k * plane + col;
+      bool in = k < N;
+      yv[q] = in ? z.dp[c] : T(0);
+      qv[q] = in ? z.q[c] : T(0);
+      ov[q] = (in && xo) ? xo[c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kZChunk; q++) {
+      int k = k0 + q;
+      if (k < N) xn[(size_t)k * plane + col] = ov[q] + omega * ((yv[q] - s * qv[q]) - ov[q]);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_zline_solve(GridG g, ZlP<T> z, const T *__restrict__ r, const T *__restrict__ xo,
+                              T *__restrict__ xn, T omega) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= g.nx * g.ny) return;
+  zline_column<T>(g, z, r, xo, xn, omega, col);
+}
+
+// ---- inter-grid transfer ---------------------------------------------------------
+// Full weighting (1/4,1/2,1/4 per axis) from fine (2I+a) to coarse I.
+template <typename T>
+__device__ __forceinline__ T restrict_at(const GridG &gf, const T *__restrict__ f, int I, int J, int K) {
+  T s = T(0);
+#pragma unroll
+  for (int dk = -1; dk <= 1; dk++) {
+    T wk = dk == 0 ? T(0.5) : T(0.25);
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+      T wj = dj == 0 ? T(0.5) : T(0.25);
+#pragma unroll
+      for (int di = -1; di <= 1; di++) {
+        T wi = di == 0 ? T(0.5) : T(0.25);
+        s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
+      }
+    }
+  }
+  return s;
+}
+template <typename T>
+__global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
+  int I, J, K;
+  if (!at3(gc.nx, gc.ny, I, J, K)) return;
+  c[lin3(gc, I, J, K)] = restrict_at(gf, f, I, J, K);
+}
+
+// Trilinear prolongation value at fine cell (i,j,k).
+template <typename T>
+__device__ __forceinline__ T prolong_at(const GridG &gc, const T *__restrict__ c, int i, int j, int k) {
+  int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
+  int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+  T wi = ni == 2 ? T(0.5) : T(1), wj = nj == 2 ? T(0.5) : T(1), wk = nk == 2 ? T(0.5) : T(1);
+  T s = T(0);
+  for (int a = 0; a < nk; a++)
+    for (int bq = 0; bq < nj; bq++)
+      for (int q = 0; q < ni; q++) s += gval(c, gc, k0 + a, j0 + bq, i0 + q);
+  return wi * wj * wk * s;
+}
+// f += P c.
+template <typename T>
+__global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__restrict__ f) {
+  int i, j, k;
+  if (!at3(gf.nx, gf.ny, i, j, k)) return;
+  f[lin3(gf, i, j, k)] += prolong_at(gc, c, i, j, k);
+}
+
+// ---- whole V-cycle of the small levels in one thread block -------------------
+template <typename T>
+struct SmallLevel {
+  OpK o;
+  T *dens, *x, *b, *r, *t;
+  ZlP<T> z;
+};
+constexpr int kMaxSmall = 8;
+template <typename T>
+struct SmallCycle {
+  int nl;
+  SmallLevel<T> lv[kMaxSmall];
+};
+
+template <typename T>
+__device__ void blk_sweep(const SmallLevel<T> &L, const T *b, const T *xo, T *xn, T omega) {
+  const GridG &g = L.o.g;
+  if (xo) {
+    for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
+      int i, j, k;
+      cell_ijk(c, g, i, j, k);
+      L.r[c] = zline_rhs_at(L.dens, b, xo, L.o, i, j, k, c);
+    }
+    __syncthreads();
+  }
+  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x)
+    zline_column<T>(g, L.z, xo ? L.r : b, xo, xn, omega, col);
+  __syncthreads();
+}
+
+// x_out = M(l0) b_in: V(1,1) over levels l0..l0+nl-1, all in this block.
+template <typename T>
+__global__ void __launch_bounds__(512) k_vcycle_small(SmallCycle<T> sc, const T *__restrict__ b_in,
+                                                      T *__restrict__ x_out, int coarse_sweeps, T omega) {
+  const int nl = sc.nl;
+  // down
+  for (int l = 0; l < nl - 1; l++) {
+    const SmallLevel<T> &L = sc.lv[l];
+    const T *b = l == 0 ? b_in : L.b;
+    blk_sweep(L, b, (const T *)nullptr, L.t, omega);
+    const GridG &g = L.o.g;
+    for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
+      int i, j, k;
+      cell_ijk(c, g, i, j, k);
+      L.r[c] = b[c] - apply_row(L.dens, L.t, L.o, i, j, k);
+    }
+    __syncthreads();
+    const SmallLevel<T> &C = sc.lv[l + 1];
+    for (unsigned c = threadIdx.x; c < C.o.g.n; c += blockDim.x) {
+      int I, J, K;
+      cell_ijk(c, C.o.g, I, J, K);
+      C.b[c] = restrict_at(g, L.r, I, J, K);
+    }
+    __syncthreads();
+  }
+  // coarsest: damped z-line Jacobi sweeps, result in its x (or x_out if nl == 1)
+  {
+    const SmallLevel<T> &L = sc.lv[nl - 1];
+    const T *b = nl == 1 ? b_in : L.b;
+    T *dst = nl == 1 ? x_out : L.x;
+    T *cur = dst, *nxt = L.t;
+    for (int sw = 0; sw < coarse_sweeps; sw++) {
+      blk_sweep(L, b, sw == 0 ? (const T *)nullptr : cur, nxt, omega);
+      T *tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+    }
+    if (cur != dst) {
+      for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) dst[c] = cur[c];
+      __syncthreads();
+    }
+  }
+  // up
+  for (int l = nl - 2; l >= 0; l--) {
+    const SmallLevel<T> &L = sc.lv[l], &C = sc.lv[l + 1];
+    const GridG &g = L.o.g;
+    for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
+      int i, j, k;
+      cell_ijk(c, g, i, j, k);
+      L.t[c] += prolong_at(C.o.g, C.x, i, j, k);
+    }
+    __syncthreads();
+    const T *b = l == 0 ? b_in : L.b;
+    blk_sweep(L, b, L.t, l == 0 ? x_out : L.x, omega);
+  }
+}
+
+// ---- vectors ----------------------------------------------------------------------
+// x64 += a * e (e in T)
+template <typename T>
+__global__ void k_axpy64(size_t n, double a, const T *__restrict__ e, double *__restrict__ x) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    x[q] += a * (double)e[q];
+}
+// d = s * scale[0] in the precision of d (the FP64 residual, normalised, to T)
+template <typename T>
+__global__ void k_scale_to(size_t n, const double *__restrict__ s, const double *__restrict__ scale, T *__restrict__ d) {
+  const T a = (T)scale[0];
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    d[q] = (T)s[q] * a;
+}
+// partial[block] = sum of v over the block's elements (FP64 accumulation)
+template <typename T>
+__global__ void k_sum_partial(size_t n, const T *__restrict__ v, double *__restrict__ partial) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    t += (double)v[e];
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+    partial[blockIdx.x] = u;
+  }
+}
+// out[0] = (sum of partial[0..nb)) / div, one block, fixed order
+__global__ void __launch_bounds__(1024) k_final_sum(int nb, const double *__restrict__ partial, double div,
+                                                    double *__restrict__ out) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+    out[0] = u / div;
+  }
+}
+// v -= value[0]
+template <typename T>
+__global__ void k_sub_value(size_t n, T *__restrict__ v, const double *__restrict__ value) {
+  const double m = value[0];
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    v[e] = (T)((double)v[e] - m);
+}
+
+// ---- FGMRES on the device -----------------------------------------------------------
+// Dot products are formed 8 slots at a time: products and sums over runs of
+// 8 elements of one thread in T, the runs accumulated in FP64, then a
+// fixed-order block reduction; slot q of block b goes to
+// partial[q * gridDim.x + b].
+constexpr int kChunk = 8;
+__device__ __forceinline__ void block_chunk(const double (&acc)[kChunk], int v0, int nslot,
+                                            double *__restrict__ partial) {
+  __shared__ double sh[kB / 32][kChunk];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < kChunk; q++) {
+    double a = acc[q];
+    for (int s = 16; s >= 1; s >>= 1) a += __shfl_xor_sync(ECS_FULL_MASK, a, s);
+    if (lane == 0) sh[warp][q] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < kChunk && v0 + (int)threadIdx.x < nslot) {
+    double t = 0.0;
+    for (int w = 0; w < kB / 32; w++) t += sh[w][threadIdx.x];
+    partial[(size_t)(v0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// Pass 1 of classical Gram-Schmidt: partial dots of V_0..V_j with w = V_{j+1}.
+template <typename T>
+__global__ void __launch_bounds__(kB) k_dots1(size_t n, const T *__restrict__ V, const KrylovDev *__restrict__ kd,
+                                              double *__restrict__ partial) {
+  const int nv = kd->j + 1;
+  const T *w = V + (size_t)nv * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int v0 = 0; v0 < nv; v0 += kChunk) {
+    double acc[kChunk];
+#pragma unroll
+    for (int q = 0; q < kChunk; q++) acc[q] = 0.0;
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    while (e < n) {
+      T run[kChunk];
+#pragma unroll
+      for (int q = 0; q < kChunk; q++) run[q] = T(0);
+      for (int r = 0; r < 8 && e < n; r++, e += stride) {
+        const T we = w[e];
+#pragma unroll
+        for (int q = 0; q < kChunk; q++)
+          if (v0 + q < nv) run[q] += V[(size_t)(v0 + q) * n + e] * we;
+      }
+#pragma unroll
+      for (int q = 0; q < kChunk; q++) acc[q] += (double)run[q];
+    }
+    block_chunk(acc, v0, nv, partial);
+  }
+}
+
+// h1[q] = sum of the pass-1 partials of slot q (one warp per slot).
+__global__ void __launch_bounds__(1024) k_dots1_final(KrylovDev *kd, int nb, const double *__restrict__ partial) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nv = kd->j + 1;
+  if (warp >= nv) return;
+  double t = 0.0;
+  for (int b = lane; b < nb; b += 32) t += partial[(size_t)warp * nb + b];
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if (lane == 0) kd->h1[warp] = t;
+}
+
+// w = V_{j+1} - sum_q h1[q] V_q (stored, in the first slot chunk), then
+// pass 2: partial dots of V_0..V_j with the new w (slots 0..j) and of w with
+// itself (slot j+1).
+template <typename T>
+__global__ void __launch_bounds__(kB) k_orth1_dots2(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd,
+                                                    double *__restrict__ partial) {
+  __shared__ T h[kSlots];
+  const int nv = kd->j + 1, nslot = nv + 1;
+  if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h1[threadIdx.x] : T(0);
+  __syncthreads();
+  T *w = V + (size_t)nv * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int v0 = 0; v0 < nslot; v0 += kChunk) {
+    double acc[kChunk];
+#pragma unroll
+    for (int q = 0; q < kChunk; q++) acc[q] = 0.0;
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    while (e < n) {
+      T run[kChunk];
+#pragma unroll
+      for (int q = 0; q < kChunk; q++) run[q] = T(0);
+      for (int r = 0; r < 8 && e < n; r++, e += stride) {
+        T s = w[e];
+        if (v0 == 0) {
+          for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
+          w[e] = s;
+        }
+#pragma unroll
+        for (int q = 0; q < kChunk; q++) {
+          const int v = v0 + q;
+          if (v < nv) run[q] += V[(size_t)v * n + e] * s;
+          else if (v == nv) run[q] += s * s;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kChunk; q++) acc[q] += (double)run[q];
+    }
+    block_chunk(acc, v0, nslot, partial);
+  }
+}
+
+// Arnoldi bookkeeping of step j (one block): reduce the pass-2 partials into
+// h2 and w.w, form column j of the Hessenberg matrix, apply the previous
+// Givens rotations and a new one, update the residual estimate and decide
+// whether the cycle stops.
+__global__ void __launch_bounds__(1024) k_arnoldi(KrylovDev *kd, int nb, const double *__restrict__ partial,
+                                                  cudaGraphConditionalHandle cond, int use_graph) {
+  __shared__ double red[kSlots];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (kd->done) {  // stopped before this step (b = 0): keep the state
+    if (threadIdx.x == 0 && use_graph) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  const int j = kd->j, nv = j + 1;
+  if (warp <= nv) {
+    double t = 0.0;
+    for (int b = lane; b < nb; b += 32) t += partial[(size_t)warp * nb + b];
+    for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+    if (lane == 0) red[warp] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const int m = kKrylovMax;
+  double ss = 0.0;
+  for (int q = 0; q <= j; q++) {
+    kd->h2[q] = red[q];
+    ss += red[q] * red[q];
+  }
+  const double ww = red[nv];
+  const double hn = sqrt(fmax(ww - ss, 0.0));
+  double *H = kd->H;
+  for (int q = 0; q <= j; q++) H[q * m + j] = kd->h1[q] + kd->h2[q];
+  H[(j + 1) * m + j] = hn;
+  for (int q = 0; q < j; q++) {
+    const double a = H[q * m + j], c = H[(q + 1) * m + j];
+    H[q * m + j] = kd->cs[q] * a + kd->sn[q] * c;
+    H[(q + 1) * m + j] = -kd->sn[q] * a + kd->cs[q] * c;
+  }
+  const double a = H[j * m + j], c = H[(j + 1) * m + j];
+  const double r = sqrt(a * a + c * c);
+  kd->cs[j] = r > 0 ? a / r : 1.0;
+  kd->sn[j] = r > 0 ? c / r : 0.0;
+  H[j * m + j] = r;
+  H[(j + 1) * m + j] = 0.0;
+  kd->g[j + 1] = -kd->sn[j] * kd->g[j];
+  kd->g[j] = kd->cs[j] * kd->g[j];
+  const double res = fabs(kd->g[j + 1]);
+  kd->res = res;
+  kd->nits = j + 1;
+  kd->inv_scale = hn > 0 ? 1.0 / hn : 0.0;
+  kd->jprev = j;
+  const int done = (res <= kd->tol_rel * kd->beta) || hn == 0.0 || (j + 1 >= kd->maxit) ||
+                   (j + 1 >= kKrylovMax) || !isfinite(res);
+  kd->done = done;
+  if (!done) kd->j = j + 1;
+  if (use_graph) cudaGraphSetConditional(cond, done ? 0u : 1u);
+}
+
+// V_{j+1} = (w - sum_q h2[q] V_q) / h_{j+1,j}, also copied to the
+// preconditioner input vin (j = the step that just finished).
+template <typename T>
+__global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd, T *__restrict__ vin) {
+  const int j = kd->jprev, nv = j + 1;
+  T *w = V + (size_t)(j + 1) * n;
+  T h[kSlots];
+#pragma unroll
+  for (int q = 0; q < kSlots; q++) h[q] = q < nv ? (T)kd->h2[q] : T(0);
+  const T sc = (T)kd->inv_scale;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    T s = w[e];
+#pragma unroll
+    for (int q = 0; q < kSlots; q++)
+      if (q < nv) s -= h[q] * V[(size_t)q * n + e];
+    s *= sc;
+    w[e] = s;
+    vin[e] = s;
+  }
+}
+
+// Z_j = zb - mean (mean = nullptr: plain copy)
+template <typename T>
+__global__ void k_store_z(size_t n, const T *__restrict__ zb, T *__restrict__ Z, const KrylovDev *__restrict__ kd,
+                          const double *__restrict__ mean) {
+  T *z = Z + (size_t)kd->j * n;
+  const T m = mean ? (T)mean[0] : T(0);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    z[e] = zb[e] - m;
+}
+
+// V_{j+1} = A Z_j
+template <typename T>
+__global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict__ Z, T *__restrict__ V,
+                            const KrylovDev *__restrict__ kd) {
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const int jj = kd->j;
+  const T *x = Z + (size_t)jj * o.g.n;
+  V[(size_t)(jj + 1) * o.g.n + lin3(o.g, i, j, k)] = apply_row(n, x, o, i, j, k);
+}
+
+// Start of a cycle: beta = ||b|| from the partials, first basis vector.
+__global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, const double *__restrict__ partial) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double u = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+  const double beta = sqrt(u);
+  kd->beta = beta;
+  kd->res = beta;
+  kd->j = 0;
+  kd->jprev = 0;
+  kd->nits = 0;
+  kd->done = !(beta > 0.0) || kd->maxit < 1;
+  kd->inv_scale = beta > 0.0 ? 1.0 / beta : 0.0;
+  for (int q = 0; q <= kKrylovMax; q++) kd->g[q] = 0.0;
+  kd->g[0] = beta;
+}
+
+// partial[block] = sum of b*b over the block (FP64 accumulation of T runs)
+template <typename T>
+__global__ void k_sq_partial(size_t n, const T *__restrict__ b, double *__restrict__ partial) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  while (e < n) {
+    T run = T(0);
+    for (int r = 0; r < 8 && e < n; r++, e += stride) run += b[e] * b[e];
+    t += (double)run;
+  }
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+    partial[blockIdx.x] = u;
+  }
+}
+
+// V_0 = b / beta, vin = V_0, x = 0
+template <typename T>
+__global__ void k_cycle_start(size_t n, const T *__restrict__ b, T *__restrict__ V, T *__restrict__ vin,
+                              T *__restrict__ x, const KrylovDev *__restrict__ kd) {
+  const T sc = (T)kd->inv_scale;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const T v = b[e] * sc;
+    V[e] = v;
+    vin[e] = v;
+    x[e] = T(0);
+  }
+}
+
+// y = H^-1 g (upper triangular, nits x nits)
+__global__ void k_cycle_solve(KrylovDev *kd) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = kKrylovMax, nj = kd->nits;
+  for (int q = nj - 1; q >= 0; q--) {
+    double s = kd->g[q];
+    for (int r2 = q + 1; r2 < nj; r2++) s -= kd->H[q * m + r2] * kd->y[r2];
+    kd->y[q] = s / kd->H[q * m + q];
+  }
+}
+
+// x += sum_q y[q] Z_q
+template <typename T>
+__global__ void k_cycle_combine(size_t n, const T *__restrict__ Z, const KrylovDev *__restrict__ kd, T *__restrict__ x) {
+  const int nj = kd->nits;
+  T y[kKrylovMax];
+#pragma unroll
+  for (int q = 0; q < kKrylovMax; q++) y[q] = q < nj ? (T)kd->y[q] : T(0);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    T s = x[e];
+#pragma unroll
+    for (int q = 0; q < kKrylovMax; q++)
+      if (q < nj) s += y[q] * Z[(size_t)q * n + e];
+    x[e] = s;
+  }
+}
+
+// ---- host side -----------------------------------------------------------------------
+unsigned int blocks_for(const EcsCtx *ctx, size_t n) {
+  size_t want = (n + kB - 1) / kB;
+  size_t cap = (size_t)ctx->nsm * 8;
+  if (want > cap) want = cap;
+  return (unsigned int)(want ? want : 1);
+}
+unsigned int dot_blocks(const EcsCtx *ctx, size_t n) { return std::min(blocks_for(ctx, n), (unsigned)kDotBlocks); }
+
+bool fully_periodic(const EcsCtx *ctx) {
+  return ctx->p.bc[0] == ECS_BC_PERIODIC && ctx->p.bc[1] == ECS_BC_PERIODIC && ctx->p.bc[2] == ECS_BC_PERIODIC;
+}
+
+template <typename T>
+Multigrid<T> &mg_of(EcsCtx *ctx);
+template <>
+Multigrid<double> &mg_of<double>(EcsCtx *ctx) { return ctx->mg64; }
+template <>
+Multigrid<float> &mg_of<float>(EcsCtx *ctx) { return ctx->mg32; }
+
+template <typename T>
+int mg_alloc(EcsCtx *ctx) {
+  Multigrid<T> &mg = mg_of<T>(ctx);
+  if (mg.built) return ECS_OK;
+  int nx = ctx->p.Nx, ny = ctx->p.Ny, nz = ctx->p.Nz;
+  double hx = ctx->p.dx, hy = ctx->p.dy, hz = ctx->p.dz;
+  for (;;) {
+    MgLevel<T> L;
+    L.nx = nx; L.ny = ny; L.nz = nz;
+    L.n = (size_t)nx * ny * nz;
+    L.hx = hx; L.hy = hy; L.hz = hz;
+    T **arr[] = {&L.dens, &L.x, &L.b, &L.r, &L.t, &L.zl_a, &L.zl_cp, &L.zl_minv, &L.zl_q, &L.zl_dp};
+    for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, L.n * sizeof(T)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_a0g, (size_t)nx * ny * sizeof(T)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_qden, (size_t)nx * ny * sizeof(T)));
+    mg.lv.push_back(L);
+    bool even = (nx % 2 == 0) && (ny % 2 == 0) && (nz % 2 == 0);
+    if (!even || std::min(nx, std::min(ny, nz)) < 8 || mg.lv.size() >= 12) break;
+    nx /= 2; ny /= 2; nz /= 2;
+    hx *= 2; hy *= 2; hz *= 2;
+  }
+  mg.built = true;
+  return ECS_OK;
+}
+
+template <typename T>
+ZlP<T> zl_of(MgLevel<T> &L) {
+  ZlP<T> z;
+  z.a = L.zl_a; z.cp = L.zl_cp; z.minv = L.zl_minv; z.q = L.zl_q; z.dp = L.zl_dp;
+  z.a0g = L.zl_a0g; z.qden = L.zl_qden;
+  return z;
+}
+template <typename T>
+OpK op_level(const EcsCtx *ctx, const MgLevel<T> &L) {
+  return make_op(ctx->p, L.nx, L.ny, L.nz, L.hx, L.hy, L.hz);
+}
+GridG grid_level(const EcsCtx *ctx, int nx, int ny, int nz) { return make_grid(ctx->p, nx, ny, nz); }
+
+constexpr int kColBlock = 128;
+constexpr int kCoarseSweeps = 21;
+template <typename T>
+constexpr T kOmega() { return T(0.8); }
+
+// Level densities (level 0 from the deposited density, coarser ones by full
+// weighting) and the z-line factorisation of every level.
+template <typename T>
+__global__ void k_density_in(size_t n, const double *__restrict__ mom, T *__restrict__ d) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    d[e] = (T)mom[e];
+}
+
+template <typename T>
+int mg_setup(EcsCtx *ctx) {
+  int rc = mg_alloc<T>(ctx);
+  if (rc) return rc;
+  Multigrid<T> &mg = mg_of<T>(ctx);
+  MgLevel<T> &L0 = mg.lv[0];
+  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, ctx->stream>>>(L0.n, ctx->mom, L0.dens);
+  ECS_LAUNCHED(ctx);
+  for (size_t l = 1; l < mg.lv.size(); l++) {
+    MgLevel<T> &F = mg.lv[l - 1], &C = mg.lv[l];
+    k_restrict<T><<<blocks3(C.nx, C.ny, C.nz), threads3(), 0, ctx->stream>>>(
+        grid_level(ctx, F.nx, F.ny, F.nz), grid_level(ctx, C.nx, C.ny, C.nz), F.dens, C.dens);
+    ECS_LAUNCHED(ctx);
+  }
+  for (auto &L : mg.lv) {
+    int ncol = L.nx * L.ny;
+    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L));
+    ECS_LAUNCHED(ctx);
+  }
+  return ECS_OK;
+}
+
+template <typename T>
+int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
+  const OpK o = op_level(ctx, L);
+  const T *r = b;
+  if (xo) {
+    k_zline_rhs<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, b, xo, L.r);
+    ECS_LAUNCHED(ctx);
+    r = L.r;
+  }
+  int ncol = L.nx * L.ny;
+  k_zline_solve<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+constexpr size_t kSmallCells = 4096;
+
+// One V(1,1) cycle on level l: xout = M(l) b, zero initial guess.  Levels of
+// at most kSmallCells cells run as one single-block kernel.
+template <typename T>
+int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
+  Multigrid<T> &mg = mg_of<T>(ctx);
+  MgLevel<T> &L = mg.lv[l];
+  int rc;
+  if (L.n <= kSmallCells && mg.lv.size() - l <= (size_t)kMaxSmall) {
+    SmallCycle<T> sc;
+    sc.nl = (int)(mg.lv.size() - l);
+    for (int q = 0; q < sc.nl; q++) {
+      MgLevel<T> &M = mg.lv[l + q];
+      sc.lv[q].o = op_level(ctx, M);
+      sc.lv[q].dens = M.dens; sc.lv[q].x = M.x; sc.lv[q].b = M.b; sc.lv[q].r = M.r; sc.lv[q].t = M.t;
+      sc.lv[q].z = zl_of(M);
+    }
+    k_vcycle_small<T><<<1, 512, 0, ctx->stream>>>(sc, b, xout, kCoarseSweeps, kOmega<T>());
+    ECS_LAUNCHED(ctx);
+    return ECS_OK;
+  }
+  if (l + 1 == mg.lv.size()) {
+    if ((rc = sweep<T>(ctx, L, b, nullptr, xout))) return rc;
+    for (int s = 0; s < (kCoarseSweeps - 1) / 2; s++) {
+      if ((rc = sweep<T>(ctx, L, b, xout, L.t))) return rc;
+      if ((rc = sweep<T>(ctx, L, b, L.t, xout))) return rc;
+    }
+    return ECS_OK;
+  }
+  MgLevel<T> &C = mg.lv[l + 1];
+  const OpK o = op_level(ctx, L);
+  if ((rc = sweep<T>(ctx, L, b, nullptr, L.t))) return rc;
+  k_apply<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, L.t, b, L.r, 1);
+  ECS_LAUNCHED(ctx);
+  const GridG gc = grid_level(ctx, C.nx, C.ny, C.nz);
+  k_restrict<T><<<blocks3(gc), threads3(), 0, ctx->stream>>>(o.g, gc, L.r, C.b);
+  ECS_LAUNCHED(ctx);
+  if ((rc = vcycle<T>(ctx, l + 1, C.b, C.x))) return rc;
+  k_prolong_add<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o.g, gc, C.x, L.t);
+  ECS_LAUNCHED(ctx);
+  return sweep<T>(ctx, L, b, L.t, xout);
+}
+
+template <typename T>
+T *basis_v(EcsCtx *ctx);
+template <>
+double *basis_v<double>(EcsCtx *ctx) { return ctx->kv64; }
+template <>
+float *basis_v<float>(EcsCtx *ctx) { return ctx->kv32; }
+template <typename T>
+T *basis_z(EcsCtx *ctx);
+template <>
+double *basis_z<double>(EcsCtx *ctx) { return ctx->kz64; }
+template <>
+float *basis_z<float>(EcsCtx *ctx) { return ctx->kz32; }
+// right-hand side and correction of the FGMRES cycle in precision T
+template <typename T>
+T *cycle_b(EcsCtx *ctx);
+template <>
+double *cycle_b<double>(EcsCtx *ctx) { return ctx->r64; }
+template <>
+float *cycle_b<float>(EcsCtx *ctx) { return ctx->kz32 + (size_t)ctx->krylov_m * ctx->ncell; }
+template <typename T>
+T *cycle_x(EcsCtx *ctx);
+template <>
+double *cycle_x<double>(EcsCtx *ctx) { return ctx->w64; }
+template <>
+float *cycle_x<float>(EcsCtx *ctx) { return ctx->kz32 + (size_t)(ctx->krylov_m + 1) * ctx->ncell; }
+
+// Kernels before the Arnoldi loop: ||b||, V_0, x = 0.
+template <typename T>
+int cycle_pre(EcsCtx *ctx) {
+  const size_t n = ctx->ncell;
+  KrylovDev *kd = (KrylovDev *)ctx->kdev;
+  Multigrid<T> &mg = mg_of<T>(ctx);
+  const T *b = cycle_b<T>(ctx);
+  const unsigned nb = dot_blocks(ctx, n);
+  k_sq_partial<T><<<nb, kB, 0, ctx->stream>>>(n, b, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_cycle_init<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_cycle_start<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, b, basis_v<T>(ctx), mg.lv[0].b, cycle_x<T>(ctx), kd);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// One Arnoldi step j (j read from the control block).
+template <typename T>
+int cycle_step(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
+  const size_t n = ctx->ncell;
+  KrylovDev *kd = (KrylovDev *)ctx->kdev;
+  Multigrid<T> &mg = mg_of<T>(ctx);
+  MgLevel<T> &L0 = mg.lv[0];
+  const OpK o0 = op_level(ctx, L0);
+  T *V = basis_v<T>(ctx), *Z = basis_z<T>(ctx);
+  int rc;
+  // z = M v_j  (vin = L0.b holds v_j, the V-cycle writes L0.x)
+  if ((rc = vcycle<T>(ctx, 0, L0.b, L0.x))) return rc;
+  const unsigned nb = dot_blocks(ctx, n);
+  const double *mean = nullptr;
+  if (fully_periodic(ctx)) {  // the operator's null space: project out the mean
+    k_sum_partial<T><<<nb, kB, 0, ctx->stream>>>(n, L0.x, ctx->red);
+    ECS_LAUNCHED(ctx);
+    k_final_sum<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, (double)n, &kd->mean);
+    ECS_LAUNCHED(ctx);
+    mean = &kd->mean;
+  }
+  k_store_z<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, L0.x, Z, kd, mean);
+  ECS_LAUNCHED(ctx);
+  k_apply_dyn<T><<<blocks3(o0.g), threads3(), 0, ctx->stream>>>(o0, L0.dens, Z, V, kd);
+  ECS_LAUNCHED(ctx);
+  // classical Gram-Schmidt, two passes
+  k_dots1<T><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_dots1_final<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_orth1_dots2<T><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_arnoldi<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red, cond, use_graph);
+  ECS_LAUNCHED(ctx);
+  k_orth2_scale<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// Kernels after the loop: x = sum_q y_q Z_q.
+template <typename T>
+int cycle_post(EcsCtx *ctx) {
+  const size_t n = ctx->ncell;
+  KrylovDev *kd = (KrylovDev *)ctx->kdev;
+  k_cycle_solve<<<1, 32, 0, ctx->stream>>>(kd);
+  ECS_LAUNCHED(ctx);
+  k_cycle_combine<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, basis_z<T>(ctx), kd, cycle_x<T>(ctx));
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+template <typename T>
+SolverGraph &graph_of(EcsCtx *ctx) {
+  return sizeof(T) == 8 ? ctx->graph64 : ctx->graph32;
+}
+
+// Capture one cycle as a graph: pre -> WHILE(step) -> post.
+template <typename T>
+int build_graph(EcsCtx *ctx) {
+  SolverGraph &sg = graph_of<T>(ctx);
+  if (sg.exec) return ECS_OK;
+  cudaGraph_t g = nullptr, pre = nullptr, post = nullptr;
+  ECS_CUDA(ctx, cudaGraphCreate(&g, 0));
+  sg.graph = g;
+  cudaGraphConditionalHandle cond;
+  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+  int rc;
+  // Kernels captured per section (the launch counter counts kernels that
+  // run, so it is restored after capture and advanced per graph launch).
+  const int64_t launches0 = ctx->launches;
+  // pre and post as captured child graphs
+  ECS_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  rc = cycle_pre<T>(ctx);
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &pre);
+  if (rc) return rc;
+  ECS_CUDA(ctx, ce);
+  const int64_t launches1 = ctx->launches;
+  ECS_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  rc = cycle_post<T>(ctx);
+  ce = cudaStreamEndCapture(ctx->stream, &post);
+  if (rc) return rc;
+  ECS_CUDA(ctx, ce);
+  const int64_t launches2 = ctx->launches;
+  cudaGraphNode_t npre, nloop, npost;
+  ECS_CUDA(ctx, cudaGraphAddChildGraphNode(&npre, g, nullptr, 0, pre));
+  // zero-initialised storage (the parameter union has no default constructor)
+  alignas(cudaGraphNodeParams) unsigned char cp_store[sizeof(cudaGraphNodeParams)];
+  memset(cp_store, 0, sizeof cp_store);
+  cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_store);
+  cp->type = cudaGraphNodeTypeConditional;
+  cp->conditional.handle = cond;
+  cp->conditional.type = cudaGraphCondTypeWhile;
+  cp->conditional.size = 1;
+  ECS_CUDA(ctx, cudaGraphAddNode(&nloop, g, &npre, nullptr, 1, cp));
+  cudaGraph_t body = cp->conditional.phGraph_out[0];
+  ECS_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  rc = cycle_step<T>(ctx, cond, 1);
+  ce = cudaStreamEndCapture(ctx->stream, &body);
+  if (rc) return rc;
+  ECS_CUDA(ctx, ce);
+  sg.kernels_fixed = (launches1 - launches0) + (launches2 - launches1);
+  sg.kernels_step = ctx->launches - launches2;
+  ctx->launches = launches0;
+  ECS_CUDA(ctx, cudaGraphAddChildGraphNode(&npost, g, &nloop, 1, post));
+  cudaGraphDestroy(pre);
+  cudaGraphDestroy(post);
+  ECS_CUDA(ctx, cudaGraphInstantiate(&sg.exec, g, 0));
+  return ECS_OK;
+}
+
+// One FGMRES cycle on (cycle_b, cycle_x) with tolerance tol (relative to
+// ||b||) and at most maxit steps; the control block ends up in ctx->kdev_host.
+template <typename T>
+int fgmres_cycle(EcsCtx *ctx, double tol, int maxit) {
+  KrylovDev *kd = (KrylovDev *)ctx->kdev;
+  KrylovDev *ctl = (KrylovDev *)ctx->kctl_host;
+  ctl->tol_rel = tol;
+  ctl->maxit = std::min(std::min(ctx->krylov_m, kKrylovMax), std::max(maxit, 1));
+  ECS_CUDA(ctx, cudaMemcpyAsync(kd, ctl, offsetof(KrylovDev, j), cudaMemcpyHostToDevice, ctx->stream));
+  int rc;
+  if (ctx->use_graphs) {
+    if ((rc = build_graph<T>(ctx))) return rc;
+    ECS_CUDA(ctx, cudaGraphLaunch(graph_of<T>(ctx).exec, ctx->stream));
+    ctx->graph_pending = &graph_of<T>(ctx);  // its kernels are counted once nits is known
+  } else {
+    if ((rc = cycle_pre<T>(ctx))) return rc;
+    KrylovDev *hk = (KrylovDev *)ctx->kdev_host;
+    for (int s = 0; s < kKrylovMax; s++) {
+      ECS_CUDA(ctx, cudaMemcpyAsync(&hk->done, &kd->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (hk->done) break;
+      cudaGraphConditionalHandle none = 0;
+      if ((rc = cycle_step<T>(ctx, none, 0))) return rc;
+    }
+    if ((rc = cycle_post<T>(ctx))) return rc;
+  }
+  return ECS_OK;
+}
+
+// ||v||_2 of an FP64 vector into dst[0] on the device.
+__global__ void __launch_bounds__(1024) k_final_norm(int nb, const double *__restrict__ partial, double *__restrict__ out) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
+  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+    out[0] = sqrt(u);
+    out[1] = u > 0.0 ? 1.0 / sqrt(u) : 0.0;
+  }
+}
+int norm64_dev(EcsCtx *ctx, const double *v, double *out2) {
+  const unsigned nb = dot_blocks(ctx, ctx->ncell);
+  k_sq_partial<double><<<nb, kB, 0, ctx->stream>>>(ctx->ncell, v, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_final_norm<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, out2);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+template <typename T>
+int project_mean(EcsCtx *ctx, T *v) {
+  if (!fully_periodic(ctx)) return ECS_OK;
+  size_t n = ctx->ncell;
+  unsigned int nb = dot_blocks(ctx, n);
+  k_sum_partial<T><<<nb, kB, 0, ctx->stream>>>(n, v, ctx->red);
+  ECS_LAUNCHED(ctx);
+  k_final_sum<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, (double)n, ctx->dots + 2);
+  ECS_LAUNCHED(ctx);
+  k_sub_value<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, v, ctx->dots + 2);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// Mixed-precision residual: r64 = b64 - A64(n64) x64.
+__global__ void k_residual64(OpK o, const double *__restrict__ n, const double *__restrict__ x,
+                             const double *__restrict__ b, double *__restrict__ r) {
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const unsigned c = lin3(o.g, i, j, k);
+  r[c] = b[c] - apply_row(n, x, o, i, j, k);
+}
+
+template <typename T>
+void free_mg(Multigrid<T> &mg) {
+  for (auto &L : mg.lv) {
+    T *arr[] = {L.dens, L.x, L.b, L.r, L.t, L.zl_a, L.zl_cp, L.zl_minv, L.zl_q, L.zl_dp, L.zl_a0g, L.zl_qden};
+    for (T *a : arr)
+      if (a) cudaFree(a);
+  }
+  mg.lv.clear();
+  mg.built = false;
+}
+
+void free_graph(SolverGraph &sg) {
+  if (sg.exec) cudaGraphExecDestroy(sg.exec);
+  if (sg.graph) cudaGraphDestroy(sg.graph);
+  sg.exec = nullptr;
+  sg.graph = nullptr;
+}
+
+}  // namespace
+
+// ============================================================================
+// entry points used by ecs_api.cu and ecs_grid.cu
+// ============================================================================
+int ecs_solver_alloc(EcsCtx *ctx) {
+  size_t n = ctx->ncell;
+  int m = ctx->krylov_m;
+  if (!ctx->red) {
+    ctx->nred = kSlots * 4096;
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->red, (size_t)ctx->nred * sizeof(double)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->dots, (size_t)(m + 2) * sizeof(double)));
+    ECS_CUDA(ctx, cudaMallocHost((void **)&ctx->h_dots, (size_t)(m + 2) * sizeof(double)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->r64, n * sizeof(double)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->w64, n * sizeof(double)));
+    ECS_CUDA(ctx, cudaMalloc(&ctx->kdev, sizeof(KrylovDev)));
+    ECS_CUDA(ctx, cudaMemset(ctx->kdev, 0, sizeof(KrylovDev)));
+    ECS_CUDA(ctx, cudaMallocHost(&ctx->kdev_host, sizeof(KrylovDev)));
+    ECS_CUDA(ctx, cudaMallocHost(&ctx->kctl_host, sizeof(KrylovDev)));
+    memset(ctx->kdev_host, 0, sizeof(KrylovDev));
+    memset(ctx->kctl_host, 0, sizeof(KrylovDev));
+  }
+  if (ctx->prec == ECS_PREC_FP64 && !ctx->kv64) {
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->kv64, (size_t)(m + 1) * n * sizeof(double)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->kz64, (size_t)m * n * sizeof(double)));
+  }
+  if (ctx->prec == ECS_PREC_MIXED && !ctx->kv32) {
+    // V, Z and two extra FP32 vectors (normalised residual, correction)
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->kv32, (size_t)(m + 1) * n * sizeof(float)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->kz32, (size_t)(m + 2) * n * sizeof(float)));
+  }
+  return ECS_OK;
+}
+
+int ecs_solver_setup(EcsCtx *ctx) {
+  int rc = ecs_solver_alloc(ctx);
+  if (rc) return rc;
+  rc = ctx->prec == ECS_PREC_FP64 ? mg_setup<double>(ctx) : mg_setup<float>(ctx);
+  if (rc) return rc;
+  ctx->lhs_ready = true;
+  return ECS_OK;
+}
+
+// Iterative refinement around FGMRES cycles.  Per refinement the host waits
+// once, for the FP64 residual norm and the finished cycle's control block.
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st) {
+  if (!ctx->lhs_ready) return ecs_fail(ctx, ECS_ERR_STATE, "solve called before lhs");
+  const size_t n = ctx->ncell;
+  const EcsParams &p = ctx->p;
+  const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
+  KrylovDev *hk = (KrylovDev *)ctx->kdev_host;
+  if (!ctx->ev_solve[0]) {
+    ECS_CUDA(ctx, cudaEventCreate(&ctx->ev_solve[0]));
+    ECS_CUDA(ctx, cudaEventCreate(&ctx->ev_solve[1]));
+  }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[0], ctx->stream));
+  int rc;
+  if (!warm) ECS_CUDA(ctx, cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream));
+  // ||b|| -> dots[0], 1/||b|| -> dots[1]
+  if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) return rc;
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const double bnorm = ctx->h_dots[0];
+  int its = 0, sweeps = 0;
+  double rel = 0.0;
+  bool cycle_pending = false;
+  if (bnorm > 0.0) {
+    for (;;) {
+      k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
+      ECS_LAUNCHED(ctx);
+      if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
+      ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      if (cycle_pending)
+        ECS_CUDA(ctx, cudaMemcpyAsync(hk, ctx->kdev, sizeof(KrylovDev), cudaMemcpyDeviceToHost, ctx->stream));
+      ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (cycle_pending) {
+        if (ctx->graph_pending) {
+          const SolverGraph *sg = (const SolverGraph *)ctx->graph_pending;
+          // the body runs at least once (its condition starts at 1)
+          ctx->launches += sg->kernels_fixed + sg->kernels_step * std::max(hk->nits, 1);
+          ctx->graph_pending = nullptr;
+        }
+        its += hk->nits;
+        sweeps++;
+        cycle_pending = false;
+        if (hk->nits == 0) {
+          rel = ctx->h_dots[0] / bnorm;
+          break;
+        }
+      }
+      const double rn = ctx->h_dots[0];
+      rel = rn / bnorm;
+      if (!isfinite(rel)) return ecs_fail(ctx, ECS_ERR_NONFINITE, "non-finite residual in solve");
+      if (rel <= rtol || its >= max_it) break;
+      const double tol_cycle = std::max(0.5 * rtol / rel, 1e-14);
+      if (ctx->prec == ECS_PREC_FP64) {
+        // the cycle solves A e = r64 directly (beta = ||r64||)
+        if ((rc = fgmres_cycle<double>(ctx, tol_cycle, max_it - its))) return rc;
+        k_axpy64<double><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, 1.0, ctx->w64, ctx->phi);
+      } else {
+        float *r32 = cycle_b<float>(ctx), *e32 = cycle_x<float>(ctx);
+        k_scale_to<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, ctx->r64, ctx->dots + 1, r32);
+        ECS_LAUNCHED(ctx);
+        if ((rc = fgmres_cycle<float>(ctx, std::max(tol_cycle, 2e-6), max_it - its))) return rc;
+        k_axpy64<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, rn, e32, ctx->phi);
+      }
+      ECS_LAUNCHED(ctx);
+      if ((rc = project_mean<double>(ctx, ctx->phi))) return rc;
+      cycle_pending = true;
+    }
+  }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[1], ctx->stream));
+  ECS_CUDA(ctx, cudaEventSynchronize(ctx->ev_solve[1]));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev_solve[0], ctx->ev_solve[1]);
+  if (st) {
+    st->iterations = its;
+    st->refinements = sweeps;
+    st->relres = rel;
+    st->seconds = ms * 1e-3;
+  }
+  if (bnorm > 0.0 && rel > rtol)
+    return ecs_fail(ctx, ECS_ERR_NOT_CONVERGED, "solve stopped at relres %.3e > %.3e after %d iterations", rel, rtol, its);
+  return ECS_OK;
+}
+
+int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y) {
+  const EcsParams &p = ctx->p;
+  const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
+  k_apply<double><<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, x, nullptr, y, 0);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+int ecs_solver_free(EcsCtx *ctx) {
+  free_graph(ctx->graph64);
+  free_graph(ctx->graph32);
+  free_mg(ctx->mg64);
+  free_mg(ctx->mg32);
+  void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->dots, ctx->red, ctx->kdev};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  if (ctx->h_dots) cudaFreeHost(ctx->h_dots);
+  if (ctx->kdev_host) cudaFreeHost(ctx->kdev_host);
+  if (ctx->kctl_host) cudaFreeHost(ctx->kctl_host);
+  for (auto &e : ctx->ev_solve)
+    if (e) cudaEventDestroy(e);
+  return ECS_OK;
+}

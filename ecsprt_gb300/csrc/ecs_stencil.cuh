@@ -1,0 +1,146 @@
+// Structured-grid helpers shared by the grid and solver translation units:
+// grid shape, ghost-aware loads, 3-D launch indexing (no integer division)
+// and the 11-coefficient operator row of src/lhs.c:366-423.
+#pragma once
+
+#include "ecs_internal.cuh"
+
+// FP64 arithmetic with every operation separately rounded (no contraction),
+// for kernels that must match the reference's FP64 results operand for
+// operand.
+struct rd {
+  double v;
+};
+__device__ __forceinline__ rd operator+(rd a, rd b) { return {__dadd_rn(a.v, b.v)}; }
+__device__ __forceinline__ rd operator-(rd a, rd b) { return {__dsub_rn(a.v, b.v)}; }
+__device__ __forceinline__ rd operator*(rd a, rd b) { return {__dmul_rn(a.v, b.v)}; }
+
+struct GridG {
+  int nx, ny, nz;
+  int bc[3];  // 0 periodic, else ghosted (value 0 outside)
+  size_t n;   // nx*ny*nz (at most 2^30)
+};
+
+// Value at (k,j,i) with the reference's ghost semantics: periodic wrap, or 0
+// outside a ghosted (non-periodic) dimension.  Offsets are at most one grid
+// length.
+template <typename T>
+__device__ __forceinline__ T gval(const T *__restrict__ F, const GridG &g, int k, int j, int i) {
+  if (i < 0 || i >= g.nx) { if (g.bc[0]) return T(0); i = i < 0 ? i + g.nx : i - g.nx; }
+  if (j < 0 || j >= g.ny) { if (g.bc[1]) return T(0); j = j < 0 ? j + g.ny : j - g.ny; }
+  if (k < 0 || k >= g.nz) { if (g.bc[2]) return T(0); k = k < 0 ? k + g.nz : k - g.nz; }
+  return F[((unsigned)k * g.ny + j) * g.nx + i];
+}
+
+// ---- 3-D launches: one thread per cell, (x, y) tiles of kTx x kTy, z from
+// blockIdx.z.  No division anywhere in the index arithmetic.
+constexpr int kTx = 32, kTy = 8;
+static inline dim3 threads3() { return dim3(kTx, kTy, 1); }
+static inline dim3 blocks3(int nx, int ny, int nz) {
+  return dim3((unsigned)((nx + kTx - 1) / kTx), (unsigned)((ny + kTy - 1) / kTy), (unsigned)nz);
+}
+static inline dim3 blocks3(const GridG &g) { return blocks3(g.nx, g.ny, g.nz); }
+__device__ __forceinline__ bool at3(int nx, int ny, int &i, int &j, int &k) {
+  i = blockIdx.x * kTx + threadIdx.x;
+  j = blockIdx.y * kTy + threadIdx.y;
+  k = blockIdx.z;
+  return i < nx && j < ny;
+}
+__device__ __forceinline__ unsigned lin3(const GridG &g, int i, int j, int k) {
+  return ((unsigned)k * g.ny + j) * g.nx + i;
+}
+// Linear block index and thread index of a 3-D launch (for block partials).
+__device__ __forceinline__ unsigned block_lin() {
+  return (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+__device__ __forceinline__ int thread_lin() { return threadIdx.y * blockDim.x + threadIdx.x; }
+
+// (i, j, k) of linear cell c, 32-bit (single-block loops over small levels).
+__device__ __forceinline__ void cell_ijk(unsigned c, const GridG &g, int &i, int &j, int &k) {
+  i = (int)(c % (unsigned)g.nx);
+  unsigned r = c / (unsigned)g.nx;
+  j = (int)(r % (unsigned)g.ny);
+  k = (int)(r / (unsigned)g.ny);
+}
+
+// ---- operator (src/lhs.c:366-423), templated on the arithmetic type --------
+struct OpK {
+  GridG g;
+  double sxx, syy, szz, sod;
+};
+
+// Stencil offsets (di, dj, dk) of the 11 row entries, in the reference's
+// order: x+, x-, y+, y-, z+, z-, (x+,y+), (x+,y-), (x-,y+), (x-,y-), centre.
+__device__ __forceinline__ int off_i(int e) { return (e == 0 || e == 6 || e == 7) ? 1 : ((e == 1 || e == 8 || e == 9) ? -1 : 0); }
+__device__ __forceinline__ int off_j(int e) { return (e == 2 || e == 6 || e == 8) ? 1 : ((e == 3 || e == 7 || e == 9) ? -1 : 0); }
+__device__ __forceinline__ int off_k(int e) { return e == 4 ? 1 : (e == 5 ? -1 : 0); }
+
+// 11 coefficients of row (k,j,i) in the order above.
+template <typename T>
+__device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int i, int j, int k, T v[11]) {
+  const GridG &g = o.g;
+  T nijk = gval(n, g, k, j, i);
+  T nmjk = gval(n, g, k, j, i - 1), npjk = gval(n, g, k, j, i + 1);
+  T nimk = gval(n, g, k, j - 1, i), nipk = gval(n, g, k, j + 1, i);
+  T nijm = gval(n, g, k - 1, j, i), nijp = gval(n, g, k + 1, j, i);
+  T sxx = T(o.sxx), syy = T(o.syy), szz = T(o.szz), sod = T(o.sod);
+  v[6] = sod * (nipk - npjk);
+  v[7] = sod * (npjk - nimk);
+  v[8] = sod * (nmjk - nipk);
+  v[9] = sod * (nimk - nmjk);
+  v[0] = sxx * (npjk + nijk) + sod * (nipk - nimk);
+  v[1] = sxx * (nijk + nmjk) - sod * (nipk - nimk);
+  v[2] = syy * (nipk + nijk) - sod * (npjk - nmjk);
+  v[3] = syy * (nijk + nimk) + sod * (npjk - nmjk);
+  v[4] = szz * (nijp + nijk);
+  v[5] = szz * (nijk + nijm);
+  v[10] = -(sxx * (npjk + T(2) * nijk + nmjk) + syy * (nipk + T(2) * nijk + nimk) +
+            szz * (nijp + T(2) * nijk + nijm));
+}
+
+// (A x)(k,j,i)
+template <typename T>
+__device__ __forceinline__ T apply_row(const T *__restrict__ n, const T *__restrict__ x, const OpK &o, int i,
+                                       int j, int k) {
+  T v[11];
+  row11(n, o, i, j, k, v);
+  T s = T(0);
+#pragma unroll
+  for (int e = 0; e < 11; e++) s += v[e] * gval(x, o.g, k + off_k(e), j + off_j(e), i + off_i(e));
+  return s;
+}
+
+// b - A_xy x at (k,j,i), A_xy = the 8 in-plane entries of the row.
+template <typename T>
+__device__ __forceinline__ T zline_rhs_at(const T *__restrict__ n, const T *__restrict__ b,
+                                          const T *__restrict__ x, const OpK &o, int i, int j, int k,
+                                          unsigned c) {
+  T v[11];
+  row11(n, o, i, j, k, v);
+  T s = b[c];
+#pragma unroll
+  for (int e = 0; e < 10; e++) {
+    if (e == 4 || e == 5) continue;
+    s -= v[e] * gval(x, o.g, k, j + off_j(e), i + off_i(e));
+  }
+  return s;
+}
+
+// Operator scale factors for spacing (hx, hy, hz), src/lhs.c:366-375.
+static inline OpK make_op(const EcsParams &p, int nx, int ny, int nz, double hx, double hy, double hz) {
+  OpK o;
+  o.g.nx = nx; o.g.ny = ny; o.g.nz = nz;
+  for (int d = 0; d < 3; d++) o.g.bc[d] = p.bc[d] == ECS_BC_PERIODIC ? 0 : 1;
+  o.g.n = (size_t)nx * ny * nz;
+  double kappa = p.kappa_e, scale = p.scale;
+  double hxx = 1.0 / (2.0 * hx * hx), hyy = 1.0 / (2.0 * hy * hy), hzz = 1.0 / (2.0 * hz * hz);
+  double hod = 1.0 / (8.0 * hy * hx);
+  o.sxx = scale * hxx;
+  o.syy = scale * hyy;
+  o.szz = scale * (1 + kappa * kappa) * hzz;
+  o.sod = scale * kappa * hod;
+  return o;
+}
+static inline GridG make_grid(const EcsParams &p, int nx, int ny, int nz) {
+  return make_op(p, nx, ny, nz, 1.0, 1.0, 1.0).g;
+}

@@ -124,6 +124,10 @@ int ecs_set_seed(EcsCtx *ctx, uint64_t seed);
 /* ecs_step starts each solve from the previous potential instead of zero
    (default 0, the reference's zero guess, src/potential.c:20-29). */
 int ecs_set_warm_start(EcsCtx *ctx, int warm);
+/* Run each FGMRES cycle of the solve as one CUDA graph (default 1), or let
+   the host launch its Arnoldi steps one by one (0).  Both give identical
+   results.  No counterpart in the reference (PETSc's KSP runs on the host). */
+int ecs_set_solver_graphs(EcsCtx *ctx, int on);
 
 /* ---- particles (host arrays in the reference's DMSwarm layout) ---------- */
 /* pos/vel are AoS FP64: pos[ip*3+d], vel[ip*3+d] (src/velocities.c:342-356). */

@@ -149,6 +149,23 @@ def test_solve(built, golden, case, prec):
         assert np.linalg.norm(phi - phi_o) / np.linalg.norm(phi_o) <= 1e-8
 
 
+@pytest.mark.parametrize("prec", [E.ECS_PREC_FP64, E.ECS_PREC_MIXED])
+def test_solver_graph_matches_host_loop(built, golden, prec):
+    """An FGMRES cycle captured as one CUDA graph (conditional WHILE over the
+    Arnoldi steps) runs the same kernels in the same order as the host loop,
+    so both give the same bits; also on a grid that needs several cycles."""
+    g = golden["fb"]
+    out = {}
+    for graphs in (True, False):
+        with new_ctx(g, prec) as ctx:
+            ctx.set_solver_graphs(graphs)
+            ctx.moments = g["moments"]
+            st = ctx.compute_potential(rtol=1e-10 if prec == E.ECS_PREC_FP64 else 1e-8, max_it=400)
+            out[graphs] = (ctx.phi, st.iterations, st.refinements)
+    assert out[True][1:] == out[False][1:]
+    assert np.array_equal(out[True][0], out[False][0])
+
+
 # ---------------------------------------------------------------- mixed path
 @pytest.mark.parametrize("case", CASES)
 def test_mixed_push(built, golden, case):
