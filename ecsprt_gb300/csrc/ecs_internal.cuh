@@ -47,7 +47,7 @@ struct MgLevel {
   // z-line factorisation of the (lower, diag, upper) z-tridiagonal part,
   // cyclic closure by Sherman-Morrison (periodic z) or plain (reflecting z).
   T *zl_a = nullptr, *zl_cp = nullptr, *zl_minv = nullptr, *zl_q = nullptr;
-  T *zl_dp = nullptr;  // per-sweep forward-substitution scratch
+  T *zl_fb = nullptr, *zl_bb = nullptr;     // in-segment products of the recurrences
   T *zl_a0g = nullptr, *zl_qden = nullptr;  // per-column Sherman-Morrison scalars
 };
 
@@ -55,6 +55,9 @@ template <typename T>
 struct Multigrid {
   std::vector<MgLevel<T>> lv;
   bool built = false;
+  // explicit inverse of the coarsest operator (transposed), when it is small
+  T *cinv = nullptr;
+  T *cwork = nullptr;  // Gauss-Jordan work matrix [n][2n]
 };
 
 // Instantiated graph of one FGMRES cycle (per arithmetic type).

@@ -72,14 +72,28 @@ __global__ void k_apply(OpK o, const T *__restrict__ n, const T *__restrict__ x,
 // diag = centre, up = z+ entry.  A periodic z closes the cycle, solved with
 // Sherman-Morrison around the Thomas factorisation of the modified matrix;
 // reflecting z drops the out-of-range couplings (Dirichlet-0 ghosts).
+// The solve runs in segments of S cells along z, one thread per segment; the
+// forward recurrence d_k = (r_k - a_k d_{k-1}) / m_k and the backward one
+// y_k = d_k - cp_k y_{k+1} are affine in the value carried in, so each
+// segment solves from zero and the carried values are stitched afterwards
+// with the in-segment products fb_k = prod(-a_i/m_i) and bb_k = prod(-cp_i).
 template <typename T>
 struct ZlP {
-  T *a, *cp, *minv, *q, *dp;  // per cell
-  T *a0g, *qden;              // per column
+  T *a, *cp, *minv, *q, *fb, *bb;  // per cell
+  T *a0g, *qden;                   // per column
 };
+// At most 16 segments a column (block of 32 x 16 threads); segments of 8
+// (FP64 only), 16, 32 or 64 cells, the shortest that fits.
+constexpr int kMaxSeg = 16;
+template <typename T>
+static inline int seg_len(int N) {
+  for (int S = sizeof(T) == 8 ? 8 : 16; S < 64; S *= 2)
+    if (N <= S * kMaxSeg) return S;
+  return 64;
+}
 
 template <typename T>
-__global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z) {
+__global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z, int S) {
   const GridG &g = o.g;
   const int ncol = g.nx * g.ny;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -92,7 +106,7 @@ __global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z) {
   row11(n, o, i, j, 0, v);
   const T lo0 = cyc ? v[5] : T(0), d0 = v[10];
   const T gamma = -d0;
-  T cp_prev = T(0), dq_prev = T(0);
+  T cp_prev = T(0), dq_prev = T(0), fprod = T(1);
   // forward: factor T' and forward-substitute u = (gamma, 0, .., up_{N-1})
   for (int k = 0; k < N; k++) {
     row11(n, o, i, j, k, v);
@@ -111,15 +125,23 @@ __global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z) {
     z.cp[c] = cp;
     z.minv[c] = minv;
     z.q[c] = dq;
+    if (k % S == 0) fprod = T(1);
+    fprod *= -(a * minv);
+    z.fb[c] = fprod;
     cp_prev = cp;
     dq_prev = dq;
   }
-  // backward substitution for q
+  // backward substitution for q, in-segment products of -cp
   T qn = z.q[(size_t)(N - 1) * plane + col];
+  T bprod = -z.cp[(size_t)(N - 1) * plane + col];
+  z.bb[(size_t)(N - 1) * plane + col] = bprod;
   for (int k = N - 2; k >= 0; k--) {
     size_t c = (size_t)k * plane + col;
     qn = z.q[c] - z.cp[c] * qn;
     z.q[c] = qn;
+    if ((k + 1) % S == 0) bprod = T(1);
+    bprod *= -z.cp[c];
+    z.bb[c] = bprod;
   }
   if (cyc) {
     T a0g = lo0 / gamma;
@@ -142,114 +164,107 @@ __global__ void k_zline_rhs(OpK o, const T *__restrict__ n, const T *__restrict_
   r[c] = zline_rhs_at(n, b, xo, o, i, j, k, c);
 }
 
-constexpr int kZChunk = 8;
-
-// Thomas solve of one column with the precomputed factors (a, cp, minv) and
-// the Sherman-Morrison closure (q, a0g, qden), then damping against xo
-// (nullptr: zero).  Loads of chunk c+1 are issued before chunk c is used.
-template <typename T>
-__device__ __forceinline__ void zline_column(const GridG &g, const ZlP<T> &z, const T *__restrict__ r,
-                                             const T *__restrict__ xo, T *__restrict__ xn, T omega, int col) {
+// Damped z-line Jacobi update: T' y = r by segments, Sherman-Morrison
+// closure of the periodic cycle, xn = xo + omega (y - s q - xo) (xo nullptr:
+// zero).  Block = 32 columns (consecutive x at one y) x P segments of S
+// cells; each phase loads its segment's operands at once so that one memory
+// latency covers the whole segment.
+template <typename T, int S>
+__global__ void __launch_bounds__(32 * kMaxSeg) k_zline_seg(GridG g, ZlP<T> z, const T *__restrict__ r,
+                                                            const T *__restrict__ xo, T *__restrict__ xn,
+                                                            T omega) {
+  __shared__ T sA[kMaxSeg][33], sB[kMaxSeg][33], sIn[kMaxSeg][33];
+  __shared__ T sLast[32], sS[32];
+  const int tx = threadIdx.x, p = threadIdx.y, P = blockDim.y;
+  const int i = blockIdx.x * 32 + tx, j = blockIdx.y;
+  const bool act = i < g.nx;
   const size_t plane = (size_t)g.nx * g.ny;
-  const int N = g.nz;
-  T ra[kZChunk], aa[kZChunk], ma[kZChunk];
-  T rb[kZChunk], ab[kZChunk], mb[kZChunk];
+  const int col = j * g.nx + i;
+  const int N = g.nz, k0 = p * S, k1 = min(N, k0 + S);
+  const size_t c0 = (size_t)k0 * plane + col;
+  auto in = [&](int q) { return act && k0 + q < k1; };
+  T loc[S];
+  // forward, from zero at the segment start
+  {
+    T rv[S], av[S], mv[S];
 #pragma unroll
-  for (int q = 0; q < kZChunk; q++) {
-    size_t c = (size_t)q * plane + col;
-    bool in = q < N;
-    ra[q] = in ? r[c] : T(0);
-    aa[q] = in ? z.a[c] : T(0);
-    ma[q] = in ? z.minv[c] : T(0);
+    for (int q = 0; q < S; q++) {
+      const size_t c = c0 + (size_t)q * plane;
+      rv[q] = in(q) ? r[c] : T(0);
+      av[q] = in(q) ? z.a[c] : T(0);
+      mv[q] = in(q) ? z.minv[c] : T(0);
+    }
+    T d = T(0);
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+      if (in(q)) d = (rv[q] - av[q] * d) * mv[q];
+      loc[q] = d;
+    }
+    sA[p][tx] = d;
+    sB[p][tx] = act ? z.fb[(size_t)(k1 - 1) * plane + col] : T(0);
   }
-  T dp = T(0);
-  for (int k0 = 0; k0 < N; k0 += kZChunk) {
+  __syncthreads();
+  if (p == 0) {
+    T din = T(0);
+    for (int pp = 0; pp < P; pp++) {
+      sIn[pp][tx] = din;
+      din = sA[pp][tx] + sB[pp][tx] * din;
+    }
+  }
+  __syncthreads();
+  // carried value in, then backward from zero at the segment end
+  {
+    const T din = sIn[p][tx];
+    T fv[S], cv[S];
 #pragma unroll
-    for (int q = 0; q < kZChunk; q++) {  // prefetch next chunk
-      int k = k0 + kZChunk + q;
-      size_t c = (size_t)k * plane + col;
-      bool in = k < N;
-      rb[q] = in ? r[c] : T(0);
-      ab[q] = in ? z.a[c] : T(0);
-      mb[q] = in ? z.minv[c] : T(0);
+    for (int q = 0; q < S; q++) {
+      const size_t c = c0 + (size_t)q * plane;
+      fv[q] = in(q) ? z.fb[c] : T(0);
+      cv[q] = in(q) ? z.cp[c] : T(0);
+    }
+    T y = T(0);
+#pragma unroll
+    for (int q = S - 1; q >= 0; q--) {
+      if (in(q)) y = (loc[q] + fv[q] * din) - cv[q] * y;
+      loc[q] = y;
+    }
+    // sA, sB are free again: the forward scan finished before the last barrier
+    sA[p][tx] = y;
+    sB[p][tx] = act ? z.bb[c0] : T(0);
+    if (p == P - 1) {  // y_{N-1}: nothing is carried into the last segment
+#pragma unroll
+      for (int q = 0; q < S; q++)
+        if (k0 + q == N - 1) sLast[tx] = loc[q];
+    }
+  }
+  __syncthreads();
+  if (p == 0) {
+    T yin = T(0);
+    for (int pp = P - 1; pp >= 0; pp--) {
+      sIn[pp][tx] = yin;
+      yin = sA[pp][tx] + sB[pp][tx] * yin;
+    }
+    sS[tx] = act ? (yin + z.a0g[col] * sLast[tx]) * z.qden[col] : T(0);  // yin = y_0
+  }
+  __syncthreads();
+  {
+    const T yin = sIn[p][tx], s = sS[tx];
+    T bv[S], qv[S], ov[S];
+#pragma unroll
+    for (int q = 0; q < S; q++) {
+      const size_t c = c0 + (size_t)q * plane;
+      bv[q] = in(q) ? z.bb[c] : T(0);
+      qv[q] = in(q) ? z.q[c] : T(0);
+      ov[q] = (in(q) && xo) ? xo[c] : T(0);
     }
 #pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      int k = k0 + q;
-      if (k < N) {
-        dp = (ra[q] - aa[q] * dp) * ma[q];
-        z.dp[(size_t)k * plane + col] = dp;
+    for (int q = 0; q < S; q++) {
+      if (in(q)) {
+        const T yk = loc[q] + bv[q] * yin;
+        xn[c0 + (size_t)q * plane] = ov[q] + omega * ((yk - s * qv[q]) - ov[q]);
       }
     }
-#pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      ra[q] = rb[q];
-      aa[q] = ab[q];
-      ma[q] = mb[q];
-    }
   }
-  // backward substitution, chunks from the top
-  T y = T(0);
-  const T yN = z.dp[(size_t)(N - 1) * plane + col];
-  const int last0 = ((N - 1) / kZChunk) * kZChunk;
-  T da[kZChunk], ca[kZChunk], db[kZChunk], cb[kZChunk];
-#pragma unroll
-  for (int q = 0; q < kZChunk; q++) {
-    int k = last0 + q;
-    size_t c = (size_t)k * plane + col;
-    bool in = k < N;
-    da[q] = in ? z.dp[c] : T(0);
-    ca[q] = in ? z.cp[c] : T(0);
-  }
-  for (int k0 = last0; k0 >= 0; k0 -= kZChunk) {
-#pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      int k = k0 - kZChunk + q;
-      size_t c = (size_t)(k < 0 ? 0 : k) * plane + col;
-      bool in = k >= 0;
-      db[q] = in ? z.dp[c] : T(0);
-      cb[q] = in ? z.cp[c] : T(0);
-    }
-#pragma unroll
-    for (int q = kZChunk - 1; q >= 0; q--) {
-      int k = k0 + q;
-      if (k < N) {
-        y = (k == N - 1) ? da[q] : da[q] - ca[q] * y;
-        z.dp[(size_t)k * plane + col] = y;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      da[q] = db[q];
-      ca[q] = cb[q];
-    }
-  }
-  const T s = (y + z.a0g[col] * yN) * z.qden[col];
-  for (int k0 = 0; k0 < N; k0 += kZChunk) {
-    T yv[kZChunk], qv[kZChunk], ov[kZChunk];
-#pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      int k = k0 + q;
-      size_t c = (size_t)k * plane + col;
-      bool in = k < N;
-      yv[q] = in ? z.dp[c] : T(0);
-      qv[q] = in ? z.q[c] : T(0);
-      ov[q] = (in && xo) ? xo[c] : T(0);
-    }
-#pragma unroll
-    for (int q = 0; q < kZChunk; q++) {
-      int k = k0 + q;
-      if (k < N) xn[(size_t)k * plane + col] = ov[q] + omega * ((yv[q] - s * qv[q]) - ov[q]);
-    }
-  }
-}
-
-template <typename T>
-__global__ void k_zline_solve(GridG g, ZlP<T> z, const T *__restrict__ r, const T *__restrict__ xo,
-                              T *__restrict__ xn, T omega) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= g.nx * g.ny) return;
-  zline_column<T>(g, z, r, xo, xn, omega, col);
 }
 
 // ---- inter-grid transfer ---------------------------------------------------------
@@ -300,74 +315,128 @@ __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__
 }
 
 // ---- whole V-cycle of the small levels in one thread block -------------------
+// The iterate, right-hand side, residual and scratch vectors of every small
+// level live in shared memory (s* are element offsets into it); the density
+// and the z-line factors are read-only and come through the L1 cache.
 template <typename T>
 struct SmallLevel {
   OpK o;
-  T *dens, *x, *b, *r, *t;
+  const T *dens;
   ZlP<T> z;
+  int sx, sb, sr, st;
 };
 constexpr int kMaxSmall = 8;
 template <typename T>
 struct SmallCycle {
   int nl;
+  const T *cinv;  // transposed inverse of the coarsest operator, or nullptr
   SmallLevel<T> lv[kMaxSmall];
 };
+constexpr int kSmallThreads = 1024;
 
+// Thomas solve of one column with all vectors in shared memory: rin (right-
+// hand side) may be the same array as dp (the substitution scratch).
 template <typename T>
-__device__ void blk_sweep(const SmallLevel<T> &L, const T *b, const T *xo, T *xn, T omega) {
+__device__ __forceinline__ void zline_col_s(const GridG &g, const ZlP<T> &z, const T *rin, T *dp,
+                                            const T *xo, T *xn, T omega, int col) {
+  const int plane = g.nx * g.ny, N = g.nz;
+  T d = T(0);
+  for (int k = 0; k < N; k++) {
+    const int c = k * plane + col;
+    d = (rin[c] - __ldg(&z.a[c]) * d) * __ldg(&z.minv[c]);
+    dp[c] = d;
+  }
+  const T yN = d;
+  T y = d;
+  for (int k = N - 2; k >= 0; k--) {
+    const int c = k * plane + col;
+    y = dp[c] - __ldg(&z.cp[c]) * y;
+    dp[c] = y;
+  }
+  const T s = (y + __ldg(&z.a0g[col]) * yN) * __ldg(&z.qden[col]);
+  for (int k = 0; k < N; k++) {
+    const int c = k * plane + col;
+    const T ov = xo ? xo[c] : T(0);
+    xn[c] = ov + omega * ((dp[c] - s * __ldg(&z.q[c])) - ov);
+  }
+}
+
+// One damped z-line Jacobi sweep of level L from xo (nullptr: zero) into xn.
+template <typename T>
+__device__ void blk_sweep(const SmallLevel<T> &L, T *sm, const T *b, const T *xo, T *xn, T omega) {
   const GridG &g = L.o.g;
+  T *r = sm + L.sr;
+  const T *rin = b;
   if (xo) {
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      L.r[c] = zline_rhs_at(L.dens, b, xo, L.o, i, j, k, c);
+      r[c] = zline_rhs_at(L.dens, b, xo, L.o, i, j, k, c);
     }
     __syncthreads();
+    rin = r;
   }
-  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x)
-    zline_column<T>(g, L.z, xo ? L.r : b, xo, xn, omega, col);
+  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x) zline_col_s<T>(g, L.z, rin, r, xo, xn, omega, col);
   __syncthreads();
 }
 
 // x_out = M(l0) b_in: V(1,1) over levels l0..l0+nl-1, all in this block.
 template <typename T>
-__global__ void __launch_bounds__(512) k_vcycle_small(SmallCycle<T> sc, const T *__restrict__ b_in,
-                                                      T *__restrict__ x_out, int coarse_sweeps, T omega) {
+__global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc, const T *__restrict__ b_in,
+                                                                T *__restrict__ x_out, int coarse_sweeps, T omega) {
+  extern __shared__ unsigned char small_smem[];
+  T *sm = reinterpret_cast<T *>(small_smem);
   const int nl = sc.nl;
+  {
+    const SmallLevel<T> &L = sc.lv[0];
+    for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) sm[L.sb + c] = b_in[c];
+    __syncthreads();
+  }
   // down
   for (int l = 0; l < nl - 1; l++) {
     const SmallLevel<T> &L = sc.lv[l];
-    const T *b = l == 0 ? b_in : L.b;
-    blk_sweep(L, b, (const T *)nullptr, L.t, omega);
     const GridG &g = L.o.g;
+    T *b = sm + L.sb, *t = sm + L.st, *r = sm + L.sr;
+    blk_sweep(L, sm, b, (const T *)nullptr, t, omega);
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      L.r[c] = b[c] - apply_row(L.dens, L.t, L.o, i, j, k);
+      r[c] = b[c] - apply_row(L.dens, (const T *)t, L.o, i, j, k);
     }
     __syncthreads();
     const SmallLevel<T> &C = sc.lv[l + 1];
+    T *cb = sm + C.sb;
     for (unsigned c = threadIdx.x; c < C.o.g.n; c += blockDim.x) {
       int I, J, K;
       cell_ijk(c, C.o.g, I, J, K);
-      C.b[c] = restrict_at(g, L.r, I, J, K);
+      cb[c] = restrict_at(g, (const T *)r, I, J, K);
     }
     __syncthreads();
   }
-  // coarsest: damped z-line Jacobi sweeps, result in its x (or x_out if nl == 1)
-  {
+  // coarsest: direct solve with the precomputed inverse, else damped z-line
+  // Jacobi sweeps; the result in its x
+  if (sc.cinv) {
     const SmallLevel<T> &L = sc.lv[nl - 1];
-    const T *b = nl == 1 ? b_in : L.b;
-    T *dst = nl == 1 ? x_out : L.x;
-    T *cur = dst, *nxt = L.t;
+    const int n = (int)L.o.g.n;
+    const T *b = sm + L.sb;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      T acc = T(0);
+      for (int k = 0; k < n; k++) acc += __ldg(&sc.cinv[(size_t)k * n + r]) * b[k];
+      sm[L.sx + r] = acc;
+    }
+    __syncthreads();
+  } else {
+    const SmallLevel<T> &L = sc.lv[nl - 1];
+    const T *b = sm + L.sb;
+    T *cur = sm + L.sx, *nxt = sm + L.st;
     for (int sw = 0; sw < coarse_sweeps; sw++) {
-      blk_sweep(L, b, sw == 0 ? (const T *)nullptr : cur, nxt, omega);
+      blk_sweep(L, sm, b, sw == 0 ? (const T *)nullptr : cur, nxt, omega);
       T *tmp = cur;
       cur = nxt;
       nxt = tmp;
     }
-    if (cur != dst) {
-      for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) dst[c] = cur[c];
+    if (cur != sm + L.sx) {
+      for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) sm[L.sx + c] = cur[c];
       __syncthreads();
     }
   }
@@ -375,18 +444,147 @@ __global__ void __launch_bounds__(512) k_vcycle_small(SmallCycle<T> sc, const T 
   for (int l = nl - 2; l >= 0; l--) {
     const SmallLevel<T> &L = sc.lv[l], &C = sc.lv[l + 1];
     const GridG &g = L.o.g;
+    T *t = sm + L.st;
+    const T *cx = sm + C.sx;
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      L.t[c] += prolong_at(C.o.g, C.x, i, j, k);
+      t[c] += prolong_at(C.o.g, cx, i, j, k);
     }
     __syncthreads();
-    const T *b = l == 0 ? b_in : L.b;
-    blk_sweep(L, b, L.t, l == 0 ? x_out : L.x, omega);
+    blk_sweep(L, sm, sm + L.sb, t, sm + L.sx, omega);
+  }
+  {
+    const SmallLevel<T> &L = sc.lv[0];
+    for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) x_out[c] = sm[L.sx + c];
+  }
+}
+
+// ---- direct solve of the coarsest level -----------------------------------------
+constexpr int kDirectMax = 128;  // largest coarsest level solved directly
+
+// invT = (A + sigma 1 1^T)^-1, transposed (invT[k n + r] = inv[r][k]), by
+// Gauss-Jordan elimination with partial pivoting on M = [A | I] (n x 2n, in
+// global memory), one block.  sigma = mean |A_rr| / n removes the constant
+// null space of a fully periodic operator (regularize = 1); without it the
+// operator is regular.  Pivot ties go to the lowest row, so the result is
+// reproducible.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restrict__ dens, int regularize,
+                                                         T *__restrict__ M, T *__restrict__ invT) {
+  __shared__ T fac[kDirectMax];
+  __shared__ T wv[32];
+  __shared__ int wi[32];
+  __shared__ int piv;
+  __shared__ T sigma;
+  const GridG &g = o.g;
+  const int n = (int)g.n, w = 2 * n, tid = threadIdx.x, bs = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < n * w; e += bs) M[e] = T(0);
+  __syncthreads();
+  for (int r = tid; r < n; r += bs) {
+    int i, j, k;
+    cell_ijk((unsigned)r, g, i, j, k);
+    T v[11];
+    row11(dens, o, i, j, k, v);
+    for (int e = 0; e < 11; e++) {
+      int ii = i + off_i(e), jj = j + off_j(e), kk = k + off_k(e);
+      bool out = false;
+      if (ii < 0 || ii >= g.nx) { if (g.bc[0]) out = true; else ii = ii < 0 ? ii + g.nx : ii - g.nx; }
+      if (jj < 0 || jj >= g.ny) { if (g.bc[1]) out = true; else jj = jj < 0 ? jj + g.ny : jj - g.ny; }
+      if (kk < 0 || kk >= g.nz) { if (g.bc[2]) out = true; else kk = kk < 0 ? kk + g.nz : kk - g.nz; }
+      if (!out) M[(size_t)r * w + ((kk * g.ny + jj) * g.nx + ii)] += v[e];
+    }
+    M[(size_t)r * w + n + r] = T(1);
+  }
+  __syncthreads();
+  if (regularize) {
+    T t = T(0);
+    for (int r = tid; r < n; r += bs) t += fabs(M[(size_t)r * w + r]);
+    for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
+    if (lane == 0) wv[warp] = t;
+    __syncthreads();
+    if (tid == 0) {
+      T u = T(0);
+      for (int q = 0; q < (bs >> 5); q++) u += wv[q];
+      sigma = u / (T(n) * T(n));
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += bs) M[(size_t)(e / n) * w + (e % n)] += sigma;
+    __syncthreads();
+  }
+  for (int c = 0; c < n; c++) {
+    // pivot: largest |M[r][c]|, r >= c
+    T best = T(-1);
+    int bi = n;
+    for (int r = c + tid; r < n; r += bs) {
+      const T a = fabs(M[(size_t)r * w + c]);
+      if (a > best) { best = a; bi = r; }
+    }
+    for (int s = 16; s >= 1; s >>= 1) {
+      const T ob = __shfl_xor_sync(ECS_FULL_MASK, best, s);
+      const int oi = __shfl_xor_sync(ECS_FULL_MASK, bi, s);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { wv[warp] = best; wi[warp] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      T b0 = T(-1);
+      int i0 = n;
+      for (int q = 0; q < (bs >> 5); q++)
+        if (wv[q] > b0 || (wv[q] == b0 && wi[q] < i0)) { b0 = wv[q]; i0 = wi[q]; }
+      piv = i0 < n ? i0 : c;
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != c)
+      for (int q = tid; q < w; q += bs) {
+        const T t = M[(size_t)c * w + q];
+        M[(size_t)c * w + q] = M[(size_t)pr * w + q];
+        M[(size_t)pr * w + q] = t;
+      }
+    __syncthreads();
+    const T pv = M[(size_t)c * w + c];
+    const T ip = pv != T(0) ? T(1) / pv : T(0);
+    __syncthreads();
+    for (int q = tid; q < w; q += bs) M[(size_t)c * w + q] *= ip;
+    for (int r = tid; r < n; r += bs) fac[r] = M[(size_t)r * w + c];
+    __syncthreads();
+    for (int e = tid; e < n * w; e += bs) {
+      const int r = e / w, q = e - r * w;
+      if (r != c) M[e] -= fac[r] * M[(size_t)c * w + q];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += bs) {
+    const int r = e / n, k = e - r * n;
+    invT[(size_t)k * n + r] = M[(size_t)r * w + n + k];
   }
 }
 
 // ---- vectors ----------------------------------------------------------------------
+// Sums of one thread use compensated (Kahan) summation in T; a warp adds its
+// 32 lanes in T (fixed tree); from there on (warps of a block, blocks) the
+// sums are FP64 in a fixed order.  FP32 sums thus need no FP64 instruction
+// per element, which matters on sm_103 where FP64 issues on a narrow pipe.
+template <typename T>
+struct KSum {
+  T s, c;
+  __device__ __forceinline__ KSum() : s(T(0)), c(T(0)) {}
+  __device__ __forceinline__ void add(T x) {
+    const T y = x - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ T value() const { return s - c; }
+};
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+  for (int s = 16; s >= 1; s >>= 1) v += __shfl_xor_sync(ECS_FULL_MASK, v, s);
+  return v;
+}
+
 // x64 += a * e (e in T)
 template <typename T>
 __global__ void k_axpy64(size_t n, double a, const T *__restrict__ e, double *__restrict__ x) {
@@ -404,11 +602,11 @@ __global__ void k_scale_to(size_t n, const double *__restrict__ s, const double 
 template <typename T>
 __global__ void k_sum_partial(size_t n, const T *__restrict__ v, double *__restrict__ partial) {
   __shared__ double sh[32];
-  double t = 0.0;
+  KSum<T> acc;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-    t += (double)v[e];
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+    acc.add(v[e]);
+  const T t = warp_sum(acc.value());
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)t;
   __syncthreads();
   if (threadIdx.x == 0) {
     double u = 0.0;
@@ -440,20 +638,18 @@ __global__ void k_sub_value(size_t n, T *__restrict__ v, const double *__restric
 }
 
 // ---- FGMRES on the device -----------------------------------------------------------
-// Dot products are formed 8 slots at a time: products and sums over runs of
-// 8 elements of one thread in T, the runs accumulated in FP64, then a
-// fixed-order block reduction; slot q of block b goes to
-// partial[q * gridDim.x + b].
+// Dot products are formed 8 slots at a time, then a fixed-order block
+// reduction; slot q of block b goes to partial[q * gridDim.x + b].
 constexpr int kChunk = 8;
-__device__ __forceinline__ void block_chunk(const double (&acc)[kChunk], int v0, int nslot,
+template <typename T>
+__device__ __forceinline__ void block_chunk(const KSum<T> (&acc)[kChunk], int v0, int nslot,
                                             double *__restrict__ partial) {
   __shared__ double sh[kB / 32][kChunk];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < kChunk; q++) {
-    double a = acc[q];
-    for (int s = 16; s >= 1; s >>= 1) a += __shfl_xor_sync(ECS_FULL_MASK, a, s);
-    if (lane == 0) sh[warp][q] = a;
+    const T a = warp_sum(acc[q].value());
+    if (lane == 0) sh[warp][q] = (double)a;
   }
   __syncthreads();
   if (threadIdx.x < kChunk && v0 + (int)threadIdx.x < nslot) {
@@ -472,22 +668,12 @@ __global__ void __launch_bounds__(kB) k_dots1(size_t n, const T *__restrict__ V,
   const T *w = V + (size_t)nv * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (int v0 = 0; v0 < nv; v0 += kChunk) {
-    double acc[kChunk];
+    KSum<T> acc[kChunk];
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+      const T we = w[e];
 #pragma unroll
-    for (int q = 0; q < kChunk; q++) acc[q] = 0.0;
-    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    while (e < n) {
-      T run[kChunk];
-#pragma unroll
-      for (int q = 0; q < kChunk; q++) run[q] = T(0);
-      for (int r = 0; r < 8 && e < n; r++, e += stride) {
-        const T we = w[e];
-#pragma unroll
-        for (int q = 0; q < kChunk; q++)
-          if (v0 + q < nv) run[q] += V[(size_t)(v0 + q) * n + e] * we;
-      }
-#pragma unroll
-      for (int q = 0; q < kChunk; q++) acc[q] += (double)run[q];
+      for (int q = 0; q < kChunk; q++)
+        if (v0 + q < nv) acc[q].add(V[(size_t)(v0 + q) * n + e] * we);
     }
     block_chunk(acc, v0, nv, partial);
   }
@@ -517,29 +703,19 @@ __global__ void __launch_bounds__(kB) k_orth1_dots2(size_t n, T *__restrict__ V,
   T *w = V + (size_t)nv * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (int v0 = 0; v0 < nslot; v0 += kChunk) {
-    double acc[kChunk];
-#pragma unroll
-    for (int q = 0; q < kChunk; q++) acc[q] = 0.0;
-    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    while (e < n) {
-      T run[kChunk];
-#pragma unroll
-      for (int q = 0; q < kChunk; q++) run[q] = T(0);
-      for (int r = 0; r < 8 && e < n; r++, e += stride) {
-        T s = w[e];
-        if (v0 == 0) {
-          for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
-          w[e] = s;
-        }
-#pragma unroll
-        for (int q = 0; q < kChunk; q++) {
-          const int v = v0 + q;
-          if (v < nv) run[q] += V[(size_t)v * n + e] * s;
-          else if (v == nv) run[q] += s * s;
-        }
+    KSum<T> acc[kChunk];
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
+      T s = w[e];
+      if (v0 == 0) {
+        for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
+        w[e] = s;
       }
 #pragma unroll
-      for (int q = 0; q < kChunk; q++) acc[q] += (double)run[q];
+      for (int q = 0; q < kChunk; q++) {
+        const int v = v0 + q;
+        if (v < nv) acc[q].add(V[(size_t)v * n + e] * s);
+        else if (v == nv) acc[q].add(s * s);
+      }
     }
     block_chunk(acc, v0, nslot, partial);
   }
@@ -606,17 +782,16 @@ __global__ void __launch_bounds__(1024) k_arnoldi(KrylovDev *kd, int nb, const d
 // preconditioner input vin (j = the step that just finished).
 template <typename T>
 __global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd, T *__restrict__ vin) {
+  __shared__ T h[kSlots + 1];
   const int j = kd->jprev, nv = j + 1;
+  if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h2[threadIdx.x] : T(0);
+  if (threadIdx.x == kSlots) h[kSlots] = (T)kd->inv_scale;
+  __syncthreads();
   T *w = V + (size_t)(j + 1) * n;
-  T h[kSlots];
-#pragma unroll
-  for (int q = 0; q < kSlots; q++) h[q] = q < nv ? (T)kd->h2[q] : T(0);
-  const T sc = (T)kd->inv_scale;
+  const T sc = h[kSlots];
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     T s = w[e];
-#pragma unroll
-    for (int q = 0; q < kSlots; q++)
-      if (q < nv) s -= h[q] * V[(size_t)q * n + e];
+    for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
     s *= sc;
     w[e] = s;
     vin[e] = s;
@@ -671,16 +846,11 @@ __global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, cons
 template <typename T>
 __global__ void k_sq_partial(size_t n, const T *__restrict__ b, double *__restrict__ partial) {
   __shared__ double sh[32];
-  double t = 0.0;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  while (e < n) {
-    T run = T(0);
-    for (int r = 0; r < 8 && e < n; r++, e += stride) run += b[e] * b[e];
-    t += (double)run;
-  }
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  KSum<T> acc;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    acc.add(b[e] * b[e]);
+  const T t = warp_sum(acc.value());
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)t;
   __syncthreads();
   if (threadIdx.x == 0) {
     double u = 0.0;
@@ -716,15 +886,13 @@ __global__ void k_cycle_solve(KrylovDev *kd) {
 // x += sum_q y[q] Z_q
 template <typename T>
 __global__ void k_cycle_combine(size_t n, const T *__restrict__ Z, const KrylovDev *__restrict__ kd, T *__restrict__ x) {
+  __shared__ T y[kKrylovMax];
   const int nj = kd->nits;
-  T y[kKrylovMax];
-#pragma unroll
-  for (int q = 0; q < kKrylovMax; q++) y[q] = q < nj ? (T)kd->y[q] : T(0);
+  if (threadIdx.x < kKrylovMax) y[threadIdx.x] = (int)threadIdx.x < nj ? (T)kd->y[threadIdx.x] : T(0);
+  __syncthreads();
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     T s = x[e];
-#pragma unroll
-    for (int q = 0; q < kKrylovMax; q++)
-      if (q < nj) s += y[q] * Z[(size_t)q * n + e];
+    for (int q = 0; q < nj; q++) s += y[q] * Z[(size_t)q * n + e];
     x[e] = s;
   }
 }
@@ -760,7 +928,7 @@ int mg_alloc(EcsCtx *ctx) {
     L.nx = nx; L.ny = ny; L.nz = nz;
     L.n = (size_t)nx * ny * nz;
     L.hx = hx; L.hy = hy; L.hz = hz;
-    T **arr[] = {&L.dens, &L.x, &L.b, &L.r, &L.t, &L.zl_a, &L.zl_cp, &L.zl_minv, &L.zl_q, &L.zl_dp};
+    T **arr[] = {&L.dens, &L.x, &L.b, &L.r, &L.t, &L.zl_a, &L.zl_cp, &L.zl_minv, &L.zl_q, &L.zl_fb, &L.zl_bb};
     for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, L.n * sizeof(T)));
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_a0g, (size_t)nx * ny * sizeof(T)));
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_qden, (size_t)nx * ny * sizeof(T)));
@@ -770,6 +938,11 @@ int mg_alloc(EcsCtx *ctx) {
     nx /= 2; ny /= 2; nz /= 2;
     hx *= 2; hy *= 2; hz *= 2;
   }
+  const size_t nc = mg.lv.back().n;
+  if (nc <= (size_t)kDirectMax) {
+    ECS_CUDA(ctx, cudaMalloc((void **)&mg.cinv, nc * nc * sizeof(T)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&mg.cwork, nc * 2 * nc * sizeof(T)));
+  }
   mg.built = true;
   return ECS_OK;
 }
@@ -777,7 +950,7 @@ int mg_alloc(EcsCtx *ctx) {
 template <typename T>
 ZlP<T> zl_of(MgLevel<T> &L) {
   ZlP<T> z;
-  z.a = L.zl_a; z.cp = L.zl_cp; z.minv = L.zl_minv; z.q = L.zl_q; z.dp = L.zl_dp;
+  z.a = L.zl_a; z.cp = L.zl_cp; z.minv = L.zl_minv; z.q = L.zl_q; z.fb = L.zl_fb; z.bb = L.zl_bb;
   z.a0g = L.zl_a0g; z.qden = L.zl_qden;
   return z;
 }
@@ -816,7 +989,14 @@ int mg_setup(EcsCtx *ctx) {
   }
   for (auto &L : mg.lv) {
     int ncol = L.nx * L.ny;
-    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L));
+    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L),
+                                                                               seg_len<T>(L.nz));
+    ECS_LAUNCHED(ctx);
+  }
+  if (mg.cinv) {
+    MgLevel<T> &C = mg.lv.back();
+    k_coarse_inverse<T><<<1, 1024, 0, ctx->stream>>>(op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, mg.cwork,
+                                                    mg.cinv);
     ECS_LAUNCHED(ctx);
   }
   return ECS_OK;
@@ -831,13 +1011,31 @@ int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
     ECS_LAUNCHED(ctx);
     r = L.r;
   }
-  int ncol = L.nx * L.ny;
-  k_zline_solve<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+  const int S = seg_len<T>(L.nz);
+  const dim3 grid((unsigned)((L.nx + 31) / 32), (unsigned)L.ny);
+  const dim3 block(32, (unsigned)((L.nz + S - 1) / S));
+  if (S == 8)
+    k_zline_seg<T, 8><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+  else if (S == 16)
+    k_zline_seg<T, 16><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+  else if (S == 32)
+    k_zline_seg<T, 32><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+  else
+    k_zline_seg<T, 64><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
 
-constexpr size_t kSmallCells = 4096;
+constexpr size_t kSmallCells = 512;
+constexpr size_t kSmallSmem = 200 * 1024;  // shared memory of the single-block cycle
+
+// Shared memory of a single-block cycle over levels l.. (4 vectors a level).
+template <typename T>
+size_t small_bytes(const Multigrid<T> &mg, size_t l) {
+  size_t cells = 0;
+  for (size_t q = l; q < mg.lv.size(); q++) cells += mg.lv[q].n;
+  return cells * 4 * sizeof(T);
+}
 
 // One V(1,1) cycle on level l: xout = M(l) b, zero initial guess.  Levels of
 // at most kSmallCells cells run as one single-block kernel.
@@ -846,16 +1044,27 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
   Multigrid<T> &mg = mg_of<T>(ctx);
   MgLevel<T> &L = mg.lv[l];
   int rc;
-  if (L.n <= kSmallCells && mg.lv.size() - l <= (size_t)kMaxSmall) {
+  if (L.n <= kSmallCells && mg.lv.size() - l <= (size_t)kMaxSmall && small_bytes(mg, l) <= kSmallSmem) {
     SmallCycle<T> sc;
     sc.nl = (int)(mg.lv.size() - l);
+    sc.cinv = mg.cinv;
+    int off = 0;
     for (int q = 0; q < sc.nl; q++) {
       MgLevel<T> &M = mg.lv[l + q];
       sc.lv[q].o = op_level(ctx, M);
-      sc.lv[q].dens = M.dens; sc.lv[q].x = M.x; sc.lv[q].b = M.b; sc.lv[q].r = M.r; sc.lv[q].t = M.t;
+      sc.lv[q].dens = M.dens;
       sc.lv[q].z = zl_of(M);
+      const int nq = (int)M.n;
+      sc.lv[q].sx = off; sc.lv[q].sb = off + nq; sc.lv[q].sr = off + 2 * nq; sc.lv[q].st = off + 3 * nq;
+      off += 4 * nq;
     }
-    k_vcycle_small<T><<<1, 512, 0, ctx->stream>>>(sc, b, xout, kCoarseSweeps, kOmega<T>());
+    const size_t bytes = (size_t)off * sizeof(T);
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[sizeof(T) == 8]) {
+      ECS_CUDA(ctx, cudaFuncSetAttribute(k_vcycle_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem));
+      attr_set[sizeof(T) == 8] = true;
+    }
+    k_vcycle_small<T><<<1, kSmallThreads, bytes, ctx->stream>>>(sc, b, xout, kCoarseSweeps, kOmega<T>());
     ECS_LAUNCHED(ctx);
     return ECS_OK;
   }
@@ -1113,11 +1322,14 @@ __global__ void k_residual64(OpK o, const double *__restrict__ n, const double *
 template <typename T>
 void free_mg(Multigrid<T> &mg) {
   for (auto &L : mg.lv) {
-    T *arr[] = {L.dens, L.x, L.b, L.r, L.t, L.zl_a, L.zl_cp, L.zl_minv, L.zl_q, L.zl_dp, L.zl_a0g, L.zl_qden};
+    T *arr[] = {L.dens, L.x, L.b, L.r, L.t, L.zl_a, L.zl_cp, L.zl_minv, L.zl_q, L.zl_fb, L.zl_bb, L.zl_a0g, L.zl_qden};
     for (T *a : arr)
       if (a) cudaFree(a);
   }
   mg.lv.clear();
+  if (mg.cinv) cudaFree(mg.cinv);
+  if (mg.cwork) cudaFree(mg.cwork);
+  mg.cinv = mg.cwork = nullptr;
   mg.built = false;
 }
 

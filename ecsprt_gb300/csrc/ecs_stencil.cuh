@@ -67,7 +67,14 @@ __device__ __forceinline__ void cell_ijk(unsigned c, const GridG &g, int &i, int
 struct OpK {
   GridG g;
   double sxx, syy, szz, sod;
+  float fxx, fyy, fzz, fod;  // the same scales rounded to FP32 (FP32 rows)
 };
+__device__ __forceinline__ void op_scales(const OpK &o, double &a, double &b, double &c, double &d) {
+  a = o.sxx; b = o.syy; c = o.szz; d = o.sod;
+}
+__device__ __forceinline__ void op_scales(const OpK &o, float &a, float &b, float &c, float &d) {
+  a = o.fxx; b = o.fyy; c = o.fzz; d = o.fod;
+}
 
 // Stencil offsets (di, dj, dk) of the 11 row entries, in the reference's
 // order: x+, x-, y+, y-, z+, z-, (x+,y+), (x+,y-), (x-,y+), (x-,y-), centre.
@@ -83,7 +90,8 @@ __device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int
   T nmjk = gval(n, g, k, j, i - 1), npjk = gval(n, g, k, j, i + 1);
   T nimk = gval(n, g, k, j - 1, i), nipk = gval(n, g, k, j + 1, i);
   T nijm = gval(n, g, k - 1, j, i), nijp = gval(n, g, k + 1, j, i);
-  T sxx = T(o.sxx), syy = T(o.syy), szz = T(o.szz), sod = T(o.sod);
+  T sxx, syy, szz, sod;
+  op_scales(o, sxx, syy, szz, sod);
   v[6] = sod * (nipk - npjk);
   v[7] = sod * (npjk - nimk);
   v[8] = sod * (nmjk - nipk);
@@ -139,6 +147,7 @@ static inline OpK make_op(const EcsParams &p, int nx, int ny, int nz, double hx,
   o.syy = scale * hyy;
   o.szz = scale * (1 + kappa * kappa) * hzz;
   o.sod = scale * kappa * hod;
+  o.fxx = (float)o.sxx; o.fyy = (float)o.syy; o.fzz = (float)o.szz; o.fod = (float)o.sod;
   return o;
 }
 static inline GridG make_grid(const EcsParams &p, int nx, int ny, int nz) {
