@@ -6,7 +6,7 @@ Workload (N=1): 128^3 periodic grid, dx = 1 (normalised), 64 ions per cell
 gyrofrequency 0.1, ion-neutral collision frequency 0.02 (Maxwellian neutrals
 at the ion temperature), kappa_e ~ 2, dt = 0.1, variable-coefficient
 potential solve to 1e-8 relative residual.  Mixed path: FP32 cell-sorted
-particles (sorted every 4 steps), FP32 multigrid-FGMRES inside FP64
+particles (sorted every 2 steps), FP32 multigrid-FGMRES inside FP64
 iterative refinement.  Synthetic seeded data (no dataset exists for this
 benchmark).
 
@@ -39,6 +39,7 @@ WORKLOAD = {
     "name": "128^3 periodic, 64 ions/cell, drift 1.0, nu 0.02, density 1+0.05 sin(2 pi x/Lx)",
     "n": 128, "ppc": 64, "dt": 0.1, "drift": 1.0, "nu": 0.02, "seed": 20261205,
 }
+SORT_EVERY = 2          # cell sort cadence of the mixed path
 ALGO_BYTES_MIXED = 56   # per particle-step: (int32 cell + 3 FP32 offset + 3 FP32 v) read + written
 ALGO_BYTES_FP64 = 96    # per particle-step: 6 FP64 read + written
 
@@ -241,7 +242,7 @@ def run_ours(args, world, rank, local):
 
     # ---------------- device-resident mixed path -----------------------
     ctx = E.Context(p, E.ECS_PREC_MIXED, np_capacity=N, stream=stream.cuda_stream)
-    ctx.set_sort_every(4)
+    ctx.set_sort_every(SORT_EVERY)
     ctx.upload_particles(pos, vel)
     ctx.collect()
     ctx.compute_potential(rtol=rtol, max_it=400)
@@ -325,7 +326,7 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": w["name"], "grid": [w["n"]] * 3, "ions": N, "ppc": w["ppc"], "dt": dt,
                    "precision": "mixed (FP32 particles + FP32 MG-FGMRES inside FP64 refinement)",
-                   "solve_rtol": rtol, "sort_every": 4,
+                   "solve_rtol": rtol, "sort_every": SORT_EVERY,
                    "l2": "inputs larger than L2 (7.5 GB of particles per step)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": "k_particles32 (fused push+collide+move+deposit)",

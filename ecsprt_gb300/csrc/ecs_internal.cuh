@@ -91,7 +91,7 @@ struct EcsCtx {
   int32_t *sort_count = nullptr;   // [ncell]
   int32_t *sort_offset = nullptr;  // [ncell+1]
   int32_t *scan_blocks = nullptr;  // block sums of the scan
-  int sort_every = 4;
+  int sort_every = 2;
   int steps_since_sort = 0;
 
   // Grid fields.

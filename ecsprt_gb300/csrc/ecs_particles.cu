@@ -140,6 +140,9 @@ struct PartK {
   // collisions, src/collisions.c:18-63
   int collide;
   double rate, vrm2, viT, vnT, vn0[3], mi, mn, M;
+  // the same in FP32 (mixed path): attempt rate, 1/vrm^2, neutral thermal
+  // speed and drift, mi/M, mn/M, 10 viT
+  float ratef, ivrm2f, vnTf, vn0f[3], wif, wnf, vlimf;
   float p0f;          // exp(-rate)
   uint32_t stepmix;   // step and seed mixed for the attempt uniform
   uint32_t key0, key1, step;
@@ -276,6 +279,31 @@ __device__ float accept_sample(const PartK &k, uint32_t h0, uint32_t h1, T vx, T
   return (float)accept_prob<T>((wx * wx + wy * wy + wz * wz) / T(k.vrm2));
 }
 
+// Collision constants in the arithmetic type of the pass.
+template <typename T>
+struct CollK;
+template <>
+struct CollK<float> {
+  float rate, ivrm2, vnT, vn0[3], wi, wn, vlim;
+  __device__ __forceinline__ explicit CollK(const PartK &k)
+      : rate(k.ratef), ivrm2(k.ivrm2f), vnT(k.vnTf), vn0{k.vn0f[0], k.vn0f[1], k.vn0f[2]}, wi(k.wif),
+        wn(k.wnf), vlim(k.vlimf) {}
+};
+template <>
+struct CollK<double> {
+  double rate, vrm2, vnT, vn0[3], mi, mn, M, viT;
+  __device__ __forceinline__ explicit CollK(const PartK &k)
+      : rate(k.rate), vrm2(k.vrm2), vnT(k.vnT), vn0{k.vn0[0], k.vn0[1], k.vn0[2]}, mi(k.mi), mn(k.mn), M(k.M),
+        viT(k.viT) {}
+};
+// acceptance test U1 U2 < |vr|^2 / vrm^2, centre-of-mass velocity, refusal
+__device__ __forceinline__ bool coll_accept(const CollK<float> &c, float u, float vrr2) { return u < vrr2 * c.ivrm2; }
+__device__ __forceinline__ bool coll_accept(const CollK<double> &c, double u, double vrr2) { return u < vrr2 / c.vrm2; }
+__device__ __forceinline__ float coll_vc(const CollK<float> &c, float vi, float vn) { return vi * c.wi + vn * c.wn; }
+__device__ __forceinline__ double coll_vc(const CollK<double> &c, double vi, double vn) { return (vi * c.mi + vn * c.mn) / c.M; }
+__device__ __forceinline__ bool coll_refuse(const CollK<float> &c, float vf2) { return sqrtf(vf2) > c.vlim; }
+__device__ __forceinline__ bool coll_refuse(const CollK<double> &c, double vf2) { return sqrt(vf2) / c.viT > 10.0; }
+
 // One ion's collisions in one pass (src/collisions.c:70-157): a Poisson
 // number of attempts (rate k.rate) by inversion of a uniform drawn from the
 // state hash mixed with the step and seed; each attempt draws a Maxwellian
@@ -288,8 +316,9 @@ __device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &
   const uint32_t hu = ecs_mix32(h1 ^ k.stepmix);
   const float u = ecs_u01f(hu);
   if (u <= k.p0f) return;  // no attempt (the common case)
+  const CollK<T> ck(k);
   float p = k.p0f, cdf = p;
-  const float rate = (float)k.rate;
+  const float rate = k.ratef;
   int natt = 0;
   while (u > cdf && natt < 16) {
     natt++;
@@ -313,18 +342,17 @@ __device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &
       M::sincospi_(T(2) * M::u01(q1.z, q1.w), &sa, &ca);
       M::sincospi_(T(2) * M::u01(q3.z, q3.w), &sb, &cb);
     }
-    T vn[3] = {ra * ca * T(k.vnT) + T(k.vn0[0]), ra * sa * T(k.vnT) + T(k.vn0[1]),
-               rb * cb * T(k.vnT) + T(k.vn0[2])};
+    T vn[3] = {ra * ca * ck.vnT + ck.vn0[0], ra * sa * ck.vnT + ck.vn0[1], rb * cb * ck.vnT + ck.vn0[2]};
     T vi[3] = {vx, vy, vz};
     T vr[3] = {vi[0] - vn[0], vi[1] - vn[1], vi[2] - vn[2]};
     T vrr2 = vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2];
     T U1 = M::u01(q2.x, q2.x), U2 = M::u01(q2.y, q2.y);
-    if (!(U1 * U2 < vrr2 / T(k.vrm2))) continue;
+    if (!coll_accept(ck, U1 * U2, vrr2)) continue;
     T vrr = M::sqrt_(vrr2);
     T vc[3], tmp = T(0);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      vc[d] = (vi[d] * T(k.mi) + vn[d] * T(k.mn)) / T(k.M);
+      vc[d] = coll_vc(ck, vi[d], vn[d]);
       tmp += (vi[d] - vc[d]) * (vi[d] - vc[d]);
     }
     T vcr = M::sqrt_(tmp);
@@ -354,7 +382,7 @@ __device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &
       vf[d] = vc[d] + vcr * u2[d];
       vf2 += vf[d] * vf[d];
     }
-    if (M::sqrt_(vf2) / T(k.viT) > T(10)) {
+    if (coll_refuse(ck, vf2)) {
       nref++;
     } else {
       vx = vf[0];
@@ -970,6 +998,12 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   k.vnT = p.vnT;
   k.vn0[0] = p.vn0x; k.vn0[1] = p.vn0y; k.vn0[2] = p.vn0z;
   k.mi = p.mi; k.mn = p.mn; k.M = p.mn + p.mi;
+  k.ivrm2f = (float)(1.0 / k.vrm2);
+  k.vnTf = (float)k.vnT;
+  for (int d = 0; d < 3; d++) k.vn0f[d] = (float)k.vn0[d];
+  k.wif = (float)(k.mi / k.M);
+  k.wnf = (float)(k.mn / k.M);
+  k.vlimf = (float)(10.0 * k.viT);
   k.key0 = (uint32_t)ctx->seed;
   k.key1 = (uint32_t)(ctx->seed >> 32);
   k.step = (uint32_t)ctx->step_index;
@@ -1105,6 +1139,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
       if (rc) return rc;
     }
     k.rate = ctx->attempt_rate;
+    k.ratef = (float)k.rate;
     k.p0f = (float)exp(-k.rate);
     ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   }

@@ -461,7 +461,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
 }
 
 // ---- direct solve of the coarsest level -----------------------------------------
-constexpr int kDirectMax = 128;  // largest coarsest level solved directly
+constexpr int kDirectMax = 128;           // largest coarsest level solved directly
+constexpr size_t kInverseSmem = 160 * 1024;  // shared memory of its Gauss-Jordan work matrix
 
 // invT = (A + sigma 1 1^T)^-1, transposed (invT[k n + r] = inv[r][k]), by
 // Gauss-Jordan elimination with partial pivoting on M = [A | I] (n x 2n, in
@@ -471,7 +472,9 @@ constexpr int kDirectMax = 128;  // largest coarsest level solved directly
 // reproducible.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restrict__ dens, int regularize,
-                                                         T *__restrict__ M, T *__restrict__ invT) {
+                                                         T *__restrict__ Mg, T *__restrict__ invT) {
+  extern __shared__ unsigned char inv_smem[];
+  T *M = Mg ? Mg : reinterpret_cast<T *>(inv_smem);  // work matrix in shared memory when it fits
   __shared__ T fac[kDirectMax];
   __shared__ T wv[32];
   __shared__ int wi[32];
@@ -995,8 +998,15 @@ int mg_setup(EcsCtx *ctx) {
   }
   if (mg.cinv) {
     MgLevel<T> &C = mg.lv.back();
-    k_coarse_inverse<T><<<1, 1024, 0, ctx->stream>>>(op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, mg.cwork,
-                                                    mg.cinv);
+    const size_t bytes = C.n * 2 * C.n * sizeof(T);
+    const bool in_smem = bytes <= kInverseSmem;
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[sizeof(T) == 8]) {
+      ECS_CUDA(ctx, cudaFuncSetAttribute(k_coarse_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInverseSmem));
+      attr_set[sizeof(T) == 8] = true;
+    }
+    k_coarse_inverse<T><<<1, 1024, in_smem ? bytes : 0, ctx->stream>>>(
+        op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, in_smem ? nullptr : mg.cwork, mg.cinv);
     ECS_LAUNCHED(ctx);
   }
   return ECS_OK;

@@ -117,7 +117,7 @@ int ecs_ctx_destroy(EcsCtx *ctx);
 int ecs_ctx_sync(EcsCtx *ctx);
 /* Device bytes held by a context of these sizes (for admission control). */
 int64_t ecs_ctx_device_bytes(const EcsParams *params, int precision, int64_t np_capacity);
-/* Cell-sort cadence of the mixed path (default 4; 0 disables sorting). */
+/* Cell-sort cadence of the mixed path (default 2; 0 disables sorting). */
 int ecs_set_sort_every(EcsCtx *ctx, int every);
 /* Seed of the counter-based collision RNG (default 20261203). */
 int ecs_set_seed(EcsCtx *ctx, uint64_t seed);
