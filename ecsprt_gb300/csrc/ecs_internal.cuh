@@ -17,7 +17,14 @@
 // density uses S = ECS_FIX_SHIFT_*; the flux uses S - e_v, where 2^e_v bounds
 // |v| (ecs_fix_shifts), so every contribution is at most 2^S in magnitude.
 #define ECS_FIX_SHIFT_FP64 48
-#define ECS_FIX_SHIFT_MIXED 40
+#define ECS_FIX_SHIFT_MIXED 38
+
+// Cell tiles of the mixed path (the deposit accumulates a tile in shared
+// memory).
+#define ECS_TILE_X 4
+#define ECS_TILE_Y 4
+#define ECS_TILE_Z 2
+#define ECS_TILE_CELLS (ECS_TILE_X * ECS_TILE_Y * ECS_TILE_Z)
 
 // Device status word bits (EcsDevStatus::flags).
 #define ECS_FLAG_NONFINITE 1u
@@ -88,9 +95,14 @@ struct EcsCtx {
   // double-buffered for the counting sort.
   float4 *ions[2] = {nullptr, nullptr};
   int cur = 0;
-  int32_t *sort_count = nullptr;   // [ncell]
-  int32_t *sort_offset = nullptr;  // [ncell+1]
+  // The sort key orders the ions by tiles of ECS_TILE_X x ECS_TILE_Y x
+  // ECS_TILE_Z cells (tile-major, x fastest), then by cell within the tile.
+  int ntile[3] = {0, 0, 0};        // tiles per axis
+  size_t nkeys = 0;                // ntiles * cells per tile
+  int32_t *sort_count = nullptr;   // [nkeys]
+  int32_t *sort_offset = nullptr;  // [nkeys+1]: ions of key q at [offset[q], offset[q+1])
   int32_t *scan_blocks = nullptr;  // block sums of the scan
+  bool tiles_valid = false;        // the buffer is ordered by the keys of sort_offset
   int sort_every = 2;
   int steps_since_sort = 0;
 

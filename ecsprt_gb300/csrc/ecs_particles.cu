@@ -50,6 +50,10 @@ __device__ __forceinline__ rd operator/(rd a, rd b) { return {__ddiv_rn(a.v, b.v
 
 constexpr int kBlock = 256;
 
+struct TileG {
+  int ntx, nty, ntz;  // tiles per axis
+};
+
 // ---- deposit fixed point ---------------------------------------------------
 // FP64: rint(v 2^S) by the FP64 conversion.
 struct FixScale64 {
@@ -57,22 +61,31 @@ struct FixScale64 {
   __device__ __forceinline__ long long put(double v) const { return __double2ll_rn(v * s); }
 };
 
-// FP32: the same integer, rint(v 2^S) with |v 2^S| <= 2^42, from FP32 adds and
-// multiply-adds only (on sm_103 a float-to-int64 conversion issues on the
-// narrow FP64 pipe).  With H = rint(v 2^(S-20)):
-//   v 2^S = H 2^20 + r,  |r| <= 2^19, r exact in FP32,
-//   rint(v 2^S) = H 2^20 + rint(r)   (2^20 H is even, so ties round alike).
-// Both integers come from adding the bias B = 1.5 * 2^23: for |t| <= 2^22,
-// fl(t + B) lies in [2^23, 2^24], where the spacing of floats is 1, so the
-// addition rounds t to the nearest integer (ties to even) and the bit pattern
-// of the sum is bits(B) + rint(t).  The two biased words are stored as one
-// 64-bit tile entry (low word H, high word rint(r)); sums over a group of n
-// lanes remove the bias n * bits(B) from each word (wrap-around int32
-// arithmetic) before recombining in int64.
+// FP32: the same integer, rint(v 2^S) with |v 2^S| <= 2^38 (S = 38 on the
+// mixed path), from FP32 adds and multiply-adds only (on sm_103 a
+// float-to-int64 conversion issues on the narrow FP64 pipe).  With the split
+// bit B = kFixSplit and H = rint(v 2^(S-B)), |H| <= 2^19:
+//   v 2^S = H 2^B + r,  |r| <= 2^(B-1), r exact in FP32,
+//   rint(v 2^S) = H 2^B + rint(r)   (2^B H is even, so ties round alike).
+// Both integers come from adding the bias 1.5 * 2^23: for |t| <= 2^22,
+// fl(t + bias) lies in [2^23, 2^24], where the spacing of floats is 1, so
+// the addition rounds t to the nearest integer (ties to even) and the bit
+// pattern of the sum is bits(bias) + rint(t).  H and rint(r) are each summed
+// in int32: over at most kWindowMax contributions they cannot overflow.
 constexpr float kFixBias = 12582912.0f;  // 1.5 * 2^23
 constexpr unsigned kFixBiasBits = 0x4B400000u;
+constexpr int kFixSplit = 19;
 struct FixScale32 {
-  float s, s_hi, s_back;  // 2^S, 2^(S-20), -2^(20-S)
+  float s, s_hi, s_back;  // 2^S, 2^(S-B), -2^(B-S)
+  // unbiased (H, rint(r))
+  __device__ __forceinline__ void split(float v, int &hi, int &lo) const {
+    const float h = __fmaf_rn(v, s_hi, kFixBias);
+    const float r = __fmaf_rn(__fsub_rn(h, kFixBias), s_back, v);
+    const float l = __fmaf_rn(r, s, kFixBias);
+    hi = (int)(__float_as_uint(h) - kFixBiasBits);
+    lo = (int)(__float_as_uint(l) - kFixBiasBits);
+  }
+  // biased words packed in one 64-bit entry (low word H, high word rint(r))
   __device__ __forceinline__ long long put(float v) const {
     const float h = __fmaf_rn(v, s_hi, kFixBias);
     const float r = __fmaf_rn(__fsub_rn(h, kFixBias), s_back, v);
@@ -80,10 +93,11 @@ struct FixScale32 {
     return (long long)(((unsigned long long)__float_as_uint(l) << 32) | __float_as_uint(h));
   }
 };
+__device__ __forceinline__ long long fix_join(int hi, int lo) { return (long long)hi * (1ll << kFixSplit) + lo; }
+// sums of n biased entries: remove n * bits(bias) from each word (wrap-around
+// int32 arithmetic), then recombine in int64
 __device__ __forceinline__ long long fix_unbias(unsigned hi_sum, unsigned lo_sum, int n) {
-  const int hi = (int)(hi_sum - (unsigned)n * kFixBiasBits);
-  const int lo = (int)(lo_sum - (unsigned)n * kFixBiasBits);
-  return (long long)hi * 1048576ll + lo;
+  return fix_join((int)(hi_sum - (unsigned)n * kFixBiasBits), (int)(lo_sum - (unsigned)n * kFixBiasBits));
 }
 
 // Exact sum of the tile entries q in `m` (bit mask of lanes).
@@ -152,6 +166,7 @@ struct PartK {
   FixScale32 fixn32, fixf32;
   double vmax;
   float vmaxf;
+  TileG tg;
 };
 
 // ---- deposit ---------------------------------------------------------------
@@ -605,8 +620,14 @@ __device__ __forceinline__ void store_ion(float4 *ions, int64_t ip, const Ion &q
 __device__ __forceinline__ int32_t ion_cell(const float4 *ions, int64_t ip) {
   return __ldcs(reinterpret_cast<const int32_t *>(ions) + 8 * ip);
 }
-__device__ __forceinline__ int lin_cell(int32_t c, int Nx, int Ny) {
-  return (((c >> 20) & 1023) * Ny + ((c >> 10) & 1023)) * Nx + (c & 1023);
+// Sort key of cell (i, j, k): tile-major (tiles of ECS_TILE_X x ECS_TILE_Y x
+// ECS_TILE_Z cells, x fastest), then the cell within its tile.
+__device__ __forceinline__ int tile_key(int i, int j, int k, const TileG &t) {
+  const int tile = ((k / ECS_TILE_Z) * t.nty + j / ECS_TILE_Y) * t.ntx + i / ECS_TILE_X;
+  return tile * ECS_TILE_CELLS + ((k % ECS_TILE_Z) * ECS_TILE_Y + j % ECS_TILE_Y) * ECS_TILE_X + i % ECS_TILE_X;
+}
+__device__ __forceinline__ int cell_key(int32_t c, const TileG &t) {
+  return tile_key(c & 1023, (c >> 10) & 1023, (c >> 20) & 1023, t);
 }
 
 // Warp-aggregated count of the lanes' cells (inactive lanes pass key < 0).
@@ -686,6 +707,62 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
   state_hash(w, 7, h0, h1);
 }
 
+// Push (src/velocities.c:281-371), collisions (src/collisions.c:9-167) and
+// move + boundary conditions (src/positions.c:436-472) of one ion, in the
+// pass's mode bits.  Returns the ion in cell (i, j, kk) with offsets o*.
+struct IonState {
+  int i, j, kk;
+  float ox, oy, oz, vx, vy, vz;
+};
+__device__ __forceinline__ void ion_update(const PartK &k, int mode, const float4 *__restrict__ E, EcsDevStatus *st,
+                                           IonState &q, unsigned int &nacc, unsigned int &nref) {
+  if (mode & 1) {
+    float f[3];
+    gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
+    float vxm = q.vx + k.escf[0] * f[0];
+    float vym = q.vy + k.escf[1] * f[1];
+    float vzm = q.vz + k.escf[2] * f[2];
+    float vxt = vxm + vym * k.tf;
+    float vyp = vym - vxt * k.sf;
+    float vxp = vxt + vyp * k.tf;
+    q.vx = vxp;
+    q.vy = vyp;
+    q.vz = vzm;
+  }
+  if ((mode & 2) && k.collide) {
+    uint32_t h0, h1;
+    hash32(q.i | (q.j << 10) | (q.kk << 20), q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, h0, h1);
+    collide_ion<float>(k, h0, h1, q.vx, q.vy, q.vz, nacc, nref);
+  }
+  if (mode & 4) {
+    q.i += advance(q.ox, q.vx * k.dtc[0]);
+    q.j += advance(q.oy, q.vy * k.dtc[1]);
+    q.kk += advance(q.oz, q.vz * k.dtc[2]);
+    const bool inside = bound_axis(k.bc[0], k.Nx, q.i, q.ox, q.vx) & bound_axis(k.bc[1], k.Ny, q.j, q.oy, q.vy) &
+                        bound_axis(k.bc[2], k.Nz, q.kk, q.oz, q.vz);
+    if (!inside) {
+      atomicOr(&st->flags, ECS_FLAG_RANGE);
+      q.i = min(max(q.i, 0), k.Nx - 1);
+      q.j = min(max(q.j, 0), k.Ny - 1);
+      q.kk = min(max(q.kk, 0), k.Nz - 1);
+    }
+  }
+  if (!(isfinite(q.vx) && isfinite(q.vy) && isfinite(q.vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
+  if ((mode & 8) && !(fabsf(q.vx) <= k.vmaxf && fabsf(q.vy) <= k.vmaxf && fabsf(q.vz) <= k.vmaxf))
+    atomicOr(&st->flags, ECS_FLAG_RANGE);
+}
+__device__ __forceinline__ IonState ion_state(const Ion &r) {
+  IonState q;
+  unpack_cell(r.c, q.i, q.j, q.kk);
+  q.ox = r.ox; q.oy = r.oy; q.oz = r.oz; q.vx = r.vx; q.vy = r.vy; q.vz = r.vz;
+  return q;
+}
+__device__ __forceinline__ Ion ion_record(const IonState &q) {
+  return {q.i | (q.j << 10) | (q.kk << 20), q.ox, q.oy, q.oz, q.vx, q.vy, q.vz};
+}
+
+// Any ion order: grid-stride over ions, deposit by warp-level cell groups
+// (deposit_warp) into global int64 accumulators.
 __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, int64_t np, float4 *ions,
                                                          const float4 *__restrict__ E,
                                                          long long *__restrict__ acc,
@@ -698,57 +775,134 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
        base += stride) {
     const int64_t ip = base + lane;
     const bool active = ip < np;
-    Ion q = {0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (active) q = load_ion(ions, ip);
-    float ox = q.ox, oy = q.oy, oz = q.oz, vx = q.vx, vy = q.vy, vz = q.vz;
-    int32_t c = q.c;
-    int i, j, kk;
-    unpack_cell(c, i, j, kk);
-    if ((mode & 1) && active) {
-      float f[3];
-      gather32(E, k, i, j, kk, ox, oy, oz, f);
-      float vxm = vx + k.escf[0] * f[0];
-      float vym = vy + k.escf[1] * f[1];
-      float vzm = vz + k.escf[2] * f[2];
-      float vxt = vxm + vym * k.tf;
-      float vyp = vym - vxt * k.sf;
-      float vxp = vxt + vyp * k.tf;
-      vx = vxp;
-      vy = vyp;
-      vz = vzm;
-    }
+    IonState q = ion_state(active ? load_ion(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
     unsigned int nacc = 0, nref = 0;
-    if ((mode & 2) && k.collide) {
-      if (active) {
-        uint32_t h0, h1;
-        hash32(c, ox, oy, oz, vx, vy, vz, h0, h1);
-        collide_ion<float>(k, h0, h1, vx, vy, vz, nacc, nref);
+    if (active) ion_update(k, mode, E, st, q, nacc, nref);
+    if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
+    if (count) count_cells(count, active ? tile_key(q.i, q.j, q.kk, k.tg) : -1);
+    if (mode & 8)
+      deposit_warp<float>(acc, tile, k, active, q.i, q.j, q.kk, q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, k.fixn32,
+                          k.fixf32);
+    if (active && (mode & 7)) store_ion(ions, ip, ion_record(q));
+  }
+}
+
+// ---- tile kernel: ions ordered by tile ----------------------------------------
+// One block per tile of cells processes the ions of the tile's key range
+// (the ions that were in the tile at the last sort) in chunks of at most
+// kWindowMax.  Each chunk deposits into a shared-memory window of the nodes
+// of the tile's cells widened by one cell on every side: the two int32 words
+// of each contribution's fixed-point value (H, rint(r)) are added with
+// shared-memory atomics, and the window is added to the global int64
+// accumulators once per chunk.  The chunk is split into 32 consecutive
+// segments, one per lane, so the lanes of a warp work on different cells and
+// rarely on the same node.  Ions outside the window (moved farther, or
+// wrapped around a periodic edge) deposit straight into the global
+// accumulators.  The cells of the moved ions are counted the same way when a
+// sort follows.  All sums are exact integers, so the moments equal those of
+// k_particles32 bit for bit.
+constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
+constexpr int kWNodes = kWX * kWY * kWZ;
+constexpr int kCX = ECS_TILE_X + 2, kCY = ECS_TILE_Y + 2, kCZ = ECS_TILE_Z + 2;  // window cells per axis
+constexpr int kWCells = kCX * kCY * kCZ;
+// |H| <= 2^19 and |rint(r)| <= 2^18, so 4000 contributions to one word stay
+// below 2^31
+constexpr int kWindowMax = 4000;
+
+__global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
+                                                     long long *__restrict__ acc, const int32_t *__restrict__ key_off,
+                                                     int32_t *__restrict__ count, EcsDevStatus *st) {
+  __shared__ int win[4][2][kWNodes];  // [field][H, rint(r)][node]
+  __shared__ int wcnt[kWCells];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = k.tg.ntx * k.tg.nty * k.tg.ntz;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tx = t % k.tg.ntx, ty = (t / k.tg.ntx) % k.tg.nty, tz = t / (k.tg.ntx * k.tg.nty);
+    // window origin: one cell below the tile on every axis
+    const int wx0 = tx * ECS_TILE_X - 1, wy0 = ty * ECS_TILE_Y - 1, wz0 = tz * ECS_TILE_Z - 1;
+    const int a = key_off[t * ECS_TILE_CELLS], b = key_off[(t + 1) * ECS_TILE_CELLS];
+    for (int ca = a; ca < b; ca += kWindowMax) {
+      const int L = min(kWindowMax, b - ca);
+      const int seg = (L + 31) >> 5;
+      if (mode & 8)
+        for (int e = threadIdx.x; e < 8 * kWNodes; e += blockDim.x) (&win[0][0][0])[e] = 0;
+      if (count)
+        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
+      __syncthreads();
+      for (int m = warp; m < seg; m += kBlock / 32) {  // warp-uniform trip count
+        const int qi = lane * seg + m;
+        const bool active = qi < L;
+        const int64_t ip = (int64_t)ca + qi;
+        IonState q = ion_state(active ? load_ion(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
+        unsigned int nacc = 0, nref = 0;
+        if (active) ion_update(k, mode, E, st, q, nacc, nref);
+        if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
+        if (active) {
+          const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
+          if (count) {
+            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ)
+              atomicAdd(&wcnt[(lk * kCY + lj) * kCX + li], 1);
+            else
+              atomicAdd(&count[tile_key(q.i, q.j, q.kk, k.tg)], 1);
+          }
+          if (mode & 8) {
+            const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
+            const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
+            const bool inwin = li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ;
+            const int n0 = (lk * kWY + lj) * kWX + li;
+#pragma unroll
+            for (int bc = 0; bc < 8; bc++) {
+              const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
+              const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
+              const int nb = n0 + ((bc >> 2) * kWY + ((bc >> 1) & 1)) * kWX + (bc & 1);
+              const long long gnode = inwin ? 0 : corner_node(k, q.i, q.j, q.kk, bc);
+#pragma unroll
+              for (int f = 0; f < 4; f++) {
+                int hi, lo;
+                (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
+                if (inwin) {
+                  atomicAdd(&win[f][0][nb], hi);
+                  atomicAdd(&win[f][1][nb], lo);
+                } else if (gnode >= 0) {
+                  atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + gnode],
+                            (unsigned long long)fix_join(hi, lo));
+                }
+              }
+            }
+          }
+          if (mode & 7) store_ion(ions, ip, ion_record(q));
+        }
       }
-      flush_counts(st, nacc, nref);
-    }
-    bool inside = true;
-    if ((mode & 4) && active) {
-      i += advance(ox, vx * k.dtc[0]);
-      j += advance(oy, vy * k.dtc[1]);
-      kk += advance(oz, vz * k.dtc[2]);
-      inside = bound_axis(k.bc[0], k.Nx, i, ox, vx) & bound_axis(k.bc[1], k.Ny, j, oy, vy) &
-               bound_axis(k.bc[2], k.Nz, kk, oz, vz);
-      if (!inside) {
-        atomicOr(&st->flags, ECS_FLAG_RANGE);
-        i = min(max(i, 0), k.Nx - 1);
-        j = min(max(j, 0), k.Ny - 1);
-        kk = min(max(kk, 0), k.Nz - 1);
+      __syncthreads();
+      // window -> global accumulators
+      if (mode & 8) {
+        for (int e = threadIdx.x; e < 4 * kWNodes; e += blockDim.x) {
+          const int f = e / kWNodes, nd = e - f * kWNodes;
+          const long long v = fix_join(win[f][0][nd], win[f][1][nd]);
+          if (v == 0) continue;
+          const int wxn = nd % kWX, wyn = (nd / kWX) % kWY, wzn = nd / (kWX * kWY);
+          int gx = wx0 + wxn, gy = wy0 + wyn, gz = wz0 + wzn;
+          // nodes past the last cell wrap (periodic) or are dropped (ghosts)
+          if (gx < 0 || gx >= k.Nx) { if (k.bc[0]) continue; gx = gx < 0 ? gx + k.Nx : gx - k.Nx; }
+          if (gy < 0 || gy >= k.Ny) { if (k.bc[1]) continue; gy = gy < 0 ? gy + k.Ny : gy - k.Ny; }
+          if (gz < 0 || gz >= k.Nz) { if (k.bc[2]) continue; gz = gz < 0 ? gz + k.Nz : gz - k.Nz; }
+          atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + ((size_t)gz * k.Ny + gy) * k.Nx + gx],
+                    (unsigned long long)v);
+        }
       }
-      c = i | (j << 10) | (kk << 20);
+      if (count) {
+        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) {
+          const int n = wcnt[e];
+          if (n == 0) continue;
+          int gx = wx0 + e % kCX, gy = wy0 + (e / kCX) % kCY, gz = wz0 + e / (kCX * kCY);
+          if (gx < 0) gx += k.Nx; else if (gx >= k.Nx) gx -= k.Nx;  // cells of moved ions are in range
+          if (gy < 0) gy += k.Ny; else if (gy >= k.Ny) gy -= k.Ny;
+          if (gz < 0) gz += k.Nz; else if (gz >= k.Nz) gz -= k.Nz;
+          atomicAdd(&count[tile_key(gx, gy, gz, k.tg)], n);
+        }
+      }
+      __syncthreads();
     }
-    if (count) count_cells(count, active ? (kk * k.Ny + j) * k.Nx + i : -1);
-    if (active && !(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
-    if (mode & 8) {
-      if (active && !(fabsf(vx) <= k.vmaxf && fabsf(vy) <= k.vmaxf && fabsf(vz) <= k.vmaxf))
-        atomicOr(&st->flags, ECS_FLAG_RANGE);
-      deposit_warp<float>(acc, tile, k, active, i, j, kk, ox, oy, oz, vx, vy, vz, k.fixn32, k.fixf32);
-    }
-    if (active && (mode & 7)) store_ion(ions, ip, {c, ox, oy, oz, vx, vy, vz});
   }
 }
 
@@ -813,13 +967,12 @@ __global__ void k_mixed_to_aos(int64_t n, PartK k, double *__restrict__ pos,
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
-__global__ void k_sort_count(int64_t np, int Nx, int Ny, const float4 *__restrict__ ions,
-                             int32_t *__restrict__ count) {
+__global__ void k_sort_count(int64_t np, TileG tg, const float4 *__restrict__ ions, int32_t *__restrict__ count) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ip = base + lane;
-    count_cells(count, ip < np ? lin_cell(ion_cell(ions, ip), Nx, Ny) : -1);
+    count_cells(count, ip < np ? cell_key(ion_cell(ions, ip), tg) : -1);
   }
 }
 
@@ -888,18 +1041,18 @@ __global__ void k_scan_sums(int nb, int32_t *sums) {
     __syncthreads();
   }
 }
-__global__ void k_scan_add(int n, int32_t *__restrict__ out, const int32_t *__restrict__ sums,
-                           int32_t *__restrict__ total_out) {
+// out[i] += block sums; out[n] = total (the number of ions).
+__global__ void k_scan_add(int n, int32_t *__restrict__ out, const int32_t *__restrict__ sums, int total) {
   const int tile = kScanBlock * kScanItems;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] += sums[i / tile];
-  if (i == n - 1 && total_out) *total_out = out[i];
+  if (i == 0) out[n] = total;
 }
 
 // Every ion record moves whole (32 bytes, one sector) to slot
-// off[cell] + (its rank among the ions of its cell), ranks handed out by a
+// off[key] + (its rank among the ions of its cell), ranks handed out by a
 // warp-aggregated atomic cursor per cell.
-__global__ void k_sort_scatter(int64_t np, int Nx, int Ny, const int32_t *__restrict__ off,
+__global__ void k_sort_scatter(int64_t np, TileG tg, const int32_t *__restrict__ off,
                                int32_t *__restrict__ cursor, const float4 *__restrict__ src,
                                float4 *__restrict__ dst) {
   const int lane = threadIdx.x & 31;
@@ -911,7 +1064,7 @@ __global__ void k_sort_scatter(int64_t np, int Nx, int Ny, const int32_t *__rest
       a = __ldcs(src + 2 * ip);
       b = __ldcs(src + 2 * ip + 1);
     }
-    const int key = ip < np ? lin_cell(__float_as_int(a.x), Nx, Ny) : -1;
+    const int key = ip < np ? cell_key(__float_as_int(a.x), tg) : -1;
     const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
     const int leader = __ffs(peers) - 1;
     int slot = 0;
@@ -1014,10 +1167,11 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   }
   k.fixn64 = ldexp(1.0, ctx->shift_n);
   k.fixf64 = ldexp(1.0, ctx->shift_f);
-  k.fixn32 = {ldexpf(1.0f, ctx->shift_n), ldexpf(1.0f, ctx->shift_n - 20), -ldexpf(1.0f, 20 - ctx->shift_n)};
-  k.fixf32 = {ldexpf(1.0f, ctx->shift_f), ldexpf(1.0f, ctx->shift_f - 20), -ldexpf(1.0f, 20 - ctx->shift_f)};
+  k.fixn32 = {ldexpf(1.0f, ctx->shift_n), ldexpf(1.0f, ctx->shift_n - kFixSplit), -ldexpf(1.0f, kFixSplit - ctx->shift_n)};
+  k.fixf32 = {ldexpf(1.0f, ctx->shift_f), ldexpf(1.0f, ctx->shift_f - kFixSplit), -ldexpf(1.0f, kFixSplit - ctx->shift_f)};
   k.vmax = ldexp(1.0, ctx->shift_n - ctx->shift_f);
   k.vmaxf = (float)k.vmax;
+  k.tg = {ctx->ntile[0], ctx->ntile[1], ctx->ntile[2]};
   return k;
 }
 
@@ -1056,9 +1210,13 @@ int ecs_particles_alloc(EcsCtx *ctx) {
     for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(double)));
   } else {
     for (int b = 0; b < 2; b++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->ions[b], n * 2 * sizeof(float4)));
-    size_t nb = ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
-    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_count, ctx->ncell * sizeof(int32_t)));
-    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_offset, (ctx->ncell + 1) * sizeof(int32_t)));
+    ctx->ntile[0] = (ctx->p.Nx + ECS_TILE_X - 1) / ECS_TILE_X;
+    ctx->ntile[1] = (ctx->p.Ny + ECS_TILE_Y - 1) / ECS_TILE_Y;
+    ctx->ntile[2] = (ctx->p.Nz + ECS_TILE_Z - 1) / ECS_TILE_Z;
+    ctx->nkeys = (size_t)ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2] * ECS_TILE_CELLS;
+    size_t nb = ecs_div_up(ctx->nkeys, (size_t)kScanBlock * kScanItems);
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_count, ctx->nkeys * sizeof(int32_t)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_offset, (ctx->nkeys + 1) * sizeof(int32_t)));
     ECS_CUDA(ctx, cudaMalloc((void **)&ctx->scan_blocks, (nb + 1) * sizeof(int32_t)));
   }
   return ECS_OK;
@@ -1096,6 +1254,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
   ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
   ctx->np = np;
   ctx->attempt_rate = -1.0;
+  ctx->tiles_valid = false;
   if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
     int rc = ecs_part_sort(ctx);
     if (rc) return rc;
@@ -1153,7 +1312,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
   }
   int32_t *count = nullptr;
   if (count_for_sort && ctx->prec == ECS_PREC_MIXED) {
-    ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+    ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
     count = ctx->sort_count;
   }
   unsigned int g = grid_blocks(ctx, ctx->np, 3);
@@ -1161,6 +1320,10 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
   if (ctx->prec == ECS_PREC_FP64) {
     k_particles64<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                                 ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
+  } else if (ctx->tiles_valid) {
+    const int ntiles = ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2];
+    k_tiles32<<<ntiles, kBlock, 0, ctx->stream>>>(k, mode, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
+                                                  ctx->sort_offset, count, ctx->dstat);
   } else {
     k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
                                                 count, ctx->dstat);
@@ -1231,21 +1394,24 @@ static bool sort_due(const EcsCtx *ctx) {
 
 // Scan of the cell counts and the scatter into the other buffer.
 static int sort_counted(EcsCtx *ctx) {
-  const int n = (int)ctx->ncell;
-  const int nb = (int)ecs_div_up(ctx->ncell, (size_t)kScanBlock * kScanItems);
+  const int n = (int)ctx->nkeys;
+  const int nb = (int)ecs_div_up(ctx->nkeys, (size_t)kScanBlock * kScanItems);
   const int a = ctx->cur, b = 1 - ctx->cur;
   k_scan_local<<<nb, kScanBlock, 0, ctx->stream>>>(n, ctx->sort_count, ctx->sort_offset, ctx->scan_blocks);
   ECS_LAUNCHED(ctx);
   k_scan_sums<<<1, 1024, 0, ctx->stream>>>(nb, ctx->scan_blocks);
   ECS_LAUNCHED(ctx);
-  k_scan_add<<<ecs_div_up(ctx->ncell, 256), 256, 0, ctx->stream>>>(n, ctx->sort_offset, ctx->scan_blocks, nullptr);
+  k_scan_add<<<ecs_div_up(ctx->nkeys, 256), 256, 0, ctx->stream>>>(n, ctx->sort_offset, ctx->scan_blocks,
+                                                                  (int)ctx->np);
   ECS_LAUNCHED(ctx);
-  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
+  const PartK k = make_k(ctx, 0.0);
   k_sort_scatter<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(
-      ctx->np, ctx->p.Nx, ctx->p.Ny, ctx->sort_offset, ctx->sort_count, ctx->ions[a], ctx->ions[b]);
+      ctx->np, k.tg, ctx->sort_offset, ctx->sort_count, ctx->ions[a], ctx->ions[b]);
   ECS_LAUNCHED(ctx);
   ctx->cur = b;
   ctx->steps_since_sort = 0;
+  ctx->tiles_valid = true;
   return ECS_OK;
 }
 
@@ -1296,9 +1462,10 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
 // Full counting sort (count pass included), used after an upload.
 int ecs_part_sort(EcsCtx *ctx) {
   if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0) return ECS_OK;
-  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->ncell * sizeof(int32_t), ctx->stream));
-  k_sort_count<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, ctx->p.Nx, ctx->p.Ny,
-                                                                        ctx->ions[ctx->cur], ctx->sort_count);
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
+  const PartK k = make_k(ctx, 0.0);
+  k_sort_count<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, k.tg, ctx->ions[ctx->cur],
+                                                                        ctx->sort_count);
   ECS_LAUNCHED(ctx);
   return sort_counted(ctx);
 }
