@@ -613,6 +613,12 @@ __device__ __forceinline__ Ion load_ion(const float4 *ions, int64_t ip) {
   const float4 a = __ldcs(ions + 2 * ip), b = __ldcs(ions + 2 * ip + 1);
   return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z};
 }
+// The same through the read-only cache: consecutive ions of one lane share
+// cache lines (each record is read before it is written, by the same thread).
+__device__ __forceinline__ Ion load_ion_ro(const float4 *ions, int64_t ip) {
+  const float4 a = __ldg(ions + 2 * ip), b = __ldg(ions + 2 * ip + 1);
+  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z};
+}
 __device__ __forceinline__ void store_ion(float4 *ions, int64_t ip, const Ion &q) {
   __stcs(ions + 2 * ip, make_float4(__int_as_float(q.c), q.ox, q.oy, q.oz));
   __stcs(ions + 2 * ip + 1, make_float4(q.vx, q.vy, q.vz, 0.f));
@@ -637,19 +643,13 @@ __device__ __forceinline__ void count_cells(int32_t *__restrict__ count, int key
   if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
 }
 
-__device__ __forceinline__ void gather32(const float4 *__restrict__ E, const PartK &k, int i,
-                                         int j, int kk, float wx, float wy, float wz, float f[3]) {
-  const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
-  const int base = kk * sxy + j * sx + i;
-  float4 D[8];
-  D[0] = __ldg(&E[base]);
-  D[1] = __ldg(&E[base + 1]);
-  D[2] = __ldg(&E[base + sx]);
-  D[3] = __ldg(&E[base + sx + 1]);
-  D[4] = __ldg(&E[base + sxy]);
-  D[5] = __ldg(&E[base + sxy + 1]);
-  D[6] = __ldg(&E[base + sxy + sx]);
-  D[7] = __ldg(&E[base + sxy + sx + 1]);
+// Corner b (x: bit 0, y: bit 1, z: bit 2) of the cell whose low corner is
+// at `base` of a node array with row stride sx and plane stride sxy.
+__device__ __forceinline__ int corner_at(int base, int sx, int sxy, int b) {
+  return base + (b & 1) + ((b >> 1) & 1) * sx + (b >> 2) * sxy;
+}
+// Trilinear interpolation of the 8 corner values D at offset (wx, wy, wz).
+__device__ __forceinline__ void interp8(const float4 (&D)[8], float wx, float wy, float wz, float f[3]) {
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     float v[8];
@@ -663,6 +663,14 @@ __device__ __forceinline__ void gather32(const float4 *__restrict__ E, const Par
     float c1 = a01 + wx * (a11 - a01);
     f[c] = c0 + wz * (c1 - c0);
   }
+}
+__device__ __forceinline__ void gather32(const float4 *__restrict__ E, const PartK &k, int i, int j, int kk,
+                                         float wx, float wy, float wz, float f[3]) {
+  const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1), base = kk * sxy + j * sx + i;
+  float4 D[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) D[b] = __ldg(&E[corner_at(base, sx, sxy, b)]);
+  interp8(D, wx, wy, wz, f);
 }
 
 // Advance an in-cell offset by du (cell units); returns the cell shift.
@@ -707,6 +715,14 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
   state_hash(w, 7, h0, h1);
 }
 
+constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
+constexpr int kWNodes = kWX * kWY * kWZ;
+constexpr int kCX = ECS_TILE_X + 2, kCY = ECS_TILE_Y + 2, kCZ = ECS_TILE_Z + 2;  // window cells per axis
+constexpr int kWCells = kCX * kCY * kCZ;
+// |H| <= 2^19 and |rint(r)| <= 2^18, so 4000 contributions to one word stay
+// below 2^31
+constexpr int kWindowMax = 4000;
+
 // Push (src/velocities.c:281-371), collisions (src/collisions.c:9-167) and
 // move + boundary conditions (src/positions.c:436-472) of one ion, in the
 // pass's mode bits.  Returns the ion in cell (i, j, kk) with offsets o*.
@@ -714,11 +730,23 @@ struct IonState {
   int i, j, kk;
   float ox, oy, oz, vx, vy, vz;
 };
+// Ew (nullptr: none) is a window of the difference numerators in shared
+// memory, kWX x kWY x kWZ nodes from node (wx0, wy0, wz0).
 __device__ __forceinline__ void ion_update(const PartK &k, int mode, const float4 *__restrict__ E, EcsDevStatus *st,
-                                           IonState &q, unsigned int &nacc, unsigned int &nref) {
+                                           IonState &q, unsigned int &nacc, unsigned int &nref,
+                                           const float4 *Ew = nullptr, int wx0 = 0, int wy0 = 0, int wz0 = 0) {
   if (mode & 1) {
     float f[3];
-    gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
+    const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
+    if (Ew && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
+      const int base = (lk * kWY + lj) * kWX + li;
+      float4 D[8];
+#pragma unroll
+      for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kWX, kWX * kWY, b)];
+      interp8(D, q.ox, q.oy, q.oz, f);
+    } else {
+      gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
+    }
     float vxm = q.vx + k.escf[0] * f[0];
     float vym = q.vy + k.escf[1] * f[1];
     float vzm = q.vz + k.escf[2] * f[2];
@@ -801,19 +829,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
 // accumulators.  The cells of the moved ions are counted the same way when a
 // sort follows.  All sums are exact integers, so the moments equal those of
 // k_particles32 bit for bit.
-constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
-constexpr int kWNodes = kWX * kWY * kWZ;
-constexpr int kCX = ECS_TILE_X + 2, kCY = ECS_TILE_Y + 2, kCZ = ECS_TILE_Z + 2;  // window cells per axis
-constexpr int kWCells = kCX * kCY * kCZ;
-// |H| <= 2^19 and |rint(r)| <= 2^18, so 4000 contributions to one word stay
-// below 2^31
-constexpr int kWindowMax = 4000;
 
 __global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
                                                      int32_t *__restrict__ count, EcsDevStatus *st) {
   __shared__ int win[4][2][kWNodes];  // [field][H, rint(r)][node]
   __shared__ int wcnt[kWCells];
+  __shared__ float4 ewin[kWNodes];    // difference numerators of the window's nodes
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = k.tg.ntx * k.tg.nty * k.tg.ntz;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -821,21 +843,31 @@ __global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *i
     // window origin: one cell below the tile on every axis
     const int wx0 = tx * ECS_TILE_X - 1, wy0 = ty * ECS_TILE_Y - 1, wz0 = tz * ECS_TILE_Z - 1;
     const int a = key_off[t * ECS_TILE_CELLS], b = key_off[(t + 1) * ECS_TILE_CELLS];
+    if (a == b) continue;
+    if (mode & 1) {  // window nodes outside the extended grid are never read
+      const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
+      for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
+        const int gx = wx0 + e % kWX, gy = wy0 + (e / kWX) % kWY, gz = wz0 + e / (kWX * kWY);
+        const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
+        ewin[e] = in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
     for (int ca = a; ca < b; ca += kWindowMax) {
       const int L = min(kWindowMax, b - ca);
-      const int seg = (L + 31) >> 5;
+      const int seg = (L + 31) >> 5;               // lane segment
+      const int sub = (seg + kBlock / 32 - 1) / (kBlock / 32);  // a warp's run inside each segment
       if (mode & 8)
         for (int e = threadIdx.x; e < 8 * kWNodes; e += blockDim.x) (&win[0][0][0])[e] = 0;
       if (count)
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
       __syncthreads();
-      for (int m = warp; m < seg; m += kBlock / 32) {  // warp-uniform trip count
-        const int qi = lane * seg + m;
-        const bool active = qi < L;
+      for (int m = 0; m < sub; m++) {  // warp-uniform trip count
+        const int si = warp * sub + m, qi = lane * seg + si;
+        const bool active = si < seg && qi < L;
         const int64_t ip = (int64_t)ca + qi;
-        IonState q = ion_state(active ? load_ion(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
+        IonState q = ion_state(active ? load_ion_ro(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
         unsigned int nacc = 0, nref = 0;
-        if (active) ion_update(k, mode, E, st, q, nacc, nref);
+        if (active) ion_update(k, mode, E, st, q, nacc, nref, ewin, wx0, wy0, wz0);
         if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
         if (active) {
           const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
