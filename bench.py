@@ -40,8 +40,12 @@ WORKLOAD = {
     "n": 128, "ppc": 64, "dt": 0.1, "drift": 1.0, "nu": 0.02, "seed": 20261205,
 }
 SORT_EVERY = 2          # cell sort cadence of the mixed path
-ALGO_BYTES_MIXED = 56   # per particle-step: (int32 cell + 3 FP32 offset + 3 FP32 v) read + written
+ALGO_BYTES_MIXED = 64   # per particle-step: one 32-byte ion record read + written
 ALGO_BYTES_FP64 = 96    # per particle-step: 6 FP64 read + written
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ion of one
+# k_tiles32 step launch, measured by ncu on the 64^3 x 64 ppc case of this
+# workload; the traffic grows with the ion count, so a launch moves this x N.
+TRAFFIC_BYTES_PER_ION = 62.0
 
 
 def options(w):
@@ -82,7 +86,9 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms, each
+    sample stamped with the host clock; summary() keeps the samples taken
+    inside the window set by mark() (the timed region)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -96,7 +102,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -106,7 +112,16 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def wait_first(self, timeout=10.0):
+        """Block until the first sample arrives (nvidia-smi start-up)."""
+        t_end = time.perf_counter() + timeout
+        while self.proc and not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -119,7 +134,11 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0, t1 = getattr(self, "window", (float("-inf"), float("inf")))
+        inside = [ln for t, ln in self.lines if t0 <= t <= t1]
+        if not inside and self.lines:  # region shorter than a sample period: nearest sample
+            inside = [min(self.lines, key=lambda x: abs(x[0] - 0.5 * (t0 + t1)))[1]]
+        for ln in inside:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -250,15 +269,18 @@ def run_ours(args, world, rank, local):
         ctx.step(dt, rtol, 400)
     stats = []
     launches0 = ctx.launches
-    barrier(world)
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        clk.wait_first()
+        barrier(world)
+        torch.cuda.synchronize()
+        t_host0 = time.perf_counter()
         e0.record(stream)
         for _ in range(args.steps):
             stats.append(ctx.step(dt, rtol, 400))
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(t_host0, time.perf_counter())
     launches = ctx.launches - launches0
     el = e0.elapsed_time(e1) * 1e-3
     el_max = max_over_ranks(el, world)
@@ -329,9 +351,11 @@ def run_ours(args, world, rank, local):
                    "solve_rtol": rtol, "sort_every": SORT_EVERY,
                    "l2": "inputs larger than L2 (7.5 GB of particles per step)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_particles32 (fused push+collide+move+deposit)",
+        "roofline": {"bound": "hbm", "kernel": "k_tiles32 (fused push+collide+move+deposit, ions by tile)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind, "traffic": TRAFFIC_BYTES_PER_ION * N,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step launch "
+                                       "on the 64^3 case, per ion, times the ions here",
                      "algorithmic_bytes_per_launch": ALGO_BYTES_MIXED * N},
         "solve_latency_ms": {"p50": 1e3 * float(np.percentile(solve_s, 50)),
                              "p99": 1e3 * float(np.percentile(solve_s, 99)),

@@ -374,45 +374,74 @@ int ecs_lhs_apply_host(EcsCtx *ctx, const double *x, double *y) {
   return ECS_OK;
 }
 
-int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stats) {
-  if (!ctx || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
+// Particle phase of a step (src/pic.c:244-252): push, collide, move + BC,
+// deposit, the cell sort when due, and the FP64 moments.
+static int step_particles(EcsCtx *ctx, double dt, EcsDevStatus *coll, int *sorted) {
   int rc = ensure_eext(ctx, ctx->eext_ready);
   if (rc) return rc;
-  int sorted = 0;
+  *sorted = 0;
   ctx->ev_particle = ctx->ev_sort = false;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
-  if ((rc = ecs_part_fused(ctx, dt, 1, &sorted))) return rc;
-  EcsDevStatus coll = *ctx->hstat;
-  if (ctx->p.mn <= 0.0) memset(&coll, 0, sizeof coll);
+  if ((rc = ecs_part_fused(ctx, dt, 1, sorted))) return rc;
+  *coll = *ctx->hstat;
+  if (ctx->p.mn <= 0.0) memset(coll, 0, sizeof *coll);
   if ((rc = ecs_grid_moments(ctx))) return rc;
-  if ((rc = read_status(ctx))) return rc;
-  if ((rc = ecs_grid_rhs(ctx))) return rc;
+  return read_status(ctx);
+}
+
+// Field phase (src/pic.c:253-258): RHS, operator, potential solve.
+static int step_field(EcsCtx *ctx, double rtol, int max_it, EcsSolveStats *st) {
+  int rc = ecs_grid_rhs(ctx);
+  if (rc) return rc;
   if ((rc = ecs_solver_setup(ctx))) return rc;
-  EcsSolveStats st;
-  memset(&st, 0, sizeof st);
-  rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, &st);
+  memset(st, 0, sizeof *st);
+  rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, st);
   ctx->eext_ready = false;
-  if (stats) {
-    stats->collisions = (int64_t)coll.collisions;
-    stats->refused = (int64_t)coll.refused;
-    stats->sorted = sorted;
-    stats->solve = st;
-    float ms = 0.f;
-    cudaStreamSynchronize(ctx->stream);
-    stats->particle_seconds = (ctx->ev_particle && cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ? ms * 1e-3 : 0.0;
-    ms = 0.f;
-    stats->sort_seconds = (ctx->ev_sort && cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]) == cudaSuccess) ? ms * 1e-3 : 0.0;
-  }
   return rc;
 }
 
+static void step_stats(EcsCtx *ctx, const EcsDevStatus &coll, int sorted, const EcsSolveStats &st,
+                       EcsStepStats *stats) {
+  if (!stats) return;
+  stats->collisions = (int64_t)coll.collisions;
+  stats->refused = (int64_t)coll.refused;
+  stats->sorted = sorted;
+  stats->solve = st;
+  float ms = 0.f;
+  cudaStreamSynchronize(ctx->stream);
+  stats->particle_seconds = (ctx->ev_particle && cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ? ms * 1e-3 : 0.0;
+  ms = 0.f;
+  stats->sort_seconds = (ctx->ev_sort && cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]) == cudaSuccess) ? ms * 1e-3 : 0.0;
+}
+
+int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stats) {
+  if (!ctx || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
+  EcsDevStatus coll;
+  int sorted = 0;
+  int rc = step_particles(ctx, dt, &coll, &sorted);
+  if (rc) return rc;
+  EcsSolveStats st;
+  rc = step_field(ctx, rtol, max_it, &st);
+  step_stats(ctx, coll, sorted, st, stats);
+  return rc;
+}
+
+// The ions come from and go back to the host arrays; their download runs on
+// side streams while the potential is solved.
 int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, double rtol, int max_it,
                   double *moments_out, double *phi_out, EcsStepStats *stats) {
-  if (!ctx || !pos || !vel) return ECS_ERR_INVALID;
+  if (!ctx || !pos || !vel || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
   int rc = ecs_part_upload(ctx, pos, vel, np);
   if (rc) return rc;
-  if ((rc = ecs_step(ctx, dt, rtol, max_it, stats))) return rc;
-  if ((rc = ecs_part_download(ctx, pos, vel))) return rc;
+  EcsDevStatus coll;
+  int sorted = 0;
+  if ((rc = step_particles(ctx, dt, &coll, &sorted))) return rc;
+  if ((rc = ecs_part_download_async(ctx, pos, vel))) return rc;
+  EcsSolveStats st;
+  const int rc_field = step_field(ctx, rtol, max_it, &st);
+  if ((rc = ecs_part_xfer_wait(ctx))) return rc;
+  if (rc_field) return rc_field;
+  step_stats(ctx, coll, sorted, st, stats);
   if (moments_out && (rc = moments_to_host(ctx, moments_out))) return rc;
   if (phi_out) {
     ECS_CUDA(ctx, cudaMemcpyAsync(phi_out, ctx->phi, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

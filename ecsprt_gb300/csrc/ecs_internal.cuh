@@ -153,6 +153,14 @@ struct EcsCtx {
   // events around the particle kernel [0,1] and the sort [2,3] of a step
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   bool ev_particle = false, ev_sort = false;
+
+  // Host transfers of the ions: two device staging buffers, conversion
+  // kernels on xs[0], copies on xs[1] (created on first use).
+  cudaStream_t xs[2] = {nullptr, nullptr};
+  cudaEvent_t xev_copy[2] = {nullptr, nullptr}, xev_kern[2] = {nullptr, nullptr};
+  cudaEvent_t xev_ready = nullptr;  // the ions are ready for a download
+  double *stage[2] = {nullptr, nullptr};
+  int64_t stage_n = 0;              // ions per staging buffer
 };
 
 // ---- error helpers -------------------------------------------------------
@@ -226,6 +234,10 @@ int ecs_particles_alloc(EcsCtx *ctx);
 int ecs_particles_free(EcsCtx *ctx);
 int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
 int ecs_part_download(EcsCtx *ctx, double *pos, double *vel);
+// Enqueue the download after ctx->stream's current work; ecs_part_xfer_wait
+// waits for it.
+int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel);
+int ecs_part_xfer_wait(EcsCtx *ctx);
 int ecs_part_push(EcsCtx *ctx, double dt);
 int ecs_part_collide(EcsCtx *ctx, double dt);
 int ecs_part_move(EcsCtx *ctx, double dt);

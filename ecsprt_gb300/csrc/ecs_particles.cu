@@ -35,6 +35,8 @@
 // particle order in memory.
 #include <math.h>
 
+#include <algorithm>
+
 #include "ecs_internal.cuh"
 
 namespace {
@@ -717,6 +719,12 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
 
 constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
 constexpr int kWNodes = kWX * kWY * kWZ;
+// Padded strides of the deposit window: the 32 cells of a tile (one lane
+// each when the ions are sorted) map to 32 different shared-memory banks,
+// lx + 12 ly + 112 lz taking every value mod 32 once for lx, ly < 4, lz < 2.
+constexpr int kSY = 12, kSZ = 112;
+constexpr int kWPad = kSZ * kWZ;
+static_assert(kWX <= kSY && kWY * kSY <= kSZ, "window strides");
 constexpr int kCX = ECS_TILE_X + 2, kCY = ECS_TILE_Y + 2, kCZ = ECS_TILE_Z + 2;  // window cells per axis
 constexpr int kWCells = kCX * kCY * kCZ;
 // |H| <= 2^19 and |rint(r)| <= 2^18, so 4000 contributions to one word stay
@@ -830,10 +838,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
 // sort follows.  All sums are exact integers, so the moments equal those of
 // k_particles32 bit for bit.
 
-__global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
+__global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
                                                      int32_t *__restrict__ count, EcsDevStatus *st) {
-  __shared__ int win[4][2][kWNodes];  // [field][H, rint(r)][node]
+  __shared__ int win[4][2][kWPad];  // [field][H, rint(r)][node, padded strides]
   __shared__ int wcnt[kWCells];
   __shared__ float4 ewin[kWNodes];    // difference numerators of the window's nodes
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -857,7 +865,7 @@ __global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *i
       const int seg = (L + 31) >> 5;               // lane segment
       const int sub = (seg + kBlock / 32 - 1) / (kBlock / 32);  // a warp's run inside each segment
       if (mode & 8)
-        for (int e = threadIdx.x; e < 8 * kWNodes; e += blockDim.x) (&win[0][0][0])[e] = 0;
+        for (int e = threadIdx.x; e < 8 * kWPad; e += blockDim.x) (&win[0][0][0])[e] = 0;
       if (count)
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
       __syncthreads();
@@ -881,12 +889,12 @@ __global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *i
             const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
             const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
             const bool inwin = li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ;
-            const int n0 = (lk * kWY + lj) * kWX + li;
-#pragma unroll
+            const int n0 = lk * kSZ + lj * kSY + li;
+#pragma unroll 1
             for (int bc = 0; bc < 8; bc++) {
               const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
               const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
-              const int nb = n0 + ((bc >> 2) * kWY + ((bc >> 1) & 1)) * kWX + (bc & 1);
+              const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
               const long long gnode = inwin ? 0 : corner_node(k, q.i, q.j, q.kk, bc);
 #pragma unroll
               for (int f = 0; f < 4; f++) {
@@ -910,9 +918,10 @@ __global__ void __launch_bounds__(kBlock) k_tiles32(PartK k, int mode, float4 *i
       if (mode & 8) {
         for (int e = threadIdx.x; e < 4 * kWNodes; e += blockDim.x) {
           const int f = e / kWNodes, nd = e - f * kWNodes;
-          const long long v = fix_join(win[f][0][nd], win[f][1][nd]);
-          if (v == 0) continue;
           const int wxn = nd % kWX, wyn = (nd / kWX) % kWY, wzn = nd / (kWX * kWY);
+          const int np_ = wzn * kSZ + wyn * kSY + wxn;
+          const long long v = fix_join(win[f][0][np_], win[f][1][np_]);
+          if (v == 0) continue;
           int gx = wx0 + wxn, gy = wy0 + wyn, gz = wz0 + wzn;
           // nodes past the last cell wrap (periodic) or are dropped (ghosts)
           if (gx < 0 || gx >= k.Nx) { if (k.bc[0]) continue; gx = gx < 0 ? gx + k.Nx : gx - k.Nx; }
@@ -1254,7 +1263,9 @@ int ecs_particles_alloc(EcsCtx *ctx) {
   return ECS_OK;
 }
 
+void ecs_part_xfer_free(EcsCtx *ctx);
 int ecs_particles_free(EcsCtx *ctx) {
+  ecs_part_xfer_free(ctx);
   void *ptrs[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ions[0], ctx->ions[1],
                   ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
   for (void *p : ptrs)
@@ -1262,61 +1273,123 @@ int ecs_particles_free(EcsCtx *ctx) {
   return ECS_OK;
 }
 
-// Host AoS FP64 -> device, in chunks through a device staging buffer.
+// ---- host transfers ------------------------------------------------------------
+// Ions move between the host's AoS FP64 arrays and the device in chunks
+// through two staging buffers, so that the copy of one chunk overlaps the
+// conversion kernel of the other.
+constexpr int64_t kStageIons = 1 << 22;
+
+static int ensure_xfer(EcsCtx *ctx) {
+  if (ctx->stage[0]) return ECS_OK;
+  for (int q = 0; q < 2; q++) {
+    ECS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->xs[q], cudaStreamNonBlocking));
+    ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_copy[q], cudaEventDisableTiming));
+    ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_kern[q], cudaEventDisableTiming));
+  }
+  ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_ready, cudaEventDisableTiming));
+  const int64_t n = std::max<int64_t>(1, std::min<int64_t>(kStageIons, ctx->cap));
+  for (int q = 0; q < 2; q++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage[q], (size_t)n * 6 * sizeof(double)));
+  ctx->stage_n = n;
+  return ECS_OK;
+}
+
+void ecs_part_xfer_free(EcsCtx *ctx) {
+  for (int q = 0; q < 2; q++) {
+    if (ctx->xs[q]) cudaStreamSynchronize(ctx->xs[q]);
+    if (ctx->stage[q]) cudaFree(ctx->stage[q]);
+    if (ctx->xev_copy[q]) cudaEventDestroy(ctx->xev_copy[q]);
+    if (ctx->xev_kern[q]) cudaEventDestroy(ctx->xev_kern[q]);
+    if (ctx->xs[q]) cudaStreamDestroy(ctx->xs[q]);
+  }
+  if (ctx->xev_ready) cudaEventDestroy(ctx->xev_ready);
+}
+
+// Host AoS FP64 -> device: copies on xs[1], conversions on ctx->stream.
 int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np) {
   if (np < 0 || np > ctx->cap) return ecs_fail(ctx, ECS_ERR_INVALID, "np %lld exceeds capacity %lld", (long long)np, (long long)ctx->cap);
-  const int64_t chunk = 1 << 22;
-  double *stage = nullptr;
-  int64_t cn = np < chunk ? (np > 0 ? np : 1) : chunk;
-  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, (size_t)cn * 6 * sizeof(double), ctx->stream));
+  int rc = ensure_xfer(ctx);
+  if (rc) return rc;
+  const int64_t chunk = ctx->stage_n;
   PartK k = make_k(ctx, 0.0);
-  for (int64_t off = 0; off < np; off += chunk) {
-    int64_t n = np - off < chunk ? np - off : chunk;
-    ECS_CUDA(ctx, cudaMemcpyAsync(stage, pos + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    ECS_CUDA(ctx, cudaMemcpyAsync(stage + 3 * n, vel + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // the previous contents of the ion buffer may still be in use
+  ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_ready, 0));
+  int64_t c = 0;
+  for (int64_t off = 0; off < np; off += chunk, c++) {
+    const int q = (int)(c & 1);
+    const int64_t n = np - off < chunk ? np - off : chunk;
+    double *st = ctx->stage[q];
+    if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));  // buffer q free
+    ECS_CUDA(ctx, cudaMemcpyAsync(st, pos + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaMemcpyAsync(st + 3 * n, vel + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
+    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_copy[q], 0));
     unsigned int g = grid_blocks(ctx, n, 8);
     if (ctx->prec == ECS_PREC_FP64) {
-      k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
+      k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, st, st + 3 * n, ctx->px + off, ctx->py + off,
                                                    ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->ions[ctx->cur] + 2 * off);
+      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, st, st + 3 * n, ctx->ions[ctx->cur] + 2 * off);
     }
     ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
   }
-  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
   ctx->np = np;
   ctx->attempt_rate = -1.0;
   ctx->tiles_valid = false;
   if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
-    int rc = ecs_part_sort(ctx);
+    rc = ecs_part_sort(ctx);
     if (rc) return rc;
+  }
+  // the host arrays may be reused once this returns
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[1]));
+  return ECS_OK;
+}
+
+// Device -> host AoS FP64: conversions on xs[0], copies on xs[1], after the
+// work enqueued on ctx->stream so far.
+int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
+  int rc = ensure_xfer(ctx);
+  if (rc) return rc;
+  const int64_t chunk = ctx->stage_n;
+  const int64_t np = ctx->np;
+  PartK k = make_k(ctx, 0.0);
+  ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
+  int64_t c = 0;
+  for (int64_t off = 0; off < np; off += chunk, c++) {
+    const int q = (int)(c & 1);
+    const int64_t n = np - off < chunk ? np - off : chunk;
+    double *st = ctx->stage[q];
+    if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_copy[q], 0));  // buffer q copied out
+    unsigned int g = grid_blocks(ctx, n, 8);
+    if (ctx->prec == ECS_PREC_FP64) {
+      k_soa_to_aos64<<<g, kBlock, 0, ctx->xs[0]>>>(n, st, st + 3 * n, ctx->px + off, ctx->py + off,
+                                                  ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
+    } else {
+      k_mixed_to_aos<<<g, kBlock, 0, ctx->xs[0]>>>(n, k, st, st + 3 * n, ctx->ions[ctx->cur] + 2 * off);
+    }
+    ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->xs[0]));
+    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));
+    if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + 3 * off, st, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
+    if (vel) ECS_CUDA(ctx, cudaMemcpyAsync(vel + 3 * off, st + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
   }
   return ECS_OK;
 }
 
-int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
-  const int64_t chunk = 1 << 22;
-  int64_t np = ctx->np;
-  double *stage = nullptr;
-  int64_t cn = np < chunk ? (np > 0 ? np : 1) : chunk;
-  ECS_CUDA(ctx, cudaMallocAsync((void **)&stage, (size_t)cn * 6 * sizeof(double), ctx->stream));
-  PartK k = make_k(ctx, 0.0);
-  for (int64_t off = 0; off < np; off += chunk) {
-    int64_t n = np - off < chunk ? np - off : chunk;
-    unsigned int g = grid_blocks(ctx, n, 8);
-    if (ctx->prec == ECS_PREC_FP64) {
-      k_soa_to_aos64<<<g, kBlock, 0, ctx->stream>>>(n, stage, stage + 3 * n, ctx->px + off, ctx->py + off,
-                                                   ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
-    } else {
-      k_mixed_to_aos<<<g, kBlock, 0, ctx->stream>>>(n, k, stage, stage + 3 * n, ctx->ions[ctx->cur] + 2 * off);
-    }
-    ECS_LAUNCHED(ctx);
-    if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + 3 * off, stage, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    if (vel) ECS_CUDA(ctx, cudaMemcpyAsync(vel + 3 * off, stage + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  ECS_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
-  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+int ecs_part_xfer_wait(EcsCtx *ctx) {
+  if (!ctx->xs[1]) return ECS_OK;
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[0]));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[1]));
   return ECS_OK;
+}
+
+int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
+  int rc = ecs_part_download_async(ctx, pos, vel);
+  if (rc) return rc;
+  return ecs_part_xfer_wait(ctx);
 }
 
 // One pass of the particle kernel over all ions.  With `count_for_sort` the
