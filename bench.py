@@ -262,6 +262,8 @@ def run_ours(args, world, rank, local):
     # ---------------- device-resident mixed path -----------------------
     ctx = E.Context(p, E.ECS_PREC_MIXED, np_capacity=N, stream=stream.cuda_stream)
     ctx.set_sort_every(SORT_EVERY)
+    if args.no_solver_graphs:
+        ctx.set_solver_graphs(False)
     ctx.upload_particles(pos, vel)
     ctx.collect()
     ctx.compute_potential(rtol=rtol, max_it=400)
@@ -381,6 +383,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=None, help="profiling only: smaller cube edge")
     ap.add_argument("--ppc", type=int, default=None, help="profiling only: ions per cell")
+    ap.add_argument("--no-solver-graphs", action="store_true",
+                    help="profiling only: launch the FGMRES steps from the host instead of as one CUDA graph "
+                         "per cycle (same kernels; ncu then lists each solver kernel)")
     args = ap.parse_args()
     if args.grid:
         WORKLOAD["n"] = args.grid
