@@ -12,7 +12,7 @@ benchmark).
 
 A step is one pass of src/pic.c:244-258: push + collide + move/BC + deposit
 + RHS + operator set-up + solve.  value = ions x steps / device time of the
-timed steps (particles resident in HBM, 7.5 GB >> L2, so no flush is needed).
+timed steps (ion records resident in HBM, 8.6 GB >> L2, so no flush is needed).
 e2e = the same metric through the host-buffer C-ABI call ecs_step_host
 (particles copied in and out of pinned host memory every step, plus the
 moments and potential out).
@@ -218,6 +218,15 @@ def barrier(world):
         dist.barrier()
 
 
+def workload_config(w, world):
+    n = w["n"]
+    return {"workload": w["name"], "grid": [n] * 3, "ions": n ** 3 * w["ppc"], "ppc": w["ppc"], "dt": w["dt"],
+            "precision": "mixed (FP32 particles + FP32 MG-FGMRES inside FP64 refinement)",
+            "solve_rtol": 1e-8, "sort_every": SORT_EVERY,
+            "l2": "inputs larger than L2 (8.6 GB of ion records per step)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -237,7 +246,8 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * (1 << 21) / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w["name"], "sample_ions": 1 << 21},
+        "config": dict(workload_config(w, 1), sample_ions=1 << 21,
+                       precision="FP64 (the reference's CPU path, restated by the oracle)"),
         "cpu_baseline": c,
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -348,11 +358,7 @@ def run_ours(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": w["name"], "grid": [w["n"]] * 3, "ions": N, "ppc": w["ppc"], "dt": dt,
-                   "precision": "mixed (FP32 particles + FP32 MG-FGMRES inside FP64 refinement)",
-                   "solve_rtol": rtol, "sort_every": SORT_EVERY,
-                   "l2": "inputs larger than L2 (7.5 GB of particles per step)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": workload_config(w, world),
         "roofline": {"bound": "hbm", "kernel": "k_tiles32 (fused push+collide+move+deposit, ions by tile)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": TRAFFIC_BYTES_PER_ION * N,
