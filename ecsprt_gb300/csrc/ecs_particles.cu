@@ -846,6 +846,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
   __shared__ float4 ewin[kWNodes];    // difference numerators of the window's nodes
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = k.tg.ntx * k.tg.nty * k.tg.ntz;
+  unsigned int nacc = 0, nref = 0;  // collision counters of this thread, flushed at the end
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int tx = t % k.tg.ntx, ty = (t / k.tg.ntx) % k.tg.nty, tz = t / (k.tg.ntx * k.tg.nty);
     // window origin: one cell below the tile on every axis
@@ -874,9 +875,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
         const bool active = si < seg && qi < L;
         const int64_t ip = (int64_t)ca + qi;
         IonState q = ion_state(active ? load_ion_ro(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
-        unsigned int nacc = 0, nref = 0;
         if (active) ion_update(k, mode, E, st, q, nacc, nref, ewin, wx0, wy0, wz0);
-        if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
         if (active) {
           const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
           if (count) {
@@ -888,22 +887,32 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
           if (mode & 8) {
             const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
             const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
-            const bool inwin = li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ;
-            const int n0 = lk * kSZ + lj * kSY + li;
+            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
+              const int n0 = lk * kSZ + lj * kSY + li;
 #pragma unroll 1
-            for (int bc = 0; bc < 8; bc++) {
-              const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
-              const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
-              const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
-              const long long gnode = inwin ? 0 : corner_node(k, q.i, q.j, q.kk, bc);
+              for (int bc = 0; bc < 8; bc++) {
+                const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
+                const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
+                const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
 #pragma unroll
-              for (int f = 0; f < 4; f++) {
-                int hi, lo;
-                (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
-                if (inwin) {
+                for (int f = 0; f < 4; f++) {
+                  int hi, lo;
+                  (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
                   atomicAdd(&win[f][0][nb], hi);
                   atomicAdd(&win[f][1][nb], lo);
-                } else if (gnode >= 0) {
+                }
+              }
+            } else {  // outside the window: straight into the global accumulators
+#pragma unroll 1
+              for (int bc = 0; bc < 8; bc++) {
+                const long long gnode = corner_node(k, q.i, q.j, q.kk, bc);
+                if (gnode < 0) continue;
+                const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
+                const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
+#pragma unroll
+                for (int f = 0; f < 4; f++) {
+                  int hi, lo;
+                  (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
                   atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + gnode],
                             (unsigned long long)fix_join(hi, lo));
                 }
@@ -945,6 +954,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
       __syncthreads();
     }
   }
+  if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
 }
 
 // ---- upload / download conversions ---------------------------------------------

@@ -82,12 +82,12 @@ struct ZlP {
   T *a, *cp, *minv, *q, *fb, *bb;  // per cell
   T *a0g, *qden;                   // per column
 };
-// At most 16 segments a column (block of 32 x 16 threads); segments of 8
-// (FP64 only), 16, 32 or 64 cells, the shortest that fits.
+// At most 16 segments a column (block of 32 x 16 threads); segments of 8,
+// 16, 32 or 64 cells, the shortest that fits.
 constexpr int kMaxSeg = 16;
 template <typename T>
 static inline int seg_len(int N) {
-  for (int S = sizeof(T) == 8 ? 8 : 16; S < 64; S *= 2)
+  for (int S = 8; S < 64; S *= 2)
     if (N <= S * kMaxSeg) return S;
   return 64;
 }
