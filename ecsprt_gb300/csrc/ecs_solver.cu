@@ -516,46 +516,46 @@ __global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restr
     for (int e = tid; e < n * n; e += bs) M[(size_t)(e / n) * w + (e % n)] += sigma;
     __syncthreads();
   }
+  // elimination with a 32 x 32 thread grid: rows by threadIdx.y, columns by
+  // threadIdx.x (the block is launched as 32 x 32)
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int c = 0; c < n; c++) {
-    // pivot: largest |M[r][c]|, r >= c
-    T best = T(-1);
-    int bi = n;
-    for (int r = c + tid; r < n; r += bs) {
-      const T a = fabs(M[(size_t)r * w + c]);
-      if (a > best) { best = a; bi = r; }
-    }
-    for (int s = 16; s >= 1; s >>= 1) {
-      const T ob = __shfl_xor_sync(ECS_FULL_MASK, best, s);
-      const int oi = __shfl_xor_sync(ECS_FULL_MASK, bi, s);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    if (lane == 0) { wv[warp] = best; wi[warp] = bi; }
-    __syncthreads();
-    if (tid == 0) {
-      T b0 = T(-1);
-      int i0 = n;
-      for (int q = 0; q < (bs >> 5); q++)
-        if (wv[q] > b0 || (wv[q] == b0 && wi[q] < i0)) { b0 = wv[q]; i0 = wi[q]; }
-      piv = i0 < n ? i0 : c;
+    // pivot: largest |M[r][c]|, r >= c, lowest row on ties (warp 0)
+    if (ty == 0) {
+      T best = T(-1);
+      int bi = n;
+      for (int r = c + tx; r < n; r += 32) {
+        const T a = fabs(M[(size_t)r * w + c]);
+        if (a > best) { best = a; bi = r; }
+      }
+      for (int s = 16; s >= 1; s >>= 1) {
+        const T ob = __shfl_xor_sync(ECS_FULL_MASK, best, s);
+        const int oi = __shfl_xor_sync(ECS_FULL_MASK, bi, s);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tx == 0) {
+        piv = bi < n ? bi : c;
+        const T pv = M[(size_t)piv * w + c];
+        sigma = pv != T(0) ? T(1) / pv : T(0);  // reused as 1 / pivot
+      }
     }
     __syncthreads();
     const int pr = piv;
     if (pr != c)
-      for (int q = tid; q < w; q += bs) {
-        const T t = M[(size_t)c * w + q];
-        M[(size_t)c * w + q] = M[(size_t)pr * w + q];
-        M[(size_t)pr * w + q] = t;
+      for (int e = threadIdx.x; e < w; e += blockDim.x) {
+        const T t = M[(size_t)c * w + e];
+        M[(size_t)c * w + e] = M[(size_t)pr * w + e];
+        M[(size_t)pr * w + e] = t;
       }
     __syncthreads();
-    const T pv = M[(size_t)c * w + c];
-    const T ip = pv != T(0) ? T(1) / pv : T(0);
+    const T ip = sigma;
+    for (int e = threadIdx.x; e < w; e += blockDim.x) M[(size_t)c * w + e] *= ip;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) fac[r] = r == c ? T(0) : M[(size_t)r * w + c];
     __syncthreads();
-    for (int q = tid; q < w; q += bs) M[(size_t)c * w + q] *= ip;
-    for (int r = tid; r < n; r += bs) fac[r] = M[(size_t)r * w + c];
-    __syncthreads();
-    for (int e = tid; e < n * w; e += bs) {
-      const int r = e / w, q = e - r * w;
-      if (r != c) M[e] -= fac[r] * M[(size_t)c * w + q];
+    for (int r = ty; r < n; r += 32) {
+      const T f = fac[r];
+      if (f != T(0))
+        for (int q = tx; q < w; q += 32) M[(size_t)r * w + q] -= f * M[(size_t)c * w + q];
     }
     __syncthreads();
   }
@@ -1416,15 +1416,21 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
   int its = 0, sweeps = 0;
   double rel = 0.0;
   bool cycle_pending = false;
+  bool zero_guess = !warm;
   if (bnorm > 0.0) {
     for (;;) {
-      k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
-      ECS_LAUNCHED(ctx);
-      if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
-      ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-      if (cycle_pending)
-        ECS_CUDA(ctx, cudaMemcpyAsync(hk, ctx->kdev, sizeof(KrylovDev), cudaMemcpyDeviceToHost, ctx->stream));
-      ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (zero_guess) {  // phi = 0: the residual is b, its norm (dots[0..1]) is known
+        ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        zero_guess = false;
+      } else {
+        k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
+        ECS_LAUNCHED(ctx);
+        if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
+        ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        if (cycle_pending)
+          ECS_CUDA(ctx, cudaMemcpyAsync(hk, ctx->kdev, sizeof(KrylovDev), cudaMemcpyDeviceToHost, ctx->stream));
+        ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      }
       if (cycle_pending) {
         if (ctx->graph_pending) {
           const SolverGraph *sg = (const SolverGraph *)ctx->graph_pending;
