@@ -889,7 +889,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
             const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
             if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
               const int n0 = lk * kSZ + lj * kSY + li;
-#pragma unroll 1
+#pragma unroll
               for (int bc = 0; bc < 8; bc++) {
                 const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
                 const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
@@ -924,20 +924,21 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
       }
       __syncthreads();
       // window -> global accumulators
-      if (mode & 8) {
-        for (int e = threadIdx.x; e < 4 * kWNodes; e += blockDim.x) {
-          const int f = e / kWNodes, nd = e - f * kWNodes;
+      if (mode & 8) {  // one node per thread, its four fields
+        for (int nd = threadIdx.x; nd < kWNodes; nd += blockDim.x) {
           const int wxn = nd % kWX, wyn = (nd / kWX) % kWY, wzn = nd / (kWX * kWY);
           const int np_ = wzn * kSZ + wyn * kSY + wxn;
-          const long long v = fix_join(win[f][0][np_], win[f][1][np_]);
-          if (v == 0) continue;
           int gx = wx0 + wxn, gy = wy0 + wyn, gz = wz0 + wzn;
           // nodes past the last cell wrap (periodic) or are dropped (ghosts)
           if (gx < 0 || gx >= k.Nx) { if (k.bc[0]) continue; gx = gx < 0 ? gx + k.Nx : gx - k.Nx; }
           if (gy < 0 || gy >= k.Ny) { if (k.bc[1]) continue; gy = gy < 0 ? gy + k.Ny : gy - k.Ny; }
           if (gz < 0 || gz >= k.Nz) { if (k.bc[2]) continue; gz = gz < 0 ? gz + k.Nz : gz - k.Nz; }
-          atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + ((size_t)gz * k.Ny + gy) * k.Nx + gx],
-                    (unsigned long long)v);
+          unsigned long long *dst = (unsigned long long *)acc + ((size_t)gz * k.Ny + gy) * k.Nx + gx;
+#pragma unroll
+          for (int f = 0; f < 4; f++) {
+            const long long v = fix_join(win[f][0][np_], win[f][1][np_]);
+            if (v != 0) atomicAdd(dst + (size_t)f * k.ncell, (unsigned long long)v);
+          }
         }
       }
       if (count) {
