@@ -67,12 +67,16 @@ struct Multigrid {
   T *cwork = nullptr;  // Gauss-Jordan work matrix [n][2n]
 };
 
-// Instantiated graph of one FGMRES cycle (per arithmetic type).
+// Instantiated graph of a whole potential solve (refinement sweeps, each an
+// FGMRES cycle), built for one (rtol, max_it, warm start).
 struct SolverGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  int64_t kernels_fixed = 0;  // kernels before and after the Arnoldi loop
-  int64_t kernels_step = 0;   // kernels of one Arnoldi step
+  double rtol = 0.0;
+  int max_it = 0, warm = -1;
+  // kernels of: the head (up to the first check), one sweep outside its
+  // Arnoldi steps, one Arnoldi step
+  int64_t k_head = 0, k_sweep = 0, k_step = 0;
 };
 
 struct EcsCtx {
@@ -131,9 +135,11 @@ struct EcsCtx {
   void *kdev = nullptr;             // device FGMRES control block
   void *kdev_host = nullptr;        // pinned copy read back after a cycle
   void *kctl_host = nullptr;        // pinned staging of the cycle's tolerance and step limit
-  SolverGraph graph64, graph32;     // one FGMRES cycle as a CUDA graph
-  int use_graphs = 1;               // 0: the host launches the Arnoldi steps one by one
-  void *graph_pending = nullptr;    // SolverGraph launched, kernels not yet counted
+  SolverGraph sgraph;               // the whole solve as one CUDA graph
+  int use_graphs = 1;               // 0: the host drives the refinement and the Arnoldi steps
+  void *rdev = nullptr;             // device state of the refinement loop
+  void *rdev_host = nullptr;        // pinned copy
+  cudaStream_t capst[3] = {nullptr, nullptr, nullptr};  // capture streams (graph nesting levels)
   cudaEvent_t ev_solve[2] = {nullptr, nullptr};
   bool lhs_ready = false;
   bool moments_ready = false;

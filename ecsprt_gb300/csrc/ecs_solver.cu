@@ -477,7 +477,6 @@ __global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restr
   T *M = Mg ? Mg : reinterpret_cast<T *>(inv_smem);  // work matrix in shared memory when it fits
   __shared__ T fac[kDirectMax];
   __shared__ T wv[32];
-  __shared__ int wi[32];
   __shared__ int piv;
   __shared__ T sigma;
   const GridG &g = o.g;
@@ -822,8 +821,11 @@ __global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict_
   V[(size_t)(jj + 1) * o.g.n + lin3(o.g, i, j, k)] = apply_row(n, x, o, i, j, k);
 }
 
-// Start of a cycle: beta = ||b|| from the partials, first basis vector.
-__global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, const double *__restrict__ partial) {
+// Start of a cycle: beta = ||b|| from the ||b||^2 partials.  In a graph it
+// also (re)arms the Arnoldi loop's condition, which keeps its last value
+// between cycles of one launch.
+__global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, const double *__restrict__ partial,
+                                                     cudaGraphConditionalHandle cond, int use_graph) {
   __shared__ double sh[32];
   double t = 0.0;
   for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
@@ -843,6 +845,7 @@ __global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, cons
   kd->inv_scale = beta > 0.0 ? 1.0 / beta : 0.0;
   for (int q = 0; q <= kKrylovMax; q++) kd->g[q] = 0.0;
   kd->g[0] = beta;
+  if (use_graph) cudaGraphSetConditional(cond, kd->done ? 0u : 1u);
 }
 
 // partial[block] = sum of b*b over the block (FP64 accumulation of T runs)
@@ -1128,7 +1131,7 @@ float *cycle_x<float>(EcsCtx *ctx) { return ctx->kz32 + (size_t)(ctx->krylov_m +
 
 // Kernels before the Arnoldi loop: ||b||, V_0, x = 0.
 template <typename T>
-int cycle_pre(EcsCtx *ctx) {
+int cycle_pre(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
   const size_t n = ctx->ncell;
   KrylovDev *kd = (KrylovDev *)ctx->kdev;
   Multigrid<T> &mg = mg_of<T>(ctx);
@@ -1136,7 +1139,7 @@ int cycle_pre(EcsCtx *ctx) {
   const unsigned nb = dot_blocks(ctx, n);
   k_sq_partial<T><<<nb, kB, 0, ctx->stream>>>(n, b, ctx->red);
   ECS_LAUNCHED(ctx);
-  k_cycle_init<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red);
+  k_cycle_init<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red, cond, use_graph);
   ECS_LAUNCHED(ctx);
   k_cycle_start<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, b, basis_v<T>(ctx), mg.lv[0].b, cycle_x<T>(ctx), kd);
   ECS_LAUNCHED(ctx);
@@ -1194,67 +1197,10 @@ int cycle_post(EcsCtx *ctx) {
   return ECS_OK;
 }
 
-template <typename T>
-SolverGraph &graph_of(EcsCtx *ctx) {
-  return sizeof(T) == 8 ? ctx->graph64 : ctx->graph32;
-}
-
-// Capture one cycle as a graph: pre -> WHILE(step) -> post.
-template <typename T>
-int build_graph(EcsCtx *ctx) {
-  SolverGraph &sg = graph_of<T>(ctx);
-  if (sg.exec) return ECS_OK;
-  cudaGraph_t g = nullptr, pre = nullptr, post = nullptr;
-  ECS_CUDA(ctx, cudaGraphCreate(&g, 0));
-  sg.graph = g;
-  cudaGraphConditionalHandle cond;
-  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
-  int rc;
-  // Kernels captured per section (the launch counter counts kernels that
-  // run, so it is restored after capture and advanced per graph launch).
-  const int64_t launches0 = ctx->launches;
-  // pre and post as captured child graphs
-  ECS_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  rc = cycle_pre<T>(ctx);
-  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &pre);
-  if (rc) return rc;
-  ECS_CUDA(ctx, ce);
-  const int64_t launches1 = ctx->launches;
-  ECS_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  rc = cycle_post<T>(ctx);
-  ce = cudaStreamEndCapture(ctx->stream, &post);
-  if (rc) return rc;
-  ECS_CUDA(ctx, ce);
-  const int64_t launches2 = ctx->launches;
-  cudaGraphNode_t npre, nloop, npost;
-  ECS_CUDA(ctx, cudaGraphAddChildGraphNode(&npre, g, nullptr, 0, pre));
-  // zero-initialised storage (the parameter union has no default constructor)
-  alignas(cudaGraphNodeParams) unsigned char cp_store[sizeof(cudaGraphNodeParams)];
-  memset(cp_store, 0, sizeof cp_store);
-  cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_store);
-  cp->type = cudaGraphNodeTypeConditional;
-  cp->conditional.handle = cond;
-  cp->conditional.type = cudaGraphCondTypeWhile;
-  cp->conditional.size = 1;
-  ECS_CUDA(ctx, cudaGraphAddNode(&nloop, g, &npre, nullptr, 1, cp));
-  cudaGraph_t body = cp->conditional.phGraph_out[0];
-  ECS_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  rc = cycle_step<T>(ctx, cond, 1);
-  ce = cudaStreamEndCapture(ctx->stream, &body);
-  if (rc) return rc;
-  ECS_CUDA(ctx, ce);
-  sg.kernels_fixed = (launches1 - launches0) + (launches2 - launches1);
-  sg.kernels_step = ctx->launches - launches2;
-  ctx->launches = launches0;
-  ECS_CUDA(ctx, cudaGraphAddChildGraphNode(&npost, g, &nloop, 1, post));
-  cudaGraphDestroy(pre);
-  cudaGraphDestroy(post);
-  ECS_CUDA(ctx, cudaGraphInstantiate(&sg.exec, g, 0));
-  return ECS_OK;
-}
-
 // One FGMRES cycle on (cycle_b, cycle_x) with tolerance tol (relative to
-// ||b||) and at most maxit steps; the control block ends up in ctx->kdev_host.
+// ||b||) and at most maxit steps, launched from the host step by step (the
+// host reads the stop flag after each step); the control block ends up in
+// ctx->kdev_host.
 template <typename T>
 int fgmres_cycle(EcsCtx *ctx, double tol, int maxit) {
   KrylovDev *kd = (KrylovDev *)ctx->kdev;
@@ -1263,23 +1209,16 @@ int fgmres_cycle(EcsCtx *ctx, double tol, int maxit) {
   ctl->maxit = std::min(std::min(ctx->krylov_m, kKrylovMax), std::max(maxit, 1));
   ECS_CUDA(ctx, cudaMemcpyAsync(kd, ctl, offsetof(KrylovDev, j), cudaMemcpyHostToDevice, ctx->stream));
   int rc;
-  if (ctx->use_graphs) {
-    if ((rc = build_graph<T>(ctx))) return rc;
-    ECS_CUDA(ctx, cudaGraphLaunch(graph_of<T>(ctx).exec, ctx->stream));
-    ctx->graph_pending = &graph_of<T>(ctx);  // its kernels are counted once nits is known
-  } else {
-    if ((rc = cycle_pre<T>(ctx))) return rc;
-    KrylovDev *hk = (KrylovDev *)ctx->kdev_host;
-    for (int s = 0; s < kKrylovMax; s++) {
-      ECS_CUDA(ctx, cudaMemcpyAsync(&hk->done, &kd->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-      ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      if (hk->done) break;
-      cudaGraphConditionalHandle none = 0;
-      if ((rc = cycle_step<T>(ctx, none, 0))) return rc;
-    }
-    if ((rc = cycle_post<T>(ctx))) return rc;
+  cudaGraphConditionalHandle none = 0;
+  if ((rc = cycle_pre<T>(ctx, none, 0))) return rc;
+  KrylovDev *hk = (KrylovDev *)ctx->kdev_host;
+  for (int s = 0; s < kKrylovMax; s++) {
+    ECS_CUDA(ctx, cudaMemcpyAsync(&hk->done, &kd->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hk->done) break;
+    if ((rc = cycle_step<T>(ctx, none, 0))) return rc;
   }
-  return ECS_OK;
+  return cycle_post<T>(ctx);
 }
 
 // ||v||_2 of an FP64 vector into dst[0] on the device.
@@ -1320,6 +1259,66 @@ int project_mean(EcsCtx *ctx, T *v) {
   return ECS_OK;
 }
 
+// ---- the whole solve on the device ------------------------------------------
+// Device state of the iterative-refinement loop.
+struct RefineDev {
+  double bnorm, rel;
+  int its, sweeps;
+  int done;  // converged, out of iterations, stalled or non-finite
+  int nonfinite;
+};
+
+__global__ void k_solve_init(RefineDev *rd, const double *__restrict__ dots) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  rd->bnorm = dots[0];
+  rd->rel = 0.0;
+  rd->its = 0;
+  rd->sweeps = 0;
+  rd->done = !(dots[0] > 0.0);
+  rd->nonfinite = 0;
+}
+
+// Refinement sweeps in one solve: each sweep runs at least one FGMRES step
+// (or ends the solve), so max_it bounds them; this caps the loop regardless.
+constexpr int kMaxSweeps = 64;
+
+// Relative residual of the current sweep (norm in dots[0]); decides whether
+// another correction follows (condition `cond` of the sweep loop) and sets
+// the FGMRES tolerance and step limit of that correction.
+__global__ void k_refine_check(RefineDev *rd, KrylovDev *kd, const double *__restrict__ dots, double rtol,
+                               int max_it, double tol_floor, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (rd->bnorm > 0.0) {
+    const double rel = dots[0] / rd->bnorm;
+    rd->rel = rel;
+    if (!isfinite(rel)) rd->nonfinite = 1;
+  }
+  const bool stop = rd->done || rd->nonfinite || rd->rel <= rtol || rd->its >= max_it || rd->sweeps >= kMaxSweeps;
+  if (stop) {
+    rd->done = 1;
+  } else {
+    const double tol = fmax(fmax(0.5 * rtol / rd->rel, 1e-14), tol_floor);
+    kd->tol_rel = tol;
+    kd->maxit = min(kKrylovMax, max(max_it - rd->its, 1));
+  }
+  cudaGraphSetConditional(cond, stop ? 0u : 1u);
+}
+
+__global__ void k_refine_update(RefineDev *rd, const KrylovDev *__restrict__ kd) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  rd->its += kd->nits;
+  rd->sweeps += 1;
+  if (kd->nits == 0) rd->done = 1;
+}
+
+// x64 += scale[0] * e (scale nullptr: 1)
+template <typename T>
+__global__ void k_axpy64_dev(size_t n, const double *__restrict__ scale, const T *__restrict__ e, double *__restrict__ x) {
+  const double a = scale ? scale[0] : 1.0;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    x[q] += a * (double)e[q];
+}
+
 // Mixed-precision residual: r64 = b64 - A64(n64) x64.
 __global__ void k_residual64(OpK o, const double *__restrict__ n, const double *__restrict__ x,
                              const double *__restrict__ b, double *__restrict__ r) {
@@ -1346,8 +1345,187 @@ void free_mg(Multigrid<T> &mg) {
 void free_graph(SolverGraph &sg) {
   if (sg.exec) cudaGraphExecDestroy(sg.exec);
   if (sg.graph) cudaGraphDestroy(sg.graph);
-  sg.exec = nullptr;
-  sg.graph = nullptr;
+  sg = SolverGraph();
+}
+
+// ---- graph construction ----------------------------------------------------------
+// Conditional node appended to the graph being captured on stream s (after
+// its current dependencies); the node's body graph is returned, to be
+// captured on another stream.
+int capture_conditional(EcsCtx *ctx, cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                        cudaGraph_t *body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t nd = 0;
+  ECS_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, &edges, &nd));
+  // zero-initialised storage (the parameter union has no default constructor)
+  alignas(cudaGraphNodeParams) unsigned char cp_store[sizeof(cudaGraphNodeParams)];
+  memset(cp_store, 0, sizeof cp_store);
+  cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_store);
+  cp->type = cudaGraphNodeTypeConditional;
+  cp->conditional.handle = h;
+  cp->conditional.type = type;
+  cp->conditional.size = 1;
+  cudaGraphNode_t node;
+  ECS_CUDA(ctx, cudaGraphAddNode(&node, g, deps, edges, nd, cp));
+  ECS_CUDA(ctx, cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  *body = cp->conditional.phGraph_out[0];
+  return ECS_OK;
+}
+// The graph being captured on stream s.
+int capture_graph(EcsCtx *ctx, cudaStream_t s, cudaGraph_t *g) {
+  cudaStreamCaptureStatus cs;
+  ECS_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, g, nullptr, nullptr, nullptr));
+  return ECS_OK;
+}
+
+template <typename T>
+int refine_decide(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
+  const double tol_floor = sizeof(T) == 4 ? 2e-6 : 0.0;
+  k_refine_check<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, (KrylovDev *)ctx->kdev, ctx->dots, rtol, max_it,
+                                            tol_floor, h);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// Residual of the current phi, its norm and the check that sets the sweep
+// loop's condition h (on ctx->stream).
+template <typename T>
+int refine_check(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
+  const EcsParams &p = ctx->p;
+  const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
+  k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
+  ECS_LAUNCHED(ctx);
+  int rc = norm64_dev(ctx, ctx->r64, ctx->dots);
+  if (rc) return rc;
+  return refine_decide<T>(ctx, rtol, max_it, h);
+}
+
+// The correction of one sweep: the FGMRES cycle (the Arnoldi loop as a WHILE
+// node captured on capture stream `lvl`), phi update, mean projection.
+template <typename T>
+int refine_correct(EcsCtx *ctx, int lvl) {
+  const size_t n = ctx->ncell;
+  int rc;
+  if (sizeof(T) == 4) {  // the normalised FP64 residual to FP32
+    k_scale_to<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, ctx->r64, ctx->dots + 1, (float *)cycle_b<T>(ctx));
+    ECS_LAUNCHED(ctx);
+  }
+  cudaGraph_t g = nullptr, body = nullptr;
+  if ((rc = capture_graph(ctx, ctx->stream, &g))) return rc;
+  cudaGraphConditionalHandle hw;
+  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&hw, g, 0, 0));
+  if ((rc = cycle_pre<T>(ctx, hw, 1))) return rc;
+  if ((rc = capture_conditional(ctx, ctx->stream, hw, cudaGraphCondTypeWhile, &body))) return rc;
+  cudaStream_t outer = ctx->stream;
+  ctx->stream = ctx->capst[lvl];
+  ECS_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const int64_t l0 = ctx->launches;
+  rc = cycle_step<T>(ctx, hw, 1);
+  ctx->sgraph.k_step = ctx->launches - l0;
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+  ctx->stream = outer;
+  if (rc) return rc;
+  ECS_CUDA(ctx, ce);
+  if ((rc = cycle_post<T>(ctx))) return rc;
+  k_axpy64_dev<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, sizeof(T) == 4 ? ctx->dots : nullptr,
+                                                             cycle_x<T>(ctx), ctx->phi);
+  ECS_LAUNCHED(ctx);
+  if ((rc = project_mean<double>(ctx, ctx->phi))) return rc;
+  k_refine_update<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, (const KrylovDev *)ctx->kdev);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// One solve as one graph:
+//   [phi = 0, r = b | r = b - A phi]  ||r||  init  check
+//   WHILE( scale  cycle(WHILE Arnoldi)  phi += e  update  residual  norm  check )
+// The checks set the sweep loop's condition; everything stays on the device.
+template <typename T>
+int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm) {
+  SolverGraph &sg = ctx->sgraph;
+  if (sg.exec && sg.rtol == rtol && sg.max_it == max_it && sg.warm == warm) return ECS_OK;
+  free_graph(sg);
+  for (auto &c : ctx->capst)
+    if (!c) ECS_CUDA(ctx, cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+  const size_t n = ctx->ncell;
+  const int64_t launches0 = ctx->launches;
+  cudaStream_t user = ctx->stream;
+  ctx->stream = ctx->capst[0];
+  int rc = ECS_OK;
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    ctx->stream = user;
+    return ecs_cuda_check(ctx, ce, "solve graph capture");
+  }
+  do {
+    cudaGraph_t top = nullptr;
+    if ((rc = capture_graph(ctx, ctx->stream, &top))) break;
+    cudaGraphConditionalHandle hs;
+    if ((ce = cudaGraphConditionalHandleCreate(&hs, top, 0, cudaGraphCondAssignDefault)) != cudaSuccess) {
+      rc = ecs_cuda_check(ctx, ce, "conditional handle");
+      break;
+    }
+    if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) break;  // ||b||
+    k_solve_init<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, ctx->dots);
+    ECS_LAUNCHED(ctx);
+    if (!warm) {  // phi = 0: the residual is b and its norm is known
+      if ((ce = cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream)) != cudaSuccess ||
+          (ce = cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream)) !=
+              cudaSuccess) {
+        rc = ecs_cuda_check(ctx, ce, "solve graph copies");
+        break;
+      }
+      rc = refine_decide<T>(ctx, rtol, max_it, hs);
+    } else {
+      rc = refine_check<T>(ctx, rtol, max_it, hs);
+    }
+    if (rc) break;
+    sg.k_head = ctx->launches - launches0;
+    cudaGraph_t body = nullptr;
+    if ((rc = capture_conditional(ctx, ctx->stream, hs, cudaGraphCondTypeWhile, &body))) break;
+    cudaStream_t outer = ctx->stream;
+    ctx->stream = ctx->capst[1];
+    if ((ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+      ctx->stream = outer;
+      rc = ecs_cuda_check(ctx, ce, "sweep capture");
+      break;
+    }
+    const int64_t l1 = ctx->launches;
+    rc = refine_correct<T>(ctx, 2);
+    if (!rc) rc = refine_check<T>(ctx, rtol, max_it, hs);
+    sg.k_sweep = ctx->launches - l1 - sg.k_step;
+    ce = cudaStreamEndCapture(ctx->stream, &body);
+    ctx->stream = outer;
+    if (!rc && ce != cudaSuccess) rc = ecs_cuda_check(ctx, ce, "sweep capture");
+  } while (0);
+  ce = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->stream = user;
+  ctx->launches = launches0;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  ECS_CUDA(ctx, ce);
+  sg.graph = g;
+  ECS_CUDA(ctx, cudaGraphInstantiate(&sg.exec, g, 0));
+  sg.rtol = rtol;
+  sg.max_it = max_it;
+  sg.warm = warm;
+  return ECS_OK;
+}
+
+// Launch the solve graph (asynchronous).
+int solve_graph_launch(EcsCtx *ctx, double rtol, int max_it, int warm) {
+  int rc = ctx->prec == ECS_PREC_FP64 ? build_solve_graph<double>(ctx, rtol, max_it, warm)
+                                      : build_solve_graph<float>(ctx, rtol, max_it, warm);
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaGraphLaunch(ctx->sgraph.exec, ctx->stream));
+  return ECS_OK;
 }
 
 }  // namespace
@@ -1371,6 +1549,10 @@ int ecs_solver_alloc(EcsCtx *ctx) {
     ECS_CUDA(ctx, cudaMallocHost(&ctx->kctl_host, sizeof(KrylovDev)));
     memset(ctx->kdev_host, 0, sizeof(KrylovDev));
     memset(ctx->kctl_host, 0, sizeof(KrylovDev));
+    ECS_CUDA(ctx, cudaMalloc(&ctx->rdev, sizeof(RefineDev)));
+    ECS_CUDA(ctx, cudaMemset(ctx->rdev, 0, sizeof(RefineDev)));
+    ECS_CUDA(ctx, cudaMallocHost(&ctx->rdev_host, sizeof(RefineDev)));
+    memset(ctx->rdev_host, 0, sizeof(RefineDev));
   }
   if (ctx->prec == ECS_PREC_FP64 && !ctx->kv64) {
     ECS_CUDA(ctx, cudaMalloc((void **)&ctx->kv64, (size_t)(m + 1) * n * sizeof(double)));
@@ -1407,6 +1589,28 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
   }
   ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[0], ctx->stream));
   int rc;
+  if (ctx->use_graphs) {  // the whole solve as one graph launch, one wait
+    if ((rc = solve_graph_launch(ctx, rtol, max_it, warm))) return rc;
+    RefineDev *hr = (RefineDev *)ctx->rdev_host;
+    ECS_CUDA(ctx, cudaMemcpyAsync(hr, ctx->rdev, sizeof(RefineDev), cudaMemcpyDeviceToHost, ctx->stream));
+    ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[1], ctx->stream));
+    ECS_CUDA(ctx, cudaEventSynchronize(ctx->ev_solve[1]));
+    const SolverGraph &sg = ctx->sgraph;
+    ctx->launches += sg.k_head + hr->sweeps * sg.k_sweep + (int64_t)hr->its * sg.k_step;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev_solve[0], ctx->ev_solve[1]);
+    if (st) {
+      st->iterations = hr->its;
+      st->refinements = hr->sweeps;
+      st->relres = hr->rel;
+      st->seconds = ms * 1e-3;
+    }
+    if (hr->nonfinite) return ecs_fail(ctx, ECS_ERR_NONFINITE, "non-finite residual in solve");
+    if (hr->bnorm > 0.0 && hr->rel > rtol)
+      return ecs_fail(ctx, ECS_ERR_NOT_CONVERGED, "solve stopped at relres %.3e > %.3e after %d iterations", hr->rel,
+                      rtol, hr->its);
+    return ECS_OK;
+  }
   if (!warm) ECS_CUDA(ctx, cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream));
   // ||b|| -> dots[0], 1/||b|| -> dots[1]
   if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) return rc;
@@ -1432,12 +1636,6 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
         ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
       }
       if (cycle_pending) {
-        if (ctx->graph_pending) {
-          const SolverGraph *sg = (const SolverGraph *)ctx->graph_pending;
-          // the body runs at least once (its condition starts at 1)
-          ctx->launches += sg->kernels_fixed + sg->kernels_step * std::max(hk->nits, 1);
-          ctx->graph_pending = nullptr;
-        }
         its += hk->nits;
         sweeps++;
         cycle_pending = false;
@@ -1491,16 +1689,19 @@ int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y) {
 }
 
 int ecs_solver_free(EcsCtx *ctx) {
-  free_graph(ctx->graph64);
-  free_graph(ctx->graph32);
+  free_graph(ctx->sgraph);
+  for (auto &c : ctx->capst)
+    if (c) cudaStreamDestroy(c);
   free_mg(ctx->mg64);
   free_mg(ctx->mg32);
-  void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->dots, ctx->red, ctx->kdev};
+  void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->dots, ctx->red, ctx->kdev,
+                  ctx->rdev};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_dots) cudaFreeHost(ctx->h_dots);
   if (ctx->kdev_host) cudaFreeHost(ctx->kdev_host);
   if (ctx->kctl_host) cudaFreeHost(ctx->kctl_host);
+  if (ctx->rdev_host) cudaFreeHost(ctx->rdev_host);
   for (auto &e : ctx->ev_solve)
     if (e) cudaEventDestroy(e);
   return ECS_OK;
