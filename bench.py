@@ -17,6 +17,13 @@ e2e = the same metric through the host-buffer C-ABI call ecs_step_host
 (particles copied in and out of pinned host memory every step, plus the
 moments and potential out).
 
+"serving" reports the request loop (include/ecs_serve.h) on its two
+workloads: stand-alone solves (Poisson arrivals at 200/s, grids uniform over
+{32,48,64,96,128}^3, lognormal x Fourier-mode densities, 40 GB HBM budget,
+latency p50/p99 from submit to result, plus the saturated solve rate of a
+burst), and an ensemble of 48 small simulations ({32,48,64}^3, 16 ions/cell,
+500 steps each, per-step p50/p99).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
 from __future__ import annotations
@@ -254,6 +261,135 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+SERVE_BUDGET = 40 << 30
+SERVE_INFLIGHT = 8
+
+
+def _size_percentiles(res, sizes):
+    by = {}
+    for r in res:
+        by.setdefault(sizes[r["id"]], []).append(r["latency"])
+    return {str(n): {"count": len(v), "p50_ms": 1e3 * float(np.percentile(v, 50)),
+                     "p99_ms": 1e3 * float(np.percentile(v, 99))} for n, v in sorted(by.items())}
+
+
+def run_serve_solves(E, W, nreq, rate=200.0, seed=20261206):
+    """Open-loop stand-alone solve load, then a saturated burst."""
+    rng = np.random.default_rng(seed)
+    params = {n: E.params_from_options(W.solver_options(n)) for n in W.SOLVE_SIZES}
+    pool = 4  # seeded densities per grid size, cycled (each request does the full work)
+    dens = {}
+    for n in W.SOLVE_SIZES:
+        dens[n] = []
+        for _ in range(pool):
+            d = E.pinned_empty((n,) * 3)
+            d[:] = W.solve_density(n, rng)
+            dens[n].append(d)
+    free = {n: [] for n in W.SOLVE_SIZES}
+
+    def out_buf(n):
+        return free[n].pop() if free[n] else E.pinned_empty((n,) * 3)
+
+    t_arr, sz = W.solve_requests(nreq, rate, seed + 1)
+    with E.Server(hbm_budget_bytes=SERVE_BUDGET, max_inflight=SERVE_INFLIGHT) as srv:
+        held = {}
+
+        def collect(rs, sizes_of):
+            for r in rs:
+                n, o = held.pop(r["id"])
+                free[n].append(o)
+                sizes_of[r["id"]] = n
+            return rs
+
+        warm_sizes = {}
+        for n in W.SOLVE_SIZES:  # one request per size builds the slots' graphs
+            o = out_buf(n)
+            rid = srv.submit_solve(params[n], dens[n][0], o)
+            held[rid] = (n, o)
+        collect(srv.wait_all(120), warm_sizes)
+        srv.reset_stats()
+        sizes_of = {}
+        res = []
+        t0 = time.perf_counter()
+        for q in range(nreq):
+            n = int(sz[q])
+            while True:
+                wait = t_arr[q] - (time.perf_counter() - t0)
+                if wait <= 0:
+                    break
+                res += collect(srv.poll(256, 0), sizes_of)
+                time.sleep(min(wait, 2e-4))
+            o = out_buf(n)
+            rid = srv.submit_solve(params[n], dens[n][q % pool], o)
+            held[rid] = (n, o)
+        res += collect(srv.wait_all(600), sizes_of)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        bad = [r for r in res if r["status"] != 0]
+        open_loop = {
+            "requests": nreq, "arrival_rate_per_s": rate, "wall_s": wall, "solves_per_s": len(res) / wall,
+            "p50_ms": 1e3 * st["solve_p50"], "p99_ms": 1e3 * st["solve_p99"],
+            "p99_over_p50": st["solve_p99"] / st["solve_p50"] if st["solve_p50"] > 0 else None,
+            "mean_ms": 1e3 * st["solve_mean"], "max_ms": 1e3 * st["solve_max"],
+            "max_relres": max(r["relres"] for r in res), "failed": len(bad),
+            "mean_iterations": float(np.mean([r["iterations"] for r in res])),
+            "by_size": _size_percentiles(res, sizes_of),
+            "peak_inflight": st["peak_inflight"], "peak_device_bytes": st["peak_device_bytes"],
+            "slot_hits": st["slot_hits"], "slots_created": st["slots_created"],
+            "busy_fraction": st["busy_seconds"] / wall, "gpu_launches": st["gpu_launches"],
+        }
+        # saturated: a burst of requests all queued at once
+        srv.reset_stats()
+        nb = min(2000, nreq)
+        sizes_b = {}
+        t0 = time.perf_counter()
+        for q in range(nb):
+            n = int(sz[q])
+            o = out_buf(n)
+            rid = srv.submit_solve(params[n], dens[n][q % pool], o)
+            held[rid] = (n, o)
+        rb = collect(srv.wait_all(600), sizes_b)
+        wall_b = time.perf_counter() - t0
+        stb = srv.stats()
+        saturated = {"requests": nb, "wall_s": wall_b, "solves_per_s": nb / wall_b,
+                     "failed": sum(r["status"] != 0 for r in rb), "peak_inflight": stb["peak_inflight"],
+                     "gpu_launches": stb["gpu_launches"]}
+    return {"workload": "stand-alone solves: grids uniform over {32,48,64,96,128}^3, density lognormal(0,0.1) x "
+                        "(1 + 12 Fourier modes of amplitude 0.05), FP32 MG-FGMRES + FP64 refinement to 1e-8",
+            "data": f"synthetic, {pool} seeded densities per size cycled",
+            "hbm_budget_bytes": SERVE_BUDGET, "max_inflight": SERVE_INFLIGHT,
+            "open_loop": open_loop, "saturated": saturated}
+
+
+def run_serve_sims(E, W, ninst, nsteps, seed=20261207):
+    """Ensemble of small simulations stepped concurrently."""
+    inst = W.sim_instances(ninst, seed)
+    rng = np.random.default_rng(seed + 1)
+    ppc = 16
+    reqs = []
+    for n, drift, nu in inst:
+        p = E.params_from_options(W.sim_options(n, ppc, drift, nu))
+        pos, vel = W.uniform_ions(n, ppc, drift, rng)
+        reqs.append((p, pos, vel, np.zeros(nsteps)))
+    ions = sum(r[1].shape[0] for r in reqs)
+    with E.Server(hbm_budget_bytes=SERVE_BUDGET, max_inflight=SERVE_INFLIGHT) as srv:
+        t0 = time.perf_counter()
+        for q, (p, pos, vel, secs) in enumerate(reqs):
+            srv.submit_sim(p, pos, vel, nsteps, 0.1, seed=1000 + q, step_seconds=secs)
+        res = srv.wait_all(1800)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    steps = np.concatenate([r[3] for r in reqs])
+    return {"workload": f"{ninst} simulations, grids uniform over {{32,48,64}}^3, {ppc} ions/cell, drift U[0.2,1.5], "
+                        f"collision frequency log-U[0.005,0.1], {nsteps} steps each, mixed precision",
+            "data": "synthetic, seeded", "instances": ninst, "steps_each": nsteps, "ions": ions,
+            "wall_s": wall, "particle_steps_per_s": ions * nsteps / wall,
+            "step_p50_ms": 1e3 * float(np.percentile(steps, 50)), "step_p99_ms": 1e3 * float(np.percentile(steps, 99)),
+            "failed": sum(r["status"] != 0 for r in res), "peak_inflight": st["peak_inflight"],
+            "peak_device_bytes": st["peak_device_bytes"], "gpu_launches": st["gpu_launches"],
+            "hbm_budget_bytes": SERVE_BUDGET, "max_inflight": SERVE_INFLIGHT}
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -350,6 +486,12 @@ def run_ours(args, world, rank, local):
                  "solve_ms": 1e3 * float(np.mean([s.solve.seconds for s in st64]))}
         ctx64.close()
 
+    serving = None
+    if not args.skip_serve:
+        from ecsprt_gb300 import workloads as W
+
+        serving = {"solves": run_serve_solves(E, W, args.serve_requests),
+                   "ensemble": run_serve_sims(E, W, 48, args.serve_steps)}
     if rank != 0:
         return
     cpu = cpu_baseline(w, pos, vel, phi_now) if not args.skip_cpu else None
@@ -374,6 +516,7 @@ def run_ours(args, world, rank, local):
         "plain_fp64": plain,
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
 
@@ -387,6 +530,9 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true", help="leave out the request-loop measurements")
+    ap.add_argument("--serve-requests", type=int, default=10000, help="stand-alone solve requests (Poisson, 200/s)")
+    ap.add_argument("--serve-steps", type=int, default=500, help="steps of each of the 48 served simulations")
     ap.add_argument("--grid", type=int, default=None, help="profiling only: smaller cube edge")
     ap.add_argument("--ppc", type=int, default=None, help="profiling only: ions per cell")
     ap.add_argument("--no-solver-graphs", action="store_true",

@@ -19,7 +19,14 @@ ComputeFullRHS3D            :meth:`Context.compute_rhs`
 ComputeFullLHS3D            :meth:`Context.compute_lhs`
 ComputePotential            :meth:`Context.compute_potential`
 one step of src/pic.c:238   :meth:`Context.step`
+src/solver.c:107-170        :meth:`Context.solve_density` (density in,
+  (LoadFluidQuantities +      fluxes = flux_scale * density, potential out)
+  ComputePotential)
 =========================  ==============================================
+
+:class:`Server` (include/ecs_serve.h) runs many stand-alone solves and small
+simulations at once on one GPU: resident slots admitted against an HBM
+budget, each solve one CUDA-graph launch, p50/p99 latency in its stats.
 
 Errors are raised as :class:`EcsError` carrying the library status code; the
 reference's aborts (10 refused collisions, src/collisions.c:141-148; NaN) map
@@ -31,13 +38,16 @@ import ctypes as C
 
 import numpy as np
 
+import weakref
+
 from . import _lib
-from ._lib import (ECS_PREC_FP64, ECS_PREC_MIXED, EcsParams, EcsPicApp, EcsSolveStats,
+from ._lib import (ECS_PREC_FP64, ECS_PREC_MIXED, ECS_SERVE_SIM, ECS_SERVE_SOLVE, EcsParams, EcsPicApp,
+                   EcsServeConfig, EcsServeResult, EcsServeStats, EcsSimRequest, EcsSolveRequest, EcsSolveStats,
                    EcsSolverApp, EcsStepStats)
 
 __all__ = [
-    "ECS_PREC_FP64", "ECS_PREC_MIXED", "EcsError", "EcsParams", "Context", "Options",
-    "params_from_options", "pic_app_from_options", "solver_app_from_options",
+    "ECS_PREC_FP64", "ECS_PREC_MIXED", "ECS_SERVE_SIM", "ECS_SERVE_SOLVE", "EcsError", "EcsParams", "Context",
+    "Options", "Server", "pinned_empty", "serve_request_bytes", "params_from_options", "pic_app_from_options", "solver_app_from_options",
 ]
 
 
@@ -49,6 +59,31 @@ class EcsError(RuntimeError):
 
 def _ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a, shape=None, writeable=False, name="array") -> np.ndarray:
+    """a as it is, if it is a C-contiguous float64 array (of `shape`); the
+    library reads and writes through its address."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError(f"{name} must be a C-contiguous float64 numpy array")
+    if shape is not None and a.size != int(np.prod(shape)):
+        raise ValueError(f"{name} has {a.size} values, expected {int(np.prod(shape))}")
+    if writeable and not a.flags.writeable:
+        raise ValueError(f"{name} must be writeable")
+    return a
+
+
+def pinned_empty(shape) -> np.ndarray:
+    """Uninitialised float64 array in page-locked host memory: request
+    buffers the copy engines read and write directly."""
+    n = int(np.prod(shape))
+    lib = _lib.gpu()
+    ptr = lib.ecs_host_alloc(max(n, 1) * 8)
+    if not ptr:
+        raise MemoryError(f"page-locked allocation of {n * 8} bytes failed")
+    buf = (C.c_double * max(n, 1)).from_address(ptr)
+    weakref.finalize(buf, lib.ecs_host_free, C.c_void_p(ptr))
+    return np.ctypeslib.as_array(buf)[:n].reshape(shape)
 
 
 class Options:
@@ -255,6 +290,21 @@ class Context:
         self.compute_lhs()
         return self.solve(rtol, max_it)
 
+    def solve_density(self, density: np.ndarray, flux_scale=(1.0, 1.0, 1.0), rtol: float = 1e-8,
+                      max_it: int = 200, phi_out: np.ndarray | None = None):
+        """The stand-alone solver (src/solver.c:158-163): moments from a
+        density (fluxes = flux_scale * density, src/file-io.c:51-59), RHS,
+        operator and the solve from phi = 0, as one CUDA graph.  Returns
+        (phi, stats)."""
+        d = _f64(density, self.shape, name="density")
+        phi = phi_out if phi_out is not None else np.empty(self.shape)
+        _f64(phi, self.shape, writeable=True, name="phi_out")
+        fs = (C.c_double * 3)(*[float(v) for v in flux_scale])
+        st = EcsSolveStats()
+        self._check(self._lib.ecs_solve_density(self._h, _ptr(d), C.byref(fs), float(rtol), int(max_it), _ptr(phi),
+                                                C.byref(st)))
+        return phi.reshape(self.shape), st
+
     def lhs_apply(self, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape)
         y = np.empty(self.shape)
@@ -274,3 +324,137 @@ class Context:
             _ptr(moments_out) if moments_out is not None else None,
             _ptr(phi_out) if phi_out is not None else None, C.byref(st)))
         return st
+
+
+def serve_request_bytes(params: EcsParams, precision: int = ECS_PREC_MIXED, kind: int = ECS_SERVE_SOLVE,
+                        np_: int = 0) -> int:
+    """Device bytes a served request's slot is charged (ecs_serve_request_bytes)."""
+    return int(_lib.gpu().ecs_serve_request_bytes(C.byref(params), int(precision), int(kind), int(np_)))
+
+
+def _result_dict(r: EcsServeResult) -> dict:
+    return {
+        "id": int(r.id), "kind": "solve" if r.kind == ECS_SERVE_SOLVE else "sim", "status": int(r.status),
+        "latency": r.latency, "queued": r.queued, "device_seconds": r.device_seconds,
+        "iterations": int(r.solve.iterations), "refinements": int(r.solve.refinements), "relres": r.solve.relres,
+        "steps": int(r.steps), "slot_reused": bool(r.slot_reused), "message": r.message.decode(errors="replace"),
+    }
+
+
+class Server:
+    """Request loop on one GPU (include/ecs_serve.h).
+
+    Stand-alone solves (:meth:`submit_solve`) and simulation instances
+    (:meth:`submit_sim`) are admitted first come, first served as worker
+    slots and the HBM budget allow; their device state stays resident, solve
+    slots are reused by later requests with the same parameters, and the
+    work of concurrent requests overlaps on the GPU.  The arrays passed to a
+    request are held until its result is polled; page-locked ones
+    (:func:`pinned_empty`) are copied by DMA directly.
+    """
+
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 8, precision: int = ECS_PREC_MIXED,
+                 timeout_seconds: float = 60.0):
+        self._lib = _lib.gpu()
+        cfg = EcsServeConfig(int(hbm_budget_bytes), int(max_inflight), int(precision), float(timeout_seconds))
+        h = C.c_void_p()
+        rc = self._lib.ecs_serve_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise EcsError(rc, "server create failed")
+        self._h = h
+        self.precision = precision
+        self._live = {}  # id -> arrays the request reads or writes
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ecs_serve_destroy(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def request_bytes(self, params: EcsParams, kind: int = ECS_SERVE_SOLVE, np_: int = 0) -> int:
+        return serve_request_bytes(params, self.precision, kind, np_)
+
+    def submit_solve(self, params: EcsParams, density: np.ndarray, phi_out: np.ndarray,
+                     flux_scale=(1.0, 1.0, 1.0), rtol: float = 1e-8, max_it: int = 200) -> int:
+        shape = (params.Nz, params.Ny, params.Nx)
+        _f64(density, shape, name="density")
+        _f64(phi_out, shape, writeable=True, name="phi_out")
+        req = EcsSolveRequest(density.ctypes.data, (C.c_double * 3)(*[float(v) for v in flux_scale]),
+                              float(rtol), int(max_it), phi_out.ctypes.data)
+        rid = C.c_int64()
+        rc = self._lib.ecs_serve_submit_solve(self._h, C.byref(params), C.byref(req), C.byref(rid))
+        if rc:
+            raise EcsError(rc, "solve request refused")
+        self._live[rid.value] = (params, density, phi_out)
+        return rid.value
+
+    def submit_sim(self, params: EcsParams, pos: np.ndarray, vel: np.ndarray, nsteps: int, dt: float,
+                   seed: int = 20261203, rtol: float = 1e-8, max_it: int = 200, sort_every: int = 0,
+                   step_seconds: np.ndarray | None = None, phi_out: np.ndarray | None = None,
+                   pos_out: np.ndarray | None = None, vel_out: np.ndarray | None = None) -> int:
+        n = pos.shape[0]
+        _f64(pos, (n, 3), name="pos")
+        _f64(vel, (n, 3), name="vel")
+        outs = {"step_seconds": (step_seconds, (int(nsteps),)), "phi_out": (phi_out, (params.Nz, params.Ny, params.Nx)),
+                "pos_out": (pos_out, (n, 3)), "vel_out": (vel_out, (n, 3))}
+        ptrs = {}
+        for k, (a, shp) in outs.items():
+            ptrs[k] = None
+            if a is not None:
+                _f64(a, shp, writeable=True, name=k)
+                ptrs[k] = a.ctypes.data
+        req = EcsSimRequest(pos.ctypes.data, vel.ctypes.data, n, int(seed), int(nsteps), int(sort_every),
+                            float(dt), float(rtol), int(max_it), ptrs["step_seconds"], ptrs["phi_out"],
+                            ptrs["pos_out"], ptrs["vel_out"])
+        rid = C.c_int64()
+        rc = self._lib.ecs_serve_submit_sim(self._h, C.byref(params), C.byref(req), C.byref(rid))
+        if rc:
+            raise EcsError(rc, "simulation request refused")
+        self._live[rid.value] = (params, pos, vel, step_seconds, phi_out, pos_out, vel_out)
+        return rid.value
+
+    def poll(self, max_results: int = 256, timeout_ms: int = 0) -> list:
+        """Finished requests as dicts (id, kind, status, latency, ...)."""
+        buf = (EcsServeResult * max_results)()
+        n = self._lib.ecs_serve_poll(self._h, buf, max_results, int(timeout_ms))
+        if n < 0:
+            raise EcsError(n, "poll failed")
+        out = []
+        for q in range(n):
+            self._live.pop(int(buf[q].id), None)
+            out.append(_result_dict(buf[q]))
+        return out
+
+    def wait_all(self, timeout_s: float = 600.0) -> list:
+        """Poll until every submitted request has a result."""
+        import time
+        out = []
+        t_end = time.monotonic() + timeout_s
+        while self.pending > 0:
+            if time.monotonic() > t_end:
+                raise TimeoutError(f"{self.pending} requests still pending")
+            out += self.poll(256, 100)
+        return out
+
+    @property
+    def pending(self) -> int:
+        return int(self._lib.ecs_serve_pending(self._h))
+
+    def stats(self) -> dict:
+        st = EcsServeStats()
+        rc = self._lib.ecs_serve_stats(self._h, C.byref(st))
+        if rc:
+            raise EcsError(rc, "stats failed")
+        return st.as_dict()
+
+    def reset_stats(self):
+        self._lib.ecs_serve_reset_stats(self._h)

@@ -1,4 +1,5 @@
-"""ctypes binding of libecsgpu (include/ecsgpu.h) and libecshost (include/ecs_host.h).
+"""ctypes binding of libecsgpu (include/ecsgpu.h, include/ecs_serve.h) and
+libecshost (include/ecs_host.h).
 
 The libraries are built in-tree by :mod:`ecsprt_gb300.build`.  Loading never
 falls back to another implementation: if ``libecsgpu.so`` is missing or
@@ -82,10 +83,52 @@ class EcsSolverApp(C.Structure):
     _fields_ = [("input", C.c_char * 4096), ("flux_scale", C.c_double * 3), ("view_lhs", C.c_int32)]
 
 
+ECS_SERVE_SOLVE = 0
+ECS_SERVE_SIM = 1
+
+
+class EcsServeConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_inflight", C.c_int32), ("precision", C.c_int32),
+                ("timeout_seconds", C.c_double)]
+
+
+class EcsSolveRequest(C.Structure):
+    _fields_ = [("density", C.c_void_p), ("flux_scale", C.c_double * 3), ("rtol", C.c_double),
+                ("max_it", C.c_int32), ("phi_out", C.c_void_p)]
+
+
+class EcsSimRequest(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("np", C.c_int64), ("seed", C.c_uint64),
+                ("nsteps", C.c_int32), ("sort_every", C.c_int32), ("dt", C.c_double), ("rtol", C.c_double),
+                ("max_it", C.c_int32), ("step_seconds", C.c_void_p), ("phi_out", C.c_void_p),
+                ("pos_out", C.c_void_p), ("vel_out", C.c_void_p)]
+
+
+class EcsServeResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("kind", C.c_int32), ("status", C.c_int32), ("latency", C.c_double),
+                ("queued", C.c_double), ("device_seconds", C.c_double), ("solve", EcsSolveStats),
+                ("steps", C.c_int32), ("slot_reused", C.c_int32), ("message", C.c_char * 160)]
+
+
+class EcsServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("solves", C.c_int64), ("solve_p50", C.c_double), ("solve_p99", C.c_double),
+                ("solve_mean", C.c_double), ("solve_max", C.c_double),
+                ("steps", C.c_int64), ("step_p50", C.c_double), ("step_p99", C.c_double),
+                ("device_bytes", C.c_int64), ("peak_device_bytes", C.c_int64),
+                ("peak_inflight", C.c_int32), ("slots", C.c_int32),
+                ("slots_created", C.c_int64), ("slot_hits", C.c_int64), ("evictions", C.c_int64),
+                ("gpu_launches", C.c_int64), ("busy_seconds", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 
-# (name, restype, argtypes): every symbol include/ecsgpu.h declares.
+# (name, restype, argtypes): every symbol include/ecsgpu.h and
+# include/ecs_serve.h declare.
 GPU_API = [
     ("ecs_version", C.c_char_p, []),
     ("ecs_status_string", C.c_char_p, [C.c_int]),
@@ -120,6 +163,21 @@ GPU_API = [
                                 C.POINTER(EcsStepStats)]),
     ("ecs_launch_count", C.c_int64, [_vp]),
     ("ecs_fix_shifts", C.c_int, [C.POINTER(EcsParams), C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    # ecs_serve.h
+    ("ecs_serve_create", C.c_int, [C.POINTER(EcsServeConfig), C.POINTER(_vp)]),
+    ("ecs_serve_destroy", C.c_int, [_vp]),
+    ("ecs_serve_submit_solve", C.c_int, [_vp, C.POINTER(EcsParams), C.POINTER(EcsSolveRequest),
+                                         C.POINTER(C.c_int64)]),
+    ("ecs_serve_submit_sim", C.c_int, [_vp, C.POINTER(EcsParams), C.POINTER(EcsSimRequest), C.POINTER(C.c_int64)]),
+    ("ecs_serve_poll", C.c_int, [_vp, C.POINTER(EcsServeResult), C.c_int, C.c_int]),
+    ("ecs_serve_pending", C.c_int64, [_vp]),
+    ("ecs_serve_stats", C.c_int, [_vp, C.POINTER(EcsServeStats)]),
+    ("ecs_serve_reset_stats", C.c_int, [_vp]),
+    ("ecs_serve_request_bytes", C.c_int64, [C.POINTER(EcsParams), C.c_int, C.c_int, C.c_int64]),
+    ("ecs_solve_density", C.c_int, [_vp, _vp, C.POINTER(C.c_double * 3), C.c_double, C.c_int, _vp,
+                                    C.POINTER(EcsSolveStats)]),
+    ("ecs_host_alloc", _vp, [C.c_size_t]),
+    ("ecs_host_free", None, [_vp]),
 ]
 
 HOST_API = [

@@ -35,7 +35,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CC_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-Wno-unused-parameter", f"-I{INCLUDE}"]
 
-GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu", "ecs_solver.cu", "ecs_noalloc.cu"]
+GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu", "ecs_solver.cu", "ecs_noalloc.cu", "ecs_serve.cu"]
 HOST_SOURCES = ["ecs_options.c", "ecs_io.c"]
 GPU_HOST_SOURCES = ["ecs_ops.c"]  # host C linked into libecsgpu (operator slots)
 
@@ -100,7 +100,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict:
         for w in ex.map(lambda t: _compile(*t, verbose), tasks):
             if w:
                 warnings.append(w)
-    link_gpu = [nvcc] + ARCH + ["-shared", "-o", str(LIBGPU)] + [str(o) for o in gpu_objs] + ["-lcudart"]
+    link_gpu = [nvcc] + ARCH + ["-shared", "-o", str(LIBGPU)] + [str(o) for o in gpu_objs] + ["-lcudart", "-lpthread"]
     if not LIBGPU.exists() or any(o.stat().st_mtime > LIBGPU.stat().st_mtime for o in gpu_objs):
         r = subprocess.run(link_gpu, capture_output=True, text=True)
         if r.returncode != 0:

@@ -101,19 +101,29 @@ const char *ecs_last_error(const EcsCtx *ctx) { return ctx ? ctx->err.c_str() : 
 
 int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
   if (!p) return -1;
-  size_t n = (size_t)p->Nx * p->Ny * p->Nz;
-  size_t ne = (size_t)(p->Nx + 1) * (p->Ny + 1) * (p->Nz + 1);
-  int64_t m = 30;
+  const int64_t n = (int64_t)p->Nx * p->Ny * p->Nz;
+  const int64_t ne = (int64_t)(p->Nx + 1) * (p->Ny + 1) * (p->Nz + 1);
+  const int64_t m = 30;  // Krylov basis vectors (FGMRES restart)
+  const int64_t t = precision == ECS_PREC_FP64 ? 8 : 4;  // solver arithmetic
   int64_t b = 0;
-  b += n * 8 * (1 + 4 + 1) + n * 8 * 4;  // phi, mom, rhs, acc
-  b += n * 8 * 2 + (m + 2) * 1024 * 8;   // r64, w64, reductions
+  b += n * 8 * (1 + 4 + 1) + n * 8 * 4;  // phi, moments, rhs; fixed-point accumulators
+  b += n * 8 * 2 + (m + 2) * 1024 * 8;   // FP64 residual and correction, reductions
+  // multigrid: 11 cell arrays and 2 plane arrays a level, levels summing to
+  // at most 8/7 of the finest; the coarsest level's inverse (<= 128 cells)
+  b += (n * 11 + n / 4) * t * 8 / 7 + 128 * 128 * 3 * t;
   if (precision == ECS_PREC_FP64) {
-    b += cap * 48 + ne * 32;
-    b += (2 * m + 1) * n * 8 + (int64_t)(n * 8 * 10 * 8 / 7);  // Krylov + multigrid levels
+    b += (2 * m + 1) * n * 8;  // Krylov bases V, Z
+    b += cap * 48 + ne * 32;   // ions (6 FP64), E numerators
   } else {
-    b += cap * 64 + ne * 16 + n * 4 * 2 + n / 1024 * 4;
-    b += (2 * m + 3) * n * 4 + (int64_t)(n * 4 * 10 * 8 / 7);
+    b += (2 * m + 3) * n * 4;  // Krylov bases V, Z, two FP32 work vectors
+    b += cap * 64 + ne * 16;   // ions (two 32-byte record buffers), E numerators
+    const int64_t keys = (int64_t)((p->Nx + ECS_TILE_X - 1) / ECS_TILE_X) * ((p->Ny + ECS_TILE_Y - 1) / ECS_TILE_Y) *
+                         ((p->Nz + ECS_TILE_Z - 1) / ECS_TILE_Z) * ECS_TILE_CELLS;
+    b += keys * 4 * 2 + keys / 1024 * 4;  // sort counts and offsets
   }
+  if (cap > 0) b += 2 * ecs_stage_ions(cap) * 48;  // host-transfer staging
+  // allocation rounding (about 40 allocations) and instantiated CUDA graphs
+  b += (int64_t)8 << 20;
   return b;
 }
 

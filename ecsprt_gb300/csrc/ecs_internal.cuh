@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -79,6 +80,24 @@ struct SolverGraph {
   int64_t k_head = 0, k_sweep = 0, k_step = 0;
 };
 
+// Instantiated graph of one stand-alone solve request (src/solver.c:107-170):
+// density in, fluxes = flux_scale * density, RHS, operator set-up, the solve,
+// potential and solve status out.  The two copy nodes are re-pointed at the
+// request's own buffers when those are pinned, else at the staging buffers.
+struct RequestGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t in_node = nullptr, out_node = nullptr;
+  double rtol = 0.0;
+  int max_it = 0;
+  double flux_scale[3] = {0.0, 0.0, 0.0};
+  int64_t k_pre = 0;                          // kernels before the solve nodes
+  double *h_in = nullptr, *h_out = nullptr;   // pinned staging, ncell doubles each
+  const double *src = nullptr;                // the launched request's buffers
+  double *dst = nullptr;
+  bool staged_out = false;
+};
+
 struct EcsCtx {
   EcsParams p;
   int prec = ECS_PREC_FP64;
@@ -136,6 +155,7 @@ struct EcsCtx {
   void *kdev_host = nullptr;        // pinned copy read back after a cycle
   void *kctl_host = nullptr;        // pinned staging of the cycle's tolerance and step limit
   SolverGraph sgraph;               // the whole solve as one CUDA graph
+  RequestGraph rgraph;              // a stand-alone solve request as one CUDA graph
   int use_graphs = 1;               // 0: the host drives the refinement and the Arnoldi steps
   void *rdev = nullptr;             // device state of the refinement loop
   void *rdev_host = nullptr;        // pinned copy
@@ -171,6 +191,15 @@ struct EcsCtx {
 
 // ---- error helpers -------------------------------------------------------
 int ecs_fail(EcsCtx *ctx, int code, const char *fmt, ...);
+// Ions per staging chunk of the host transfers (two chunks are held): an
+// eighth of the capacity, between 2^16 and 2^22 ions.
+inline int64_t ecs_stage_ions(int64_t cap) {
+  int64_t n = cap / 8;
+  if (n < ((int64_t)1 << 16)) n = (int64_t)1 << 16;
+  if (n > ((int64_t)1 << 22)) n = (int64_t)1 << 22;
+  return cap < n ? (cap > 0 ? cap : 1) : n;
+}
+
 int ecs_cuda_check(EcsCtx *ctx, cudaError_t e, const char *what);
 #define ECS_CUDA(ctx, call)                                        \
   do {                                                             \
@@ -235,6 +264,11 @@ int ecs_solver_setup(EcsCtx *ctx);       // multigrid hierarchy from the density
 int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st);
 int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y);
 int ecs_solver_free(EcsCtx *ctx);
+// Stand-alone solve request: launch (asynchronous, on ctx->stream) and, once
+// the stream's work is complete, finish (potential to the caller, stats).
+int ecs_request_launch(EcsCtx *ctx, const double *density, double *phi, const double flux_scale[3], double rtol,
+                       int max_it);
+int ecs_request_finish(EcsCtx *ctx, EcsSolveStats *st);
 // (defined in ecs_particles.cu)
 int ecs_particles_alloc(EcsCtx *ctx);
 int ecs_particles_free(EcsCtx *ctx);

@@ -1286,9 +1286,8 @@ int ecs_particles_free(EcsCtx *ctx) {
 
 // ---- host transfers ------------------------------------------------------------
 // Ions move between the host's AoS FP64 arrays and the device in chunks
-// through two staging buffers, so that the copy of one chunk overlaps the
-// conversion kernel of the other.
-constexpr int64_t kStageIons = 1 << 22;
+// (ecs_stage_ions) through two staging buffers, so that the copy of one
+// chunk overlaps the conversion kernel of the other.
 
 static int ensure_xfer(EcsCtx *ctx) {
   if (ctx->stage[0]) return ECS_OK;
@@ -1298,7 +1297,7 @@ static int ensure_xfer(EcsCtx *ctx) {
     ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_kern[q], cudaEventDisableTiming));
   }
   ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_ready, cudaEventDisableTiming));
-  const int64_t n = std::max<int64_t>(1, std::min<int64_t>(kStageIons, ctx->cap));
+  const int64_t n = ecs_stage_ions(ctx->cap);
   for (int q = 0; q < 2; q++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage[q], (size_t)n * 6 * sizeof(double)));
   ctx->stage_n = n;
   return ECS_OK;
@@ -1420,7 +1419,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
   }
   if (!k.collide) mode &= ~2;
   const size_t shm = (size_t)(kBlock / 32) * 32 * kTileStride * sizeof(long long);
-  static bool attr_set = false;
+  static std::atomic<bool> attr_set{false};
   if (!attr_set) {
     cudaFuncSetAttribute(k_particles64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     cudaFuncSetAttribute(k_particles32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);

@@ -1003,7 +1003,7 @@ int mg_setup(EcsCtx *ctx) {
     MgLevel<T> &C = mg.lv.back();
     const size_t bytes = C.n * 2 * C.n * sizeof(T);
     const bool in_smem = bytes <= kInverseSmem;
-    static bool attr_set[2] = {false, false};
+    static std::atomic<bool> attr_set[2];  // zero-initialised: false
     if (!attr_set[sizeof(T) == 8]) {
       ECS_CUDA(ctx, cudaFuncSetAttribute(k_coarse_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInverseSmem));
       attr_set[sizeof(T) == 8] = true;
@@ -1072,7 +1072,7 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
       off += 4 * nq;
     }
     const size_t bytes = (size_t)off * sizeof(T);
-    static bool attr_set[2] = {false, false};
+    static std::atomic<bool> attr_set[2];  // zero-initialised: false
     if (!attr_set[sizeof(T) == 8]) {
       ECS_CUDA(ctx, cudaFuncSetAttribute(k_vcycle_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem));
       attr_set[sizeof(T) == 8] = true;
@@ -1439,70 +1439,79 @@ int refine_correct(EcsCtx *ctx, int lvl) {
   return ECS_OK;
 }
 
-// One solve as one graph:
+// The nodes of one solve, appended to the graph being captured on
+// ctx->stream:
 //   [phi = 0, r = b | r = b - A phi]  ||r||  init  check
 //   WHILE( scale  cycle(WHILE Arnoldi)  phi += e  update  residual  norm  check )
 // The checks set the sweep loop's condition; everything stays on the device.
+// The kernel counts of the head, a sweep and an Arnoldi step go to sgraph.
+template <typename T>
+int capture_solve(EcsCtx *ctx, double rtol, int max_it, int warm) {
+  SolverGraph &sg = ctx->sgraph;
+  const size_t n = ctx->ncell;
+  const int64_t launches0 = ctx->launches;
+  int rc;
+  cudaError_t ce;
+  cudaGraph_t top = nullptr;
+  if ((rc = capture_graph(ctx, ctx->stream, &top))) return rc;
+  cudaGraphConditionalHandle hs;
+  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&hs, top, 0, cudaGraphCondAssignDefault));
+  if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) return rc;  // ||b||
+  k_solve_init<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, ctx->dots);
+  ECS_LAUNCHED(ctx);
+  if (!warm) {  // phi = 0: the residual is b and its norm is known
+    ECS_CUDA(ctx, cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream));
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    rc = refine_decide<T>(ctx, rtol, max_it, hs);
+  } else {
+    rc = refine_check<T>(ctx, rtol, max_it, hs);
+  }
+  if (rc) return rc;
+  sg.k_head = ctx->launches - launches0;
+  cudaGraph_t body = nullptr;
+  if ((rc = capture_conditional(ctx, ctx->stream, hs, cudaGraphCondTypeWhile, &body))) return rc;
+  cudaStream_t outer = ctx->stream;
+  ctx->stream = ctx->capst[1];
+  ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    ctx->stream = outer;
+    return ecs_cuda_check(ctx, ce, "sweep capture");
+  }
+  const int64_t l1 = ctx->launches;
+  rc = refine_correct<T>(ctx, 2);
+  if (!rc) rc = refine_check<T>(ctx, rtol, max_it, hs);
+  sg.k_sweep = ctx->launches - l1 - sg.k_step;
+  ce = cudaStreamEndCapture(ctx->stream, &body);
+  ctx->stream = outer;
+  if (rc) return rc;
+  ECS_CUDA(ctx, ce);
+  return ECS_OK;
+}
+
+int ensure_capture_streams(EcsCtx *ctx) {
+  for (auto &c : ctx->capst)
+    if (!c) ECS_CUDA(ctx, cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+  return ECS_OK;
+}
+
+// One solve as one graph (see capture_solve), built for (rtol, max_it, warm).
 template <typename T>
 int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm) {
   SolverGraph &sg = ctx->sgraph;
   if (sg.exec && sg.rtol == rtol && sg.max_it == max_it && sg.warm == warm) return ECS_OK;
   free_graph(sg);
-  for (auto &c : ctx->capst)
-    if (!c) ECS_CUDA(ctx, cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
-  const size_t n = ctx->ncell;
+  int rc = ensure_capture_streams(ctx);
+  if (rc) return rc;
   const int64_t launches0 = ctx->launches;
   cudaStream_t user = ctx->stream;
   ctx->stream = ctx->capst[0];
-  int rc = ECS_OK;
   cudaGraph_t g = nullptr;
   cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
   if (ce != cudaSuccess) {
     ctx->stream = user;
     return ecs_cuda_check(ctx, ce, "solve graph capture");
   }
-  do {
-    cudaGraph_t top = nullptr;
-    if ((rc = capture_graph(ctx, ctx->stream, &top))) break;
-    cudaGraphConditionalHandle hs;
-    if ((ce = cudaGraphConditionalHandleCreate(&hs, top, 0, cudaGraphCondAssignDefault)) != cudaSuccess) {
-      rc = ecs_cuda_check(ctx, ce, "conditional handle");
-      break;
-    }
-    if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) break;  // ||b||
-    k_solve_init<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, ctx->dots);
-    ECS_LAUNCHED(ctx);
-    if (!warm) {  // phi = 0: the residual is b and its norm is known
-      if ((ce = cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream)) != cudaSuccess ||
-          (ce = cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream)) !=
-              cudaSuccess) {
-        rc = ecs_cuda_check(ctx, ce, "solve graph copies");
-        break;
-      }
-      rc = refine_decide<T>(ctx, rtol, max_it, hs);
-    } else {
-      rc = refine_check<T>(ctx, rtol, max_it, hs);
-    }
-    if (rc) break;
-    sg.k_head = ctx->launches - launches0;
-    cudaGraph_t body = nullptr;
-    if ((rc = capture_conditional(ctx, ctx->stream, hs, cudaGraphCondTypeWhile, &body))) break;
-    cudaStream_t outer = ctx->stream;
-    ctx->stream = ctx->capst[1];
-    if ((ce = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
-                                            cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
-      ctx->stream = outer;
-      rc = ecs_cuda_check(ctx, ce, "sweep capture");
-      break;
-    }
-    const int64_t l1 = ctx->launches;
-    rc = refine_correct<T>(ctx, 2);
-    if (!rc) rc = refine_check<T>(ctx, rtol, max_it, hs);
-    sg.k_sweep = ctx->launches - l1 - sg.k_step;
-    ce = cudaStreamEndCapture(ctx->stream, &body);
-    ctx->stream = outer;
-    if (!rc && ce != cudaSuccess) rc = ecs_cuda_check(ctx, ce, "sweep capture");
-  } while (0);
+  rc = capture_solve<T>(ctx, rtol, max_it, warm);
   ce = cudaStreamEndCapture(ctx->stream, &g);
   ctx->stream = user;
   ctx->launches = launches0;
@@ -1526,6 +1535,119 @@ int solve_graph_launch(EcsCtx *ctx, double rtol, int max_it, int warm) {
   if (rc) return rc;
   ECS_CUDA(ctx, cudaGraphLaunch(ctx->sgraph.exec, ctx->stream));
   return ECS_OK;
+}
+
+// ---- stand-alone solve request ----------------------------------------------
+// Fluxes of a loaded density (src/file-io.c:51-59: VecAXPY into a zeroed
+// vector, so G_d = 0 + flux_scale_d * n), into the SoA moment planes 1..3.
+__global__ void k_density_flux(size_t n, double f0, double f1, double f2, double *__restrict__ mom) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double d = mom[c];
+    mom[n + c] = __dadd_rn(0.0, __dmul_rn(f0, d));
+    mom[2 * n + c] = __dadd_rn(0.0, __dmul_rn(f1, d));
+    mom[3 * n + c] = __dadd_rn(0.0, __dmul_rn(f2, d));
+  }
+}
+
+// The node that the last call captured on stream s.
+int last_captured(EcsCtx *ctx, cudaStream_t s, cudaGraphNode_t *node) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  ECS_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+  if (nd != 1) return ecs_fail(ctx, ECS_ERR_CUDA, "capture: expected one tail node, found %zu", nd);
+  *node = deps[0];
+  return ECS_OK;
+}
+
+void free_request_graph(RequestGraph &rg) {
+  if (rg.exec) cudaGraphExecDestroy(rg.exec);
+  if (rg.graph) cudaGraphDestroy(rg.graph);
+  rg.exec = nullptr;
+  rg.graph = nullptr;
+  rg.in_node = rg.out_node = nullptr;
+}
+
+// density -> moments -> RHS -> operator set-up -> solve -> phi, as one graph.
+template <typename T>
+int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it) {
+  RequestGraph &rg = ctx->rgraph;
+  if (rg.exec && rg.rtol == rtol && rg.max_it == max_it && rg.flux_scale[0] == fs[0] && rg.flux_scale[1] == fs[1] &&
+      rg.flux_scale[2] == fs[2])
+    return ECS_OK;
+  free_request_graph(rg);
+  const size_t n = ctx->ncell, bytes = n * sizeof(double);
+  if (!rg.h_in) {
+    ECS_CUDA(ctx, cudaMallocHost((void **)&rg.h_in, bytes));
+    ECS_CUDA(ctx, cudaMallocHost((void **)&rg.h_out, bytes));
+  }
+  int rc;
+  // allocations and one-time attributes outside the capture
+  if ((rc = ecs_solver_alloc(ctx))) return rc;
+  if ((rc = mg_alloc<T>(ctx))) return rc;
+  if ((rc = ensure_capture_streams(ctx))) return rc;
+  const int64_t launches0 = ctx->launches;
+  cudaStream_t user = ctx->stream;
+  ctx->stream = ctx->capst[0];
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) {
+    ctx->stream = user;
+    return ecs_cuda_check(ctx, ce, "request graph capture");
+  }
+  do {
+    if ((ce = cudaMemcpyAsync(ctx->mom, rg.h_in, bytes, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess) {
+      rc = ecs_cuda_check(ctx, ce, "density copy");
+      break;
+    }
+    if ((rc = last_captured(ctx, ctx->stream, &rg.in_node))) break;
+    k_density_flux<<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, fs[0], fs[1], fs[2], ctx->mom);
+    if ((ce = cudaGetLastError()) != cudaSuccess) {
+      rc = ecs_cuda_check(ctx, ce, "kernel launch");
+      break;
+    }
+    ctx->launches++;
+    if ((rc = ecs_grid_rhs(ctx))) break;
+    if ((rc = mg_setup<T>(ctx))) break;
+    rg.k_pre = ctx->launches - launches0;
+    if ((rc = capture_solve<T>(ctx, rtol, max_it, 0))) break;
+    if ((ce = cudaMemcpyAsync(rg.h_out, ctx->phi, bytes, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess) {
+      rc = ecs_cuda_check(ctx, ce, "potential copy");
+      break;
+    }
+    if ((rc = last_captured(ctx, ctx->stream, &rg.out_node))) break;
+    if ((ce = cudaMemcpyAsync(ctx->rdev_host, ctx->rdev, sizeof(RefineDev), cudaMemcpyDeviceToHost, ctx->stream)) !=
+        cudaSuccess) {
+      rc = ecs_cuda_check(ctx, ce, "status copy");
+      break;
+    }
+  } while (0);
+  ce = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->stream = user;
+  ctx->launches = launches0;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    rg.in_node = rg.out_node = nullptr;
+    return rc;
+  }
+  ECS_CUDA(ctx, ce);
+  rg.graph = g;
+  ECS_CUDA(ctx, cudaGraphInstantiate(&rg.exec, g, 0));
+  rg.rtol = rtol;
+  rg.max_it = max_it;
+  for (int d = 0; d < 3; d++) rg.flux_scale[d] = fs[d];
+  return ECS_OK;
+}
+
+// Page-locked (or registered) host memory: the copy engines read and write it
+// directly.
+bool host_pinned(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
 }
 
 }  // namespace
@@ -1690,6 +1812,9 @@ int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y) {
 
 int ecs_solver_free(EcsCtx *ctx) {
   free_graph(ctx->sgraph);
+  free_request_graph(ctx->rgraph);
+  if (ctx->rgraph.h_in) cudaFreeHost(ctx->rgraph.h_in);
+  if (ctx->rgraph.h_out) cudaFreeHost(ctx->rgraph.h_out);
   for (auto &c : ctx->capst)
     if (c) cudaStreamDestroy(c);
   free_mg(ctx->mg64);
@@ -1704,5 +1829,57 @@ int ecs_solver_free(EcsCtx *ctx) {
   if (ctx->rdev_host) cudaFreeHost(ctx->rdev_host);
   for (auto &e : ctx->ev_solve)
     if (e) cudaEventDestroy(e);
+  return ECS_OK;
+}
+
+// ---- stand-alone solve requests ---------------------------------------------
+int ecs_request_launch(EcsCtx *ctx, const double *density, double *phi, const double flux_scale[3], double rtol,
+                       int max_it) {
+  int rc = ctx->prec == ECS_PREC_FP64 ? build_request_graph<double>(ctx, flux_scale, rtol, max_it)
+                                      : build_request_graph<float>(ctx, flux_scale, rtol, max_it);
+  if (rc) return rc;
+  RequestGraph &rg = ctx->rgraph;
+  const size_t bytes = ctx->ncell * sizeof(double);
+  const double *src = density;
+  if (!host_pinned(density)) {
+    memcpy(rg.h_in, density, bytes);
+    src = rg.h_in;
+  }
+  rg.staged_out = !host_pinned(phi);
+  rg.dst = phi;
+  double *dst = rg.staged_out ? rg.h_out : phi;
+  ECS_CUDA(ctx, cudaGraphExecMemcpyNodeSetParams1D(rg.exec, rg.in_node, ctx->mom, src, bytes, cudaMemcpyHostToDevice));
+  ECS_CUDA(ctx, cudaGraphExecMemcpyNodeSetParams1D(rg.exec, rg.out_node, dst, ctx->phi, bytes, cudaMemcpyDeviceToHost));
+  if (!ctx->ev_solve[0]) {
+    ECS_CUDA(ctx, cudaEventCreate(&ctx->ev_solve[0]));
+    ECS_CUDA(ctx, cudaEventCreate(&ctx->ev_solve[1]));
+  }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[0], ctx->stream));
+  ECS_CUDA(ctx, cudaGraphLaunch(rg.exec, ctx->stream));
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[1], ctx->stream));
+  ctx->moments_ready = true;
+  ctx->lhs_ready = true;
+  ctx->eext_ready = false;
+  return ECS_OK;
+}
+
+int ecs_request_finish(EcsCtx *ctx, EcsSolveStats *st) {
+  RequestGraph &rg = ctx->rgraph;
+  const RefineDev *hr = (const RefineDev *)ctx->rdev_host;
+  if (rg.staged_out) memcpy(rg.dst, rg.h_out, ctx->ncell * sizeof(double));
+  const SolverGraph &sg = ctx->sgraph;
+  ctx->launches += rg.k_pre + sg.k_head + hr->sweeps * sg.k_sweep + (int64_t)hr->its * sg.k_step;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev_solve[0], ctx->ev_solve[1]);
+  if (st) {
+    st->iterations = hr->its;
+    st->refinements = hr->sweeps;
+    st->relres = hr->rel;
+    st->seconds = ms * 1e-3;
+  }
+  if (hr->nonfinite) return ecs_fail(ctx, ECS_ERR_NONFINITE, "non-finite residual in solve");
+  if (hr->bnorm > 0.0 && hr->rel > rg.rtol)
+    return ecs_fail(ctx, ECS_ERR_NOT_CONVERGED, "solve stopped at relres %.3e > %.3e after %d iterations", hr->rel,
+                    rg.rtol, hr->its);
   return ECS_OK;
 }

@@ -108,8 +108,8 @@ def _declared(header):
 
 def test_gpu_library_exports_every_declared_symbol(built):
     lib = ctypes.CDLL(str(_lib.GPU_LIB_PATH))
-    names = _declared("ecsgpu.h")
-    assert len(names) >= 25
+    names = _declared("ecsgpu.h") + _declared("ecs_serve.h")
+    assert len(names) >= 35
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     bound = {n for n, _, _ in _lib.GPU_API}
