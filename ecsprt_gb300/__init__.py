@@ -41,11 +41,13 @@ import numpy as np
 import weakref
 
 from . import _lib
-from ._lib import (ECS_PREC_FP64, ECS_PREC_MIXED, ECS_SERVE_SIM, ECS_SERVE_SOLVE, EcsParams, EcsPicApp,
+from ._lib import (ECS_INIT_MODES, ECS_INIT_RANDOM, ECS_INIT_SINUSOIDAL, ECS_INIT_SOBOL, ECS_PREC_FP64,
+                   ECS_PREC_MIXED, ECS_SERVE_SIM, ECS_SERVE_SOLVE, EcsDensityModes, EcsParams, EcsPicApp,
                    EcsServeConfig, EcsServeResult, EcsServeStats, EcsSimRequest, EcsSolveRequest, EcsSolveStats,
                    EcsSolverApp, EcsStepStats)
 
 __all__ = [
+    "ECS_INIT_MODES", "ECS_INIT_RANDOM", "ECS_INIT_SINUSOIDAL", "ECS_INIT_SOBOL", "density_modes",
     "ECS_PREC_FP64", "ECS_PREC_MIXED", "ECS_SERVE_SIM", "ECS_SERVE_SOLVE", "EcsError", "EcsParams", "Context",
     "Options", "Server", "pinned_empty", "serve_request_bytes", "params_from_options", "pic_app_from_options", "solver_app_from_options",
 ]
@@ -71,6 +73,21 @@ def _f64(a, shape=None, writeable=False, name="array") -> np.ndarray:
     if writeable and not a.flags.writeable:
         raise ValueError(f"{name} must be writeable")
     return a
+
+
+def density_modes(modes) -> EcsDensityModes:
+    """EcsDensityModes from [(kx, ky, kz, amplitude, phase), ...]: density
+    1 + sum a cos(2 pi k.(x/L) + phase)."""
+    m = EcsDensityModes()
+    modes = list(modes)
+    if len(modes) > 16:
+        raise ValueError("at most 16 modes")
+    m.nmodes = len(modes)
+    for q, (kx, ky, kz, a, ph) in enumerate(modes):
+        m.k[q][0], m.k[q][1], m.k[q][2] = int(kx), int(ky), int(kz)
+        m.amplitude[q] = float(a)
+        m.phase[q] = float(ph)
+    return m
 
 
 def pinned_empty(shape) -> np.ndarray:
@@ -217,6 +234,16 @@ class Context:
         if pos.shape != vel.shape:
             raise EcsError(_lib.ECS_ERR_INVALID, "pos and vel differ in shape")
         self._check(self._lib.ecs_particles_upload(self._h, _ptr(pos), _ptr(vel), pos.shape[0]))
+
+    def init_particles(self, dist: int, np_: int, seed: int = 20261203, modes=None):
+        """Initial ions generated on the device (ecs_particles_init): Sobol
+        positions as the reference's (``ECS_INIT_SOBOL``), uniform random
+        (``ECS_INIT_RANDOM``), the reference's sinusoidal rejection
+        (``ECS_INIT_SINUSOIDAL``) or Fourier-mode densities (``ECS_INIT_MODES``,
+        ``modes`` from :func:`density_modes`); Maxwellian velocities."""
+        m = modes if modes is None or isinstance(modes, EcsDensityModes) else density_modes(modes)
+        self._check(self._lib.ecs_particles_init(self._h, int(dist), int(np_), int(seed),
+                                                 C.byref(m) if m is not None else None))
 
     def download_particles(self):
         n = int(self._lib.ecs_particles_count(self._h))

@@ -86,6 +86,16 @@ class EcsSolverApp(C.Structure):
 ECS_SERVE_SOLVE = 0
 ECS_SERVE_SIM = 1
 
+ECS_INIT_SOBOL = 0
+ECS_INIT_RANDOM = 2
+ECS_INIT_SINUSOIDAL = 4
+ECS_INIT_MODES = 16
+
+
+class EcsDensityModes(C.Structure):
+    _fields_ = [("nmodes", C.c_int32), ("k", (C.c_int32 * 3) * 16), ("amplitude", C.c_double * 16),
+                ("phase", C.c_double * 16)]
+
 
 class EcsServeConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_inflight", C.c_int32), ("precision", C.c_int32),
@@ -144,6 +154,7 @@ GPU_API = [
     ("ecs_particles_upload", C.c_int, [_vp, _vp, _vp, C.c_int64]),
     ("ecs_particles_download", C.c_int, [_vp, _vp, _vp]),
     ("ecs_particles_count", C.c_int64, [_vp]),
+    ("ecs_particles_init", C.c_int, [_vp, C.c_int, C.c_int64, C.c_uint64, C.POINTER(EcsDensityModes)]),
     ("ecs_phi_upload", C.c_int, [_vp, _vp]),
     ("ecs_phi_download", C.c_int, [_vp, _vp]),
     ("ecs_moments_upload", C.c_int, [_vp, _vp]),

@@ -259,6 +259,11 @@ int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel) {
 
 int64_t ecs_particles_count(const EcsCtx *ctx) { return ctx ? ctx->np : -1; }
 
+int ecs_particles_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes) {
+  if (!ctx) return ECS_ERR_INVALID;
+  return ecs_part_init(ctx, dist, np, seed, modes);
+}
+
 int ecs_phi_upload(EcsCtx *ctx, const double *phi) {
   if (!ctx || !phi) return ECS_ERR_INVALID;
   ECS_CUDA(ctx, cudaMemcpyAsync(ctx->phi, phi, ctx->ncell * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));

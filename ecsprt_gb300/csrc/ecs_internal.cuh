@@ -273,6 +273,7 @@ int ecs_request_finish(EcsCtx *ctx, EcsSolveStats *st);
 int ecs_particles_alloc(EcsCtx *ctx);
 int ecs_particles_free(EcsCtx *ctx);
 int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
+int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes);
 int ecs_part_download(EcsCtx *ctx, double *pos, double *vel);
 // Enqueue the download after ctx->stream's current work; ecs_part_xfer_wait
 // waits for it.

@@ -1249,6 +1249,126 @@ unsigned int grid_blocks(const EcsCtx *ctx, int64_t n, int per_sm) {
   return (unsigned int)want;
 }
 
+// ---- initial ions on the device ----------------------------------------------
+// Positions (src/positions.c:139-388) and Maxwellian velocities
+// (src/velocities.c:14-47), one thread per ion, stored like an upload.
+constexpr int kSobolBits = 30;     // MAXBIT of src/random.c
+constexpr int kInitTries = 256;    // rejection attempts per ion
+constexpr int kInitModes = 16;
+
+struct InitK {
+  int dist;
+  uint32_t key0, key1;
+  double L[3];
+  double vT[3], v0[3];
+  uint32_t sob[3][kSobolBits];  // direction numbers v_{j}, j = 1..30, of dimensions 1..3
+  int nmodes;
+  int kv[kInitModes][3];
+  double amp[kInitModes], phase[kInitModes];
+  double inv_max;  // acceptance scale of the rejection
+};
+
+// Sobol direction numbers of the first three dimensions (Bratley-Fox, 30
+// bits), with the reference's recurrence: the higher numbers XOR v_{j-1}
+// where the published method XORs v_{j-l} (src/random.c:256-266).
+void sobol_directions(uint32_t v[3][kSobolBits]) {
+  static const int deg[3] = {1, 2, 3};
+  static const uint32_t poly[3] = {0, 1, 1};
+  static const uint32_t start[3][3] = {{1, 0, 0}, {1, 1, 0}, {1, 3, 7}};
+  for (int d = 0; d < 3; d++) {
+    uint32_t w[kSobolBits + 1] = {0};
+    for (int j = 1; j <= deg[d]; j++) w[j] = start[d][j - 1] << (kSobolBits - j);
+    for (int j = deg[d] + 1; j <= kSobolBits; j++) {
+      uint32_t x = w[j - deg[d]];
+      x ^= x >> deg[d];
+      uint32_t c = poly[d];
+      for (int l = deg[d] - 1; l >= 1; l--) {
+        if (c & 1u) x ^= w[j - 1];
+        c >>= 1;
+      }
+      w[j] = x;
+    }
+    for (int j = 1; j <= kSobolBits; j++) v[d][j - 1] = w[j];
+  }
+}
+
+__device__ __forceinline__ double init_density(const InitK &k, const double s[3]) {
+  if (k.dist == ECS_INIT_SINUSOIDAL) return 1.0 + 0.25 * sin(2.0 * M_PI * s[0]);  // src/positions.c:236-251
+  double w = 1.0;
+  for (int m = 0; m < k.nmodes; m++) {
+    const double a = (double)k.kv[m][0] * s[0] + (double)k.kv[m][1] * s[1] + (double)k.kv[m][2] * s[2];
+    w += k.amp[m] * cos(2.0 * M_PI * a + k.phase[m]);
+  }
+  return w;
+}
+
+// Position of ion i as fractions s of the box; false if the rejection gave up.
+__device__ bool init_fraction(const InitK &k, int64_t i, double s[3]) {
+  const uint32_t lo = (uint32_t)i, hi = (uint32_t)((uint64_t)i >> 32);
+  if (k.dist == ECS_INIT_SOBOL) {
+    // after i+1 draws the generator state is the XOR of the direction
+    // numbers at the set bits of gray(i+1)
+    const uint64_t m = (uint64_t)i + 1;
+    const uint32_t g = (uint32_t)(m ^ (m >> 1));
+    for (int d = 0; d < 3; d++) {
+      uint32_t x = 0;
+      for (int b = 0; b < kSobolBits; b++)
+        if ((g >> b) & 1u) x ^= k.sob[d][b];
+      s[d] = (double)x * (1.0 / 1073741824.0);
+    }
+    return true;
+  }
+  for (int a = 0; a < kInitTries; a++) {
+    const EcsU4 q1 = ecs_philox({lo, hi, 0x504F5300u + 2u * (uint32_t)a, 0x494E4954u}, k.key0, k.key1);
+    const EcsU4 q2 = ecs_philox({lo, hi, 0x504F5301u + 2u * (uint32_t)a, 0x494E4954u}, k.key0, k.key1);
+    s[0] = ecs_u01d(q1.x, q1.y);
+    s[1] = ecs_u01d(q1.z, q1.w);
+    s[2] = ecs_u01d(q2.x, q2.y);
+    if (k.dist == ECS_INIT_RANDOM) return true;
+    if (init_density(k, s) * k.inv_max > ecs_u01d(q2.z, q2.w)) return true;  // src/positions.c:314-321
+  }
+  return false;
+}
+
+// v_d = vT_d * N(0,1) + v0_d (Box-Muller on the ion's own counter)
+__device__ void init_velocity(const InitK &k, int64_t i, double v[3]) {
+  const uint32_t lo = (uint32_t)i, hi = (uint32_t)((uint64_t)i >> 32);
+  const EcsU4 q1 = ecs_philox({lo, hi, 0x56454C00u, 0x494E4954u}, k.key0, k.key1);
+  const EcsU4 q2 = ecs_philox({lo, hi, 0x56454C01u, 0x494E4954u}, k.key0, k.key1);
+  const double r1 = sqrt(-2.0 * log(ecs_u01d(q1.x, q1.y)));
+  double sn, cs;
+  sincospi(2.0 * ecs_u01d(q1.z, q1.w), &sn, &cs);
+  const double n2 = sqrt(-2.0 * log(ecs_u01d(q2.x, q2.y))) * cospi(2.0 * ecs_u01d(q2.z, q2.w));
+  const double nd[3] = {r1 * cs, r1 * sn, n2};
+  for (int d = 0; d < 3; d++) v[d] = k.vT[d] * nd[d] + k.v0[d];
+}
+
+__global__ void k_init_ions(InitK ik, PartK k, int64_t n, int fp64, float4 *__restrict__ ions, double *px,
+                            double *py, double *pz, double *vx, double *vy, double *vz, EcsDevStatus *st) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double s[3], pos[3], vel[3];
+    if (!init_fraction(ik, i, s)) {
+      atomicOr(&st->flags, ECS_FLAG_RANGE);
+      s[0] = s[1] = s[2] = 0.5;
+    }
+    for (int d = 0; d < 3; d++) {
+      pos[d] = s[d] * ik.L[d];  // src/positions.c:174, 318
+      if (pos[d] >= ik.L[d]) pos[d] = nextafter(ik.L[d], 0.0);
+    }
+    init_velocity(ik, i, vel);
+    if (fp64) {
+      px[i] = pos[0]; py[i] = pos[1]; pz[i] = pos[2];
+      vx[i] = vel[0]; vy[i] = vel[1]; vz[i] = vel[2];
+    } else {
+      float a, b, c;
+      const int ci = to_cell(pos[0], k.dx, k.Nx, a);
+      const int cj = to_cell(pos[1], k.dy, k.Ny, b);
+      const int ck = to_cell(pos[2], k.dz, k.Nz, c);
+      store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[0], (float)vel[1], (float)vel[2]});
+    }
+  }
+}
+
 }  // namespace
 
 // ============================================================================
@@ -1353,6 +1473,74 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
   }
   // the host arrays may be reused once this returns
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[1]));
+  return ECS_OK;
+}
+
+// Initial ions generated on the device (see InitK); the same bookkeeping as
+// an upload.
+int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes) {
+  if (np < 0 || np > ctx->cap) return ecs_fail(ctx, ECS_ERR_INVALID, "np %lld exceeds capacity %lld", (long long)np, (long long)ctx->cap);
+  const EcsParams &p = ctx->p;
+  InitK ik;
+  memset(&ik, 0, sizeof ik);
+  ik.dist = dist;
+  ik.key0 = (uint32_t)seed ^ 0x52414E44u;
+  ik.key1 = (uint32_t)(seed >> 32);
+  ik.L[0] = p.Lx; ik.L[1] = p.Ly; ik.L[2] = p.Lz;
+  ik.vT[0] = p.viTx; ik.vT[1] = p.viTy; ik.vT[2] = p.viTz;
+  ik.v0[0] = p.vi0x; ik.v0[1] = p.vi0y; ik.v0[2] = p.vi0z;
+  switch (dist) {
+    case ECS_INIT_SOBOL:
+      if (np >= ((int64_t)1 << kSobolBits)) return ecs_fail(ctx, ECS_ERR_INVALID, "Sobol positions need np < 2^30");
+      sobol_directions(ik.sob);
+      break;
+    case ECS_INIT_RANDOM:
+      break;
+    case ECS_INIT_SINUSOIDAL: {
+      // the largest density at the grid nodes, src/positions.c:292-303
+      double mx = 0.0;
+      for (int i = 0; i < p.Nx; i++) mx = std::max(mx, 1.0 + 0.25 * sin(2 * M_PI * ((double)i / p.Nx)));
+      ik.inv_max = 1.0 / mx;
+      break;
+    }
+    case ECS_INIT_MODES: {
+      if (!modes || modes->nmodes < 0 || modes->nmodes > kInitModes)
+        return ecs_fail(ctx, ECS_ERR_INVALID, "density modes: 0..%d modes required", kInitModes);
+      double sum = 0.0;
+      ik.nmodes = modes->nmodes;
+      for (int m = 0; m < modes->nmodes; m++) {
+        for (int d = 0; d < 3; d++) ik.kv[m][d] = modes->k[m][d];
+        ik.amp[m] = modes->amplitude[m];
+        ik.phase[m] = modes->phase[m];
+        sum += fabs(modes->amplitude[m]);
+      }
+      if (!(sum < 1.0)) return ecs_fail(ctx, ECS_ERR_INVALID, "density modes: sum of |amplitude| must be < 1");
+      ik.inv_max = 1.0 / (1.0 + sum);
+      break;
+    }
+    default:
+      return ecs_fail(ctx, ECS_ERR_UNSUPPORTED, "position distribution %d is not available on the device", dist);
+  }
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  const PartK k = make_k(ctx, 0.0);
+  const bool fp64 = ctx->prec == ECS_PREC_FP64;
+  if (np > 0) {
+    k_init_ions<<<grid_blocks(ctx, np, 8), kBlock, 0, ctx->stream>>>(
+        ik, k, np, fp64 ? 1 : 0, fp64 ? nullptr : ctx->ions[ctx->cur], ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy,
+        ctx->vz, ctx->dstat);
+    ECS_LAUNCHED(ctx);
+  }
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->hstat->flags & ECS_FLAG_RANGE)
+    return ecs_fail(ctx, ECS_ERR_RANGE, "rejection sampling gave up after %d attempts for an ion", kInitTries);
+  ctx->np = np;
+  ctx->attempt_rate = -1.0;
+  ctx->tiles_valid = false;
+  if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
+    int rc = ecs_part_sort(ctx);
+    if (rc) return rc;
+  }
   return ECS_OK;
 }
 

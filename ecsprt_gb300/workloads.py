@@ -35,16 +35,33 @@ def sim_options(n: int, ppc: int, drift: float, nu: float, dt: float = 0.1) -> s
             f"-nui {nu} -nue 8.79e9 -Te 11604.5 -E0 0 -Np -{ppc} -dt {dt}")
 
 
-def fourier_modes(shape, nmodes: int, amplitude: float, rng: np.random.Generator, kmax: int = 4) -> np.ndarray:
-    """sum_m amplitude cos(k_m . r + phi_m) on a [Nz][Ny][Nx] grid of unit
-    cells (r at the nodes, L = the grid extent)."""
-    nz, ny, nx = shape
+def random_modes(nmodes: int, amplitude: float, rng: np.random.Generator, kmax: int = 4):
+    """[(kx, ky, kz, amplitude, phase)]: integer wavevectors with
+    0 < |k| <= kmax, phases uniform in [0, 2 pi)."""
     ks = []
     while len(ks) < nmodes:
         k = rng.integers(-kmax, kmax + 1, size=3)
         if 0 < float(np.sqrt((k * k).sum())) <= kmax:
             ks.append(k)
     phases = rng.uniform(0.0, 2.0 * np.pi, nmodes)
+    return [(int(k[0]), int(k[1]), int(k[2]), float(amplitude), float(ph)) for k, ph in zip(ks, phases)]
+
+
+# the 256 x 256 x 128 workload's initial density: 1 + 8 modes of amplitude 0.02
+C3_SEED = 20261208
+
+
+def c3_modes():
+    return random_modes(8, 0.02, np.random.default_rng(C3_SEED))
+
+
+def fourier_modes(shape, nmodes: int, amplitude: float, rng: np.random.Generator, kmax: int = 4) -> np.ndarray:
+    """sum_m amplitude cos(k_m . r + phi_m) on a [Nz][Ny][Nx] grid of unit
+    cells (r at the nodes, L = the grid extent)."""
+    nz, ny, nx = shape
+    modes = random_modes(nmodes, amplitude, rng, kmax)
+    ks = [np.array(m[:3]) for m in modes]
+    phases = [m[4] for m in modes]
     x = 2.0 * np.pi * np.arange(nx) / nx
     y = 2.0 * np.pi * np.arange(ny) / ny
     z = 2.0 * np.pi * np.arange(nz) / nz

@@ -135,6 +135,32 @@ int ecs_particles_upload(EcsCtx *ctx, const double *pos, const double *vel, int6
 int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel);
 int64_t ecs_particles_count(const EcsCtx *ctx);
 
+/* ---- initial ions generated on the device -------------------------------- */
+/* Position distributions: the PDistType values of src/positions.c:8-10 that
+   the reference implements, plus Fourier-mode densities. */
+enum {
+  ECS_INIT_SOBOL = 0,      /* SobolDistribution src/positions.c:139-233: the same
+                              positions, bit for bit (np < 2^30) */
+  ECS_INIT_RANDOM = 2,     /* "normal", src/positions.c:42-137: uniform s*L (ran3 there,
+                              a counter-based generator here: same distribution) */
+  ECS_INIT_SINUSOIDAL = 4, /* Rejection + SinusoidalDistribution src/positions.c:236-388:
+                              density 1 + 0.25 sin(2 pi x/Lx), same acceptance test */
+  ECS_INIT_MODES = 16      /* density 1 + sum_m a_m cos(2 pi k_m.(x/L) + phase_m) by
+                              rejection (no reference counterpart; sum |a_m| < 1) */
+};
+typedef struct EcsDensityModes {
+  int32_t nmodes;       /* at most 16 */
+  int32_t k[16][3];     /* integer wavevectors, cycles per box length */
+  double amplitude[16];
+  double phase[16];
+} EcsDensityModes;
+/* np ions (np <= np_capacity): positions from `dist` (modes only for
+   ECS_INIT_MODES), velocities vT_d * N(0,1) + v0_d as NormalVelocities
+   (src/velocities.c:14-47; gasdev there, Box-Muller on Philox4x32-10 keyed
+   by `seed` here).  Replaces the host generation and broadcast of
+   InitializePositions / InitializeVelocities (src/positions.c:390-431). */
+int ecs_particles_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes);
+
 /* ---- grid fields (host arrays, [Nz][Ny][Nx], x fastest) ----------------- */
 int ecs_phi_upload(EcsCtx *ctx, const double *phi);
 int ecs_phi_download(EcsCtx *ctx, double *phi);
