@@ -52,8 +52,9 @@ int validate(const EcsParams *p) {
     if (p->bc[d] == ECS_BC_INJECT_ADVECT) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "inject-advect boundaries are not implemented");
     if (p->bc[d] == ECS_BC_INJECT_REFLECT && d != 2) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "reflecting boundaries are supported on z only");
   }
-  if (p->lhs_type != ECS_LHS_FULL || p->rhs_type != ECS_RHS_FULL)
-    return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "only -lhs full and -rhs full run on the GPU path");
+  if (p->lhs_type < ECS_LHS_IDENTITY || p->lhs_type > ECS_LHS_FULL || p->rhs_type < ECS_RHS_CONSTANT ||
+      p->rhs_type > ECS_RHS_FULL)
+    return ecs_fail(nullptr, ECS_ERR_INVALID, "unknown -lhs %d / -rhs %d", p->lhs_type, p->rhs_type);
   return ECS_OK;
 }
 

@@ -52,6 +52,19 @@ struct RhsK {
   double kappa, hx, hy, hz, hxx, hyy, hzz, E0, cth, cG, scale;
 };
 
+// Fixed-order sum of `local` over the block into partial[block].
+__device__ __forceinline__ void block_partial(double local, double *sh, double *__restrict__ partial) {
+  for (int s = 16; s >= 1; s >>= 1) local += __shfl_xor_sync(ECS_FULL_MASK, local, s);
+  const int t = thread_lin();
+  if ((t & 31) == 0) sh[t >> 5] = local;
+  __syncthreads();
+  if (t == 0) {
+    double u = 0.0;
+    for (int w = 0; w < kTx * kTy / 32; w++) u += sh[w];
+    partial[block_lin()] = u;
+  }
+}
+
 // b at every cell; each block writes the sum of its cells to partial[block]
 // (z loop with stride gridDim.z, so the block count stays bounded).
 __global__ void k_rhs(GridG g, RhsK r, const double *__restrict__ mom, double *__restrict__ b,
@@ -83,16 +96,36 @@ __global__ void k_rhs(GridG g, RhsK r, const double *__restrict__ mom, double *_
       local += v;
     }
   }
-  // fixed-order block sum
-  for (int s = 16; s >= 1; s >>= 1) local += __shfl_xor_sync(ECS_FULL_MASK, local, s);
-  const int t = thread_lin();
-  if ((t & 31) == 0) sh[t >> 5] = local;
-  __syncthreads();
-  if (t == 0) {
-    double u = 0.0;
-    for (int w = 0; w < kTx * kTy / 32; w++) u += sh[w];
-    partial[block_lin()] = u;
+  block_partial(local, sh, partial);
+}
+
+// -rhs sinusoidal (ComputeSinusoidalRHS3D, src/rhs.c:82-148): b = n0 cos(2 pi
+// x) cos(2 pi y) cos(2 pi z) scale at the cell centres x = (i + 1/2) dx (in
+// the grid's own units, as the reference), block partials for the mean that
+// MatNullSpaceRemove takes out (src/rhs.c:138-141).
+__global__ void k_rhs_sin(GridG g, double dx, double dy, double dz, double n0, double scale, double *__restrict__ b,
+                          double *__restrict__ partial) {
+  __shared__ double sh[kTx * kTy / 32];
+  double local = 0.0;
+  int i, j, k0;
+  if (at3(g.nx, g.ny, i, j, k0)) {
+    const double twopi = 2 * M_PI;
+    const double cx = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)i, 0.5), dx)));
+    const double cy = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)j, 0.5), dy)));
+    for (int k = k0; k < g.nz; k += gridDim.z) {
+      const double cz = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)k, 0.5), dz)));
+      const double v = __dmul_rn(__dmul_rn(n0, __dmul_rn(__dmul_rn(cx, cy), cz)), scale);
+      b[lin3(g, i, j, k)] = v;
+      local += v;
+    }
   }
+  block_partial(local, sh, partial);
+}
+
+// -rhs constant (ComputeConstantRHS, src/rhs.c:6-23): b = n0 * scale, no
+// projection.
+__global__ void k_fill(size_t n, double v, double *__restrict__ b) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) b[c] = v;
 }
 
 // out[0] = (sum of partial[0..nb)) / div, one block, fixed order.
@@ -157,17 +190,26 @@ int ecs_grid_rhs(EcsCtx *ctx) {
   int rc = ecs_solver_alloc(ctx);
   if (rc) return rc;
   const EcsParams &p = ctx->p;
+  if (p.rhs_type == ECS_RHS_CONSTANT) {
+    k_fill<<<blocks1d(ctx, ctx->ncell), 256, 0, ctx->stream>>>(ctx->ncell, p.n0 * p.scale, ctx->rhs);
+    ECS_LAUNCHED(ctx);
+    return ECS_OK;
+  }
   GridG g = make_grid(p, p.Nx, p.Ny, p.Nz);
-  RhsK r;
-  r.kappa = p.kappa_e;
-  r.hx = 1.0 / (2.0 * p.dx); r.hy = 1.0 / (2.0 * p.dy); r.hz = 1.0 / (2.0 * p.dz);
-  r.hxx = 1.0 / (p.dx * p.dx); r.hyy = 1.0 / (p.dy * p.dy); r.hzz = 1.0 / (p.dz * p.dz);
-  r.E0 = p.E0; r.cth = p.cth; r.cG = p.cG; r.scale = p.scale;
   dim3 grid = blocks3(g);
   const unsigned plane_blocks = grid.x * grid.y;
   grid.z = std::max(1u, std::min(grid.z, (unsigned)ctx->nred / plane_blocks));
   const int nb = (int)(grid.x * grid.y * grid.z);
-  k_rhs<<<grid, threads3(), 0, ctx->stream>>>(g, r, ctx->mom, ctx->rhs, ctx->red);
+  if (p.rhs_type == ECS_RHS_SINUSOIDAL) {
+    k_rhs_sin<<<grid, threads3(), 0, ctx->stream>>>(g, p.dx, p.dy, p.dz, p.n0, p.scale, ctx->rhs, ctx->red);
+  } else {
+    RhsK r;
+    r.kappa = p.kappa_e;
+    r.hx = 1.0 / (2.0 * p.dx); r.hy = 1.0 / (2.0 * p.dy); r.hz = 1.0 / (2.0 * p.dz);
+    r.hxx = 1.0 / (p.dx * p.dx); r.hyy = 1.0 / (p.dy * p.dy); r.hzz = 1.0 / (p.dz * p.dz);
+    r.E0 = p.E0; r.cth = p.cth; r.cG = p.cG; r.scale = p.scale;
+    k_rhs<<<grid, threads3(), 0, ctx->stream>>>(g, r, ctx->mom, ctx->rhs, ctx->red);
+  }
   ECS_LAUNCHED(ctx);
   k_sum_final<<<1, 1024, 0, ctx->stream>>>(nb, ctx->red, (double)ctx->ncell, ctx->dots);
   ECS_LAUNCHED(ctx);

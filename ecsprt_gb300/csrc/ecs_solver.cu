@@ -916,6 +916,11 @@ bool fully_periodic(const EcsCtx *ctx) {
   return ctx->p.bc[0] == ECS_BC_PERIODIC && ctx->p.bc[1] == ECS_BC_PERIODIC && ctx->p.bc[2] == ECS_BC_PERIODIC;
 }
 
+// The density the operator is built from (-lhs laplacian ignores it: see
+// make_op).
+const double *op_density(const EcsCtx *ctx) { return ctx->mom; }
+bool identity_lhs(const EcsCtx *ctx) { return ctx->p.lhs_type == ECS_LHS_IDENTITY; }
+
 template <typename T>
 Multigrid<T> &mg_of(EcsCtx *ctx);
 template <>
@@ -985,7 +990,7 @@ int mg_setup(EcsCtx *ctx) {
   if (rc) return rc;
   Multigrid<T> &mg = mg_of<T>(ctx);
   MgLevel<T> &L0 = mg.lv[0];
-  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, ctx->stream>>>(L0.n, ctx->mom, L0.dens);
+  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, ctx->stream>>>(L0.n, op_density(ctx), L0.dens);
   ECS_LAUNCHED(ctx);
   for (size_t l = 1; l < mg.lv.size(); l++) {
     MgLevel<T> &F = mg.lv[l - 1], &C = mg.lv[l];
@@ -1396,7 +1401,7 @@ template <typename T>
 int refine_check(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
   const EcsParams &p = ctx->p;
   const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
-  k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
+  k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
   ECS_LAUNCHED(ctx);
   int rc = norm64_dev(ctx, ctx->r64, ctx->dots);
   if (rc) return rc;
@@ -1454,11 +1459,17 @@ int capture_solve(EcsCtx *ctx, double rtol, int max_it, int warm) {
   cudaError_t ce;
   cudaGraph_t top = nullptr;
   if ((rc = capture_graph(ctx, ctx->stream, &top))) return rc;
-  cudaGraphConditionalHandle hs;
-  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&hs, top, 0, cudaGraphCondAssignDefault));
   if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) return rc;  // ||b||
   k_solve_init<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, ctx->dots);
   ECS_LAUNCHED(ctx);
+  if (identity_lhs(ctx)) {  // -lhs identity (ComputeIdentityLHS, src/lhs.c:11-23): phi = b exactly
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->phi, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    sg.k_head = ctx->launches - launches0;
+    sg.k_sweep = sg.k_step = 0;
+    return ECS_OK;
+  }
+  cudaGraphConditionalHandle hs;
+  ECS_CUDA(ctx, cudaGraphConditionalHandleCreate(&hs, top, 0, cudaGraphCondAssignDefault));
   if (!warm) {  // phi = 0: the residual is b and its norm is known
     ECS_CUDA(ctx, cudaMemsetAsync(ctx->phi, 0, n * sizeof(double), ctx->stream));
     ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1584,7 +1595,7 @@ int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it
   int rc;
   // allocations and one-time attributes outside the capture
   if ((rc = ecs_solver_alloc(ctx))) return rc;
-  if ((rc = mg_alloc<T>(ctx))) return rc;
+  if (!identity_lhs(ctx) && (rc = mg_alloc<T>(ctx))) return rc;
   if ((rc = ensure_capture_streams(ctx))) return rc;
   const int64_t launches0 = ctx->launches;
   cudaStream_t user = ctx->stream;
@@ -1608,7 +1619,7 @@ int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it
     }
     ctx->launches++;
     if ((rc = ecs_grid_rhs(ctx))) break;
-    if ((rc = mg_setup<T>(ctx))) break;
+    if (!identity_lhs(ctx) && (rc = mg_setup<T>(ctx))) break;
     rg.k_pre = ctx->launches - launches0;
     if ((rc = capture_solve<T>(ctx, rtol, max_it, 0))) break;
     if ((ce = cudaMemcpyAsync(rg.h_out, ctx->phi, bytes, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess) {
@@ -1691,7 +1702,7 @@ int ecs_solver_alloc(EcsCtx *ctx) {
 int ecs_solver_setup(EcsCtx *ctx) {
   int rc = ecs_solver_alloc(ctx);
   if (rc) return rc;
-  rc = ctx->prec == ECS_PREC_FP64 ? mg_setup<double>(ctx) : mg_setup<float>(ctx);
+  if (!identity_lhs(ctx)) rc = ctx->prec == ECS_PREC_FP64 ? mg_setup<double>(ctx) : mg_setup<float>(ctx);
   if (rc) return rc;
   ctx->lhs_ready = true;
   return ECS_OK;
@@ -1711,7 +1722,7 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
   }
   ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[0], ctx->stream));
   int rc;
-  if (ctx->use_graphs) {  // the whole solve as one graph launch, one wait
+  if (ctx->use_graphs || identity_lhs(ctx)) {  // the whole solve as one graph launch, one wait
     if ((rc = solve_graph_launch(ctx, rtol, max_it, warm))) return rc;
     RefineDev *hr = (RefineDev *)ctx->rdev_host;
     ECS_CUDA(ctx, cudaMemcpyAsync(hr, ctx->rdev, sizeof(RefineDev), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1749,7 +1760,7 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         zero_guess = false;
       } else {
-        k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, ctx->phi, ctx->rhs, ctx->r64);
+        k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
         ECS_LAUNCHED(ctx);
         if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1805,7 +1816,11 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
 int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y) {
   const EcsParams &p = ctx->p;
   const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
-  k_apply<double><<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, ctx->mom, x, nullptr, y, 0);
+  if (identity_lhs(ctx)) {
+    ECS_CUDA(ctx, cudaMemcpyAsync(y, x, ctx->ncell * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    return ECS_OK;
+  }
+  k_apply<double><<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), x, nullptr, y, 0);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }

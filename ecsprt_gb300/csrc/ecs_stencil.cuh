@@ -68,6 +68,7 @@ struct OpK {
   GridG g;
   double sxx, syy, szz, sod;
   float fxx, fyy, fzz, fod;  // the same scales rounded to FP32 (FP32 rows)
+  int unit;                  // density 1 at every stencil point, ghosts included (-lhs laplacian)
 };
 __device__ __forceinline__ void op_scales(const OpK &o, double &a, double &b, double &c, double &d) {
   a = o.sxx; b = o.syy; c = o.szz; d = o.sod;
@@ -90,6 +91,7 @@ __device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int
   T nmjk = gval(n, g, k, j, i - 1), npjk = gval(n, g, k, j, i + 1);
   T nimk = gval(n, g, k, j - 1, i), nipk = gval(n, g, k, j + 1, i);
   T nijm = gval(n, g, k - 1, j, i), nijp = gval(n, g, k + 1, j, i);
+  if (o.unit) nijk = nmjk = npjk = nimk = nipk = nijm = nijp = T(1);
   T sxx, syy, szz, sod;
   op_scales(o, sxx, syy, szz, sod);
   v[6] = sod * (nipk - npjk);
@@ -134,13 +136,19 @@ __device__ __forceinline__ T zline_rhs_at(const T *__restrict__ n, const T *__re
   return s;
 }
 
-// Operator scale factors for spacing (hx, hy, hz), src/lhs.c:366-375.
+// Operator scale factors for spacing (hx, hy, hz), src/lhs.c:366-375.  The
+// constant-coefficient Laplacian of -lhs laplacian (ComputeLaplacianLHS3D,
+// src/lhs.c:101-191: 1/h^2 off the diagonal, minus their sum on it, the same
+// in boundary rows whose out-of-range columns are dropped) is this operator
+// with kappa = 0, scale = 1 and the density 1 everywhere, ghost points
+// included (`unit`): 2 * (1/(2 h^2)) equals 1/h^2 exactly.
 static inline OpK make_op(const EcsParams &p, int nx, int ny, int nz, double hx, double hy, double hz) {
   OpK o;
   o.g.nx = nx; o.g.ny = ny; o.g.nz = nz;
   for (int d = 0; d < 3; d++) o.g.bc[d] = p.bc[d] == ECS_BC_PERIODIC ? 0 : 1;
   o.g.n = (size_t)nx * ny * nz;
-  double kappa = p.kappa_e, scale = p.scale;
+  const bool lap = p.lhs_type == ECS_LHS_LAPLACIAN;
+  double kappa = lap ? 0.0 : p.kappa_e, scale = lap ? 1.0 : p.scale;
   double hxx = 1.0 / (2.0 * hx * hx), hyy = 1.0 / (2.0 * hy * hy), hzz = 1.0 / (2.0 * hz * hz);
   double hod = 1.0 / (8.0 * hy * hx);
   o.sxx = scale * hxx;
@@ -148,6 +156,7 @@ static inline OpK make_op(const EcsParams &p, int nx, int ny, int nz, double hx,
   o.szz = scale * (1 + kappa * kappa) * hzz;
   o.sod = scale * kappa * hod;
   o.fxx = (float)o.sxx; o.fyy = (float)o.syy; o.fzz = (float)o.szz; o.fod = (float)o.sod;
+  o.unit = lap ? 1 : 0;
   return o;
 }
 static inline GridG make_grid(const EcsParams &p, int nx, int ny, int nz) {

@@ -46,6 +46,9 @@ typedef struct {
   double scale;        /* 1/(1+kappa_e^2) (src/setup.c:230) */
   double cth;          /* gammaT*KB*Te/Q (src/rhs.c:291) */
   double cG;           /* (1+kappa^2)*me*nue/Q (src/rhs.c:292) */
+  double n0;           /* background density (-n0) */
+  int lhs_type;        /* LHSType src/global.h: 0 identity, 1 laplacian, 2 full */
+  int rhs_type;        /* RHSType: 0 constant, 1 sinusoidal, 2 full */
 } OrcParams;
 
 static inline int wrapi(int i, int n) { return ((i % n) + n) % n; }
@@ -294,7 +297,47 @@ static inline double mom(const OrcParams *p, const double *m, int k, int j, int 
   return m[(((size_t)k * p->Ny + j) * p->Nx + i) * 4 + c];
 }
 
+/* Mean removal of MatNullSpaceRemove with the constant null space: b - sum/n. */
+static void null_space_remove(double *b, size_t n) {
+  double s = 0.0;
+  for (size_t e = 0; e < n; e++) s += b[e];
+  s = s / (double)n;
+  for (size_t e = 0; e < n; e++) b[e] -= s;
+}
+
+/* -rhs constant, ComputeConstantRHS src/rhs.c:6-23: b = n0 * scale. */
+static void rhs_constant(const OrcParams *p, double *b) {
+  size_t n = (size_t)p->Nx * p->Ny * p->Nz;
+  double val = p->n0 * p->scale;
+  for (size_t e = 0; e < n; e++) b[e] = val;
+}
+
+/* -rhs sinusoidal, ComputeSinusoidalRHS3D src/rhs.c:82-148: at the cell
+   centres x = (i + 0.5) dx (grid units), b = n0 cos(2 pi x) cos(2 pi y)
+   cos(2 pi z) scale, then the constant null space removed. */
+static void rhs_sinusoidal(const OrcParams *p, double *b) {
+  const double PI = 3.141592653589793238462643383279502884;
+  for (int k = 0; k < p->Nz; k++)
+    for (int j = 0; j < p->Ny; j++)
+      for (int i = 0; i < p->Nx; i++) {
+        double x = ((double)i + 0.5) * p->dx, y = ((double)j + 0.5) * p->dy, z = ((double)k + 0.5) * p->dz;
+        double Cx = cos(2 * PI * x), Cy = cos(2 * PI * y), Cz = cos(2 * PI * z);
+        double val = Cx * Cy * Cz;
+        b[((size_t)k * p->Ny + j) * p->Nx + i] = p->n0 * val * p->scale;
+      }
+  null_space_remove(b, (size_t)p->Nx * p->Ny * p->Nz);
+}
+
+static int rhs_full(const OrcParams *p, const double *m, double *b);
+
+/* RHS by -rhs type (the ctx->potential.rhs binding of src/setup.c:63-90). */
 int orc_rhs(const OrcParams *p, const double *m, double *b) {
+  if (p->rhs_type == 0) { rhs_constant(p, b); return 0; }
+  if (p->rhs_type == 1) { rhs_sinusoidal(p, b); return 0; }
+  return rhs_full(p, m, b);
+}
+
+static int rhs_full(const OrcParams *p, const double *m, double *b) {
   double kappa = p->kappa_e;
   double hx = 1.0 / (2.0 * p->dx), hy = 1.0 / (2.0 * p->dy), hz = 1.0 / (2.0 * p->dz);
   double hxx = 1.0 / (p->dx * p->dx), hyy = 1.0 / (p->dy * p->dy), hzz = 1.0 / (p->dz * p->dz);
@@ -340,7 +383,24 @@ static inline double dens(const OrcParams *p, const double *n, int k, int j, int
   return node_val(p, n, k, j, i);
 }
 
+/* Rows of -lhs identity (ComputeIdentityLHS src/lhs.c:11-23: A = I) and
+   -lhs laplacian (ComputeLaplacianLHS3D src/lhs.c:101-191: 1/h^2 off the
+   diagonal, the diagonal minus their sum in insertion order) in the 11-entry
+   layout; the corner entries stay 0. */
+static int lhs_row_simple(const OrcParams *p, double v[11]) {
+  for (int e = 0; e < 11; e++) v[e] = 0.0;
+  if (p->lhs_type == 0) { v[10] = 1.0; return 1; }
+  if (p->lhs_type != 1) return 0;
+  double vpjk = 1.0 / (p->dx * p->dx), vmjk = 1.0 / (p->dx * p->dx);
+  double vipk = 1.0 / (p->dy * p->dy), vimk = 1.0 / (p->dy * p->dy);
+  double vijp = 1.0 / (p->dz * p->dz), vijm = 1.0 / (p->dz * p->dz);
+  v[0] = vpjk; v[1] = vmjk; v[2] = vipk; v[3] = vimk; v[4] = vijp; v[5] = vijm;
+  v[10] = -(vpjk + vipk + vijp + vmjk + vimk + vijm);
+  return 1;
+}
+
 void orc_lhs_row(const OrcParams *p, const double *n, int k, int j, int i, double v[11]) {
+  if (lhs_row_simple(p, v)) return;
   double kappa = p->kappa_e, scale = p->scale;
   double hxx = 1.0 / (2.0 * p->dx * p->dx);
   double hyy = 1.0 / (2.0 * p->dy * p->dy);

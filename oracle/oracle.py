@@ -30,6 +30,7 @@ class OrcParams(C.Structure):
         ("nui", C.c_double), ("viT", C.c_double), ("vi0", C.c_double * 3),
         ("mn", C.c_double), ("vnT", C.c_double), ("vn0", C.c_double * 3), ("vn0mag", C.c_double),
         ("kappa_e", C.c_double), ("scale", C.c_double), ("cth", C.c_double), ("cG", C.c_double),
+        ("n0", C.c_double), ("lhs_type", C.c_int), ("rhs_type", C.c_int),
     ]
 
 
@@ -92,6 +93,7 @@ def from_ref_context(d: dict) -> dict:
     src/rhs.c:291-292 evaluated in the same order."""
     out = dict(d)
     out["bc"] = [int(d["xBC"]), int(d["yBC"]), int(d["zBC"])]
+    out["lhs_type"], out["rhs_type"] = int(d["lhsType"]), int(d["rhsType"])
     out["cth"] = d["gammaT"] * KB * d["Te"] / Q
     out["cG"] = (1 + d["kappa_e"] * d["kappa_e"]) * d["me"] * d["nue"] / Q
     return out
@@ -108,8 +110,9 @@ def params_from(p) -> OrcParams:
     for d in range(3):
         o.bc[d] = 0 if int(bc[d]) == 0 else 1
     for k in ("dx", "dy", "dz", "x0", "y0", "z0", "x1", "y1", "z1", "Lx", "Ly", "Lz",
-              "qi", "mi", "B0", "E0", "nui", "viT", "mn", "vnT", "kappa_e", "scale", "cth", "cG"):
+              "qi", "mi", "B0", "E0", "nui", "viT", "mn", "vnT", "kappa_e", "scale", "cth", "cG", "n0"):
         setattr(o, k, float(g(k)))
+    o.lhs_type, o.rhs_type = int(g("lhs_type")), int(g("rhs_type"))
     o.vi0[0], o.vi0[1], o.vi0[2] = float(g("vi0x")), float(g("vi0y")), float(g("vi0z"))
     o.vn0[0], o.vn0[1], o.vn0[2] = float(g("vn0x")), float(g("vn0y")), float(g("vn0z"))
     o.vn0mag = float(g("vn0"))

@@ -188,7 +188,7 @@ PetscErrorCode PetscOptionsGetEnum(PetscOptions o, const char pre[], const char 
   *set = PETSC_FALSE;
   if (k < 0) return 0;
   while (list[n]) n++;
-  n -= 3; /* trailing entries: enum type name, prefix, NULL */
+  n -= 2; /* trailing entries before the NULL: enum type name, prefix */
   for (int i = 0; i < n; i++) {
     if (g_vals[k] && !strcasecmp(g_vals[k], list[i])) {
       *v = i;

@@ -21,6 +21,10 @@ Cases:
        kappa_e ~ 88) on tests/grid3D.ini spacing (dx = 0.5) at 16^3, one ion
        per cell, dt = 1e-5 as in tests/test_all.sh.
   rng  ran1 / ran3 / gasdev streams and Sobol points from a fresh process.
+  ops  the other operator options on a 6x5x4 grid (dx = 0.1, dy = 0.125,
+       dz = 0.2, n0 = 2.5): RHS and dense LHS of -lhs laplacian -rhs
+       sinusoidal, of -lhs laplacian -rhs constant with a reflecting z, of
+       -lhs identity -rhs constant, and of -lhs full -rhs sinusoidal.
 """
 from __future__ import annotations
 
@@ -173,7 +177,31 @@ def case_rng():
     return out
 
 
-CASES = {"c1": case_c1, "edge": case_edge, "fb": case_fb, "rng": case_rng}
+OPS_BASE = "-Nx 6 -Ny 5 -Nz 4 -dx 0.1 -dy 0.125 -dz 0.2 -n0 2.5 " + C1_PHYS
+OPS_VARIANTS = {
+    "lap_sin": "-lhs laplacian -rhs sinusoidal",
+    "lap_const_zrefl": "-lhs laplacian -rhs constant -zBC inject-reflect",
+    "id_const": "-lhs identity -rhs constant",
+    "full_sin": "-lhs full -rhs sinusoidal",
+}
+
+
+def case_ops():
+    out = {"opts_base": OPS_BASE, "variants": json.dumps(OPS_VARIANTS)}
+    for name, extra in OPS_VARIANTS.items():
+        R = refmod.Ref(OPS_BASE + extra, 8)
+        if name == "full_sin":  # a density for the variable-coefficient operator
+            m = np.zeros(R.shape + (4,))
+            m[..., 0] = 2.0 + smooth_phi(R.shape, 21, amp=0.3)
+            R.set_moments(m)
+            out["full_sin_density"] = m[..., 0]
+        out[f"{name}_rhs"] = R.rhs()
+        out[f"{name}_lhs"] = R.lhs_dense()
+        out[f"{name}_params"] = json.dumps(R.params)
+    return out
+
+
+CASES = {"c1": case_c1, "edge": case_edge, "fb": case_fb, "rng": case_rng, "ops": case_ops}
 
 
 def main():

@@ -122,3 +122,24 @@ def test_collisions_bit_exact(O, golden, case):
         assert ns == O[case].collision_count(v.shape[0], float(g["dt"]))
         c += 1
     assert c > 1
+
+
+OPS_VARIANTS = ("lap_sin", "lap_const_zrefl", "id_const", "full_sin")
+
+
+@pytest.mark.parametrize("variant", OPS_VARIANTS)
+def test_operator_options_bit_exact(built, variant):
+    """-lhs identity / laplacian and -rhs constant / sinusoidal (src/lhs.c:11-191,
+    src/rhs.c:6-148) against the reference's own RHS vectors and assembled
+    matrices, bit for bit."""
+    import json
+
+    from conftest import GOLDEN
+    d = np.load(GOLDEN / "ops.npz")
+    params = json.loads(str(d[f"{variant}_params"]))
+    O = orc.Oracle(params)
+    dens = d["full_sin_density"] if variant == "full_sin" else np.zeros(O.shape)
+    m = np.zeros(O.shape + (4,))
+    m[..., 0] = dens
+    eq(O.rhs(m), d[f"{variant}_rhs"])
+    eq(O.lhs_dense(dens), d[f"{variant}_lhs"])
