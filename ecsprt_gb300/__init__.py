@@ -183,6 +183,7 @@ class Context:
         self._h = h
         self.ncell = params.Nx * params.Ny * params.Nz
         self.shape = (params.Nz, params.Ny, params.Nx)
+        self.nd = 2 if params.ndim == 2 else 3  # components an ion in host arrays
 
     # ---- plumbing --------------------------------------------------------
     def _check(self, rc: int):
@@ -229,8 +230,8 @@ class Context:
 
     # ---- data ----------------------------------------------------------
     def upload_particles(self, pos: np.ndarray, vel: np.ndarray):
-        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
-        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, self.nd)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, self.nd)
         if pos.shape != vel.shape:
             raise EcsError(_lib.ECS_ERR_INVALID, "pos and vel differ in shape")
         self._check(self._lib.ecs_particles_upload(self._h, _ptr(pos), _ptr(vel), pos.shape[0]))
@@ -247,8 +248,8 @@ class Context:
 
     def download_particles(self):
         n = int(self._lib.ecs_particles_count(self._h))
-        pos = np.empty((n, 3))
-        vel = np.empty((n, 3))
+        pos = np.empty((n, self.nd))
+        vel = np.empty((n, self.nd))
         self._check(self._lib.ecs_particles_download(self._h, _ptr(pos), _ptr(vel)))
         return pos, vel
 
@@ -429,10 +430,11 @@ class Server:
                    step_seconds: np.ndarray | None = None, phi_out: np.ndarray | None = None,
                    pos_out: np.ndarray | None = None, vel_out: np.ndarray | None = None) -> int:
         n = pos.shape[0]
-        _f64(pos, (n, 3), name="pos")
-        _f64(vel, (n, 3), name="vel")
+        nd = 2 if params.ndim == 2 else 3
+        _f64(pos, (n, nd), name="pos")
+        _f64(vel, (n, nd), name="vel")
         outs = {"step_seconds": (step_seconds, (int(nsteps),)), "phi_out": (phi_out, (params.Nz, params.Ny, params.Nx)),
-                "pos_out": (pos_out, (n, 3)), "vel_out": (vel_out, (n, 3))}
+                "pos_out": (pos_out, (n, nd)), "vel_out": (vel_out, (n, nd))}
         ptrs = {}
         for k, (a, shp) in outs.items():
             ptrs[k] = None

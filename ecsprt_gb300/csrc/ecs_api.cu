@@ -43,12 +43,18 @@ unsigned int blocks(const EcsCtx *ctx, size_t n) {
 
 int validate(const EcsParams *p) {
   if (!p) return ecs_fail(nullptr, ECS_ERR_INVALID, "params is NULL");
-  if (p->ndim != 3) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "ndim %d: the GPU path is 3-D", p->ndim);
-  if (p->Nx < 4 || p->Ny < 4 || p->Nz < 4 || p->Nx > 1024 || p->Ny > 1024 || p->Nz > 1024)
-    return ecs_fail(nullptr, ECS_ERR_INVALID, "grid %dx%dx%d outside 4..1024 per axis", p->Nx, p->Ny, p->Nz);
-  if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return ecs_fail(nullptr, ECS_ERR_INVALID, "non-positive cell width");
+  if (p->ndim != 3 && p->ndim != 2) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "ndim %d", p->ndim);
+  const bool flat = p->ndim == 2;
+  if (p->Nx < 4 || p->Ny < 4 || p->Nx > 1024 || p->Ny > 1024 || (flat ? p->Nz != 1 : (p->Nz < 4 || p->Nz > 1024)))
+    return ecs_fail(nullptr, ECS_ERR_INVALID, "grid %dx%dx%d outside 4..1024 per axis (Nz = 1 for ndim 2)", p->Nx,
+                    p->Ny, p->Nz);
+  if (!(p->dx > 0 && p->dy > 0 && (flat || p->dz > 0))) return ecs_fail(nullptr, ECS_ERR_INVALID, "non-positive cell width");
+  // ScatterElastic reads the relative velocity's z component (src/collisions.c:104),
+  // which a 2-D run never sets (src/collisions.c:78-83): undefined in the reference.
+  if (flat && p->mn > 0.0)
+    return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "2-D collisions are undefined in the reference; use -mn 0 with -ndim 2");
   if (!(p->mi > 0)) return ecs_fail(nullptr, ECS_ERR_INVALID, "non-positive ion mass");
-  for (int d = 0; d < 3; d++) {
+  for (int d = 0; d < (flat ? 2 : 3); d++) {
     if (p->bc[d] == ECS_BC_INJECT_ADVECT) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "inject-advect boundaries are not implemented");
     if (p->bc[d] == ECS_BC_INJECT_REFLECT && d != 2) return ecs_fail(nullptr, ECS_ERR_UNSUPPORTED, "reflecting boundaries are supported on z only");
   }
@@ -138,6 +144,13 @@ int ecs_ctx_create(const EcsParams *params, int precision, int64_t np_capacity, 
   EcsCtx *ctx = new (std::nothrow) EcsCtx();
   if (!ctx) return ecs_fail(nullptr, ECS_ERR_NOMEM, "host allocation failed");
   ctx->p = *params;
+  if (params->ndim == 2) {
+    // 2-D runs on a one-cell-deep grid with the ions at z = 0: a unit z cell,
+    // periodic, so that every z term is exactly zero rather than 0/0 (the
+    // reference's 2-D context has dz = Lz = 0).
+    ctx->p.dz = 1.0; ctx->p.Lz = 1.0; ctx->p.z0 = 0.0; ctx->p.z1 = 1.0;
+    ctx->p.bc[2] = ECS_BC_PERIODIC;
+  }
   ctx->prec = precision;
   ctx->cap = np_capacity;
   ctx->ncell = (size_t)params->Nx * params->Ny * params->Nz;

@@ -103,8 +103,8 @@ __global__ void k_rhs(GridG g, RhsK r, const double *__restrict__ mom, double *_
 // x) cos(2 pi y) cos(2 pi z) scale at the cell centres x = (i + 1/2) dx (in
 // the grid's own units, as the reference), block partials for the mean that
 // MatNullSpaceRemove takes out (src/rhs.c:138-141).
-__global__ void k_rhs_sin(GridG g, double dx, double dy, double dz, double n0, double scale, double *__restrict__ b,
-                          double *__restrict__ partial) {
+__global__ void k_rhs_sin(GridG g, int ndim, double dx, double dy, double dz, double n0, double scale,
+                          double *__restrict__ b, double *__restrict__ partial) {
   __shared__ double sh[kTx * kTy / 32];
   double local = 0.0;
   int i, j, k0;
@@ -113,8 +113,11 @@ __global__ void k_rhs_sin(GridG g, double dx, double dy, double dz, double n0, d
     const double cx = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)i, 0.5), dx)));
     const double cy = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)j, 0.5), dy)));
     for (int k = k0; k < g.nz; k += gridDim.z) {
-      const double cz = cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)k, 0.5), dz)));
-      const double v = __dmul_rn(__dmul_rn(n0, __dmul_rn(__dmul_rn(cx, cy), cz)), scale);
+      // 2-D (ComputeSinusoidalRHS2D src/rhs.c:26-79): n0 Cx Cy scale
+      const double cxy = __dmul_rn(cx, cy);
+      const double val =
+          ndim == 2 ? cxy : __dmul_rn(cxy, cos(__dmul_rn(twopi, __dmul_rn(__dadd_rn((double)k, 0.5), dz))));
+      const double v = __dmul_rn(__dmul_rn(n0, val), scale);
       b[lin3(g, i, j, k)] = v;
       local += v;
     }
@@ -201,7 +204,7 @@ int ecs_grid_rhs(EcsCtx *ctx) {
   grid.z = std::max(1u, std::min(grid.z, (unsigned)ctx->nred / plane_blocks));
   const int nb = (int)(grid.x * grid.y * grid.z);
   if (p.rhs_type == ECS_RHS_SINUSOIDAL) {
-    k_rhs_sin<<<grid, threads3(), 0, ctx->stream>>>(g, p.dx, p.dy, p.dz, p.n0, p.scale, ctx->rhs, ctx->red);
+    k_rhs_sin<<<grid, threads3(), 0, ctx->stream>>>(g, p.ndim, p.dx, p.dy, p.dz, p.n0, p.scale, ctx->rhs, ctx->red);
   } else {
     RhsK r;
     r.kappa = p.kappa_e;

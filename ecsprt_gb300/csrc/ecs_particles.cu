@@ -143,6 +143,7 @@ __device__ __forceinline__ long long full_sum(const long long *row, const FixSca
 
 
 struct PartK {
+  int ndim;  // 2: ions in the z = 0 plane of a one-cell-deep grid (-ndim 2)
   int Nx, Ny, Nz;
   int bc[3];
   size_t ncell;
@@ -434,7 +435,8 @@ __device__ __forceinline__ void flush_samples(EcsDevStatus *st, float sample, bo
 
 // Difference numerators at the 8 corners, interpolated with the reference's
 // weight order (src/vector-math.c:645-651): along y with wyh, across the z
-// pair with wxh, across the x pair with wzh.
+// pair with wxh, across the x pair with wzh.  In 2-D the four corners of the
+// z = 0 plane, along y with wyh, across x with wxh.
 __device__ __forceinline__ void gather64(const double4_32a *__restrict__ E, const PartK &k, int i,
                                          int j, int kk, rd wx, rd wy, rd wz, rd f[3]) {
   const size_t sx = (size_t)k.Nx + 1, sxy = sx * ((size_t)k.Ny + 1);
@@ -458,6 +460,10 @@ __device__ __forceinline__ void gather64(const double4_32a *__restrict__ E, cons
     rd a01 = v[1] + wy * (v[3] - v[1]);
     rd a10 = v[4] + wy * (v[6] - v[4]);
     rd a11 = v[5] + wy * (v[7] - v[5]);
+    if (k.ndim == 2) {  // DifferenceVector2D src/vector-math.c:576-591: bilinear, no swap
+      f[c] = c == 2 ? rd{0.0} : a00 + wx * (a01 - a00);
+      continue;
+    }
     rd c0 = a00 + wx * (a10 - a00);
     rd c1 = a01 + wx * (a11 - a01);
     f[c] = c0 + wz * (c1 - c0);
@@ -666,10 +672,28 @@ __device__ __forceinline__ void interp8(const float4 (&D)[8], float wx, float wy
     f[c] = c0 + wz * (c1 - c0);
   }
 }
+// The same in 2-D (four corners of the z = 0 plane, as gather64).
+__device__ __forceinline__ void interp4(const float4 (&D)[8], float wx, float wy, float f[3]) {
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const float v0 = c == 0 ? D[0].x : D[0].y, v1 = c == 0 ? D[1].x : D[1].y;
+    const float v2 = c == 0 ? D[2].x : D[2].y, v3 = c == 0 ? D[3].x : D[3].y;
+    const float a00 = v0 + wy * (v2 - v0);
+    const float a01 = v1 + wy * (v3 - v1);
+    f[c] = a00 + wx * (a01 - a00);
+  }
+  f[2] = 0.0f;
+}
 __device__ __forceinline__ void gather32(const float4 *__restrict__ E, const PartK &k, int i, int j, int kk,
                                          float wx, float wy, float wz, float f[3]) {
   const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1), base = kk * sxy + j * sx + i;
   float4 D[8];
+  if (k.ndim == 2) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) D[b] = __ldg(&E[corner_at(base, sx, sxy, b)]);
+    interp4(D, wx, wy, f);
+    return;
+  }
 #pragma unroll
   for (int b = 0; b < 8; b++) D[b] = __ldg(&E[corner_at(base, sx, sxy, b)]);
   interp8(D, wx, wy, wz, f);
@@ -959,22 +983,25 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
 }
 
 // ---- upload / download conversions ---------------------------------------------
-__global__ void k_aos_to_soa64(int64_t n, const double *__restrict__ pos,
+// Host AoS arrays have nd components an ion (3, or 2 for -ndim 2, whose ions
+// sit at z = 0 with vz = 0 on the device).
+__global__ void k_aos_to_soa64(int64_t n, int nd, const double *__restrict__ pos,
                                const double *__restrict__ vel, double *px, double *py,
                                double *pz, double *vx, double *vy, double *vz) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    px[i] = pos[3 * i]; py[i] = pos[3 * i + 1]; pz[i] = pos[3 * i + 2];
-    vx[i] = vel[3 * i]; vy[i] = vel[3 * i + 1]; vz[i] = vel[3 * i + 2];
+    px[i] = pos[nd * i]; py[i] = pos[nd * i + 1]; pz[i] = nd == 3 ? pos[3 * i + 2] : 0.0;
+    vx[i] = vel[nd * i]; vy[i] = vel[nd * i + 1]; vz[i] = nd == 3 ? vel[3 * i + 2] : 0.0;
   }
 }
-__global__ void k_soa_to_aos64(int64_t n, double *__restrict__ pos, double *__restrict__ vel,
+__global__ void k_soa_to_aos64(int64_t n, int nd, double *__restrict__ pos, double *__restrict__ vel,
                                const double *px, const double *py, const double *pz,
                                const double *vx, const double *vy, const double *vz) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    pos[3 * i] = px[i]; pos[3 * i + 1] = py[i]; pos[3 * i + 2] = pz[i];
-    vel[3 * i] = vx[i]; vel[3 * i + 1] = vy[i]; vel[3 * i + 2] = vz[i];
+    pos[nd * i] = px[i]; pos[nd * i + 1] = py[i];
+    vel[nd * i] = vx[i]; vel[nd * i + 1] = vy[i];
+    if (nd == 3) { pos[3 * i + 2] = pz[i]; vel[3 * i + 2] = vz[i]; }
   }
 }
 
@@ -991,30 +1018,33 @@ __device__ __forceinline__ int to_cell(double pos, double d, int N, float &o) {
   return c;
 }
 
-__global__ void k_aos_to_mixed(int64_t n, PartK k, const double *__restrict__ pos,
+__global__ void k_aos_to_mixed(int64_t n, int nd, PartK k, const double *__restrict__ pos,
                                const double *__restrict__ vel, float4 *__restrict__ ions) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    float a, b, c;
-    int ci = to_cell(pos[3 * i], k.dx, k.Nx, a);
-    int cj = to_cell(pos[3 * i + 1], k.dy, k.Ny, b);
-    int ck = to_cell(pos[3 * i + 2], k.dz, k.Nz, c);
-    store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[3 * i], (float)vel[3 * i + 1],
-                        (float)vel[3 * i + 2]});
+    float a, b, c = 0.0f;
+    int ci = to_cell(pos[nd * i], k.dx, k.Nx, a);
+    int cj = to_cell(pos[nd * i + 1], k.dy, k.Ny, b);
+    int ck = nd == 3 ? to_cell(pos[3 * i + 2], k.dz, k.Nz, c) : 0;
+    store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[nd * i], (float)vel[nd * i + 1],
+                        nd == 3 ? (float)vel[3 * i + 2] : 0.0f});
   }
 }
 
-__global__ void k_mixed_to_aos(int64_t n, PartK k, double *__restrict__ pos,
+__global__ void k_mixed_to_aos(int64_t n, int nd, PartK k, double *__restrict__ pos,
                                double *__restrict__ vel, const float4 *__restrict__ ions) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const Ion q = load_ion(ions, i);
     int ci, cj, ck;
     unpack_cell(q.c, ci, cj, ck);
-    pos[3 * i] = ((double)ci + (double)q.ox) * k.dx;
-    pos[3 * i + 1] = ((double)cj + (double)q.oy) * k.dy;
-    pos[3 * i + 2] = ((double)ck + (double)q.oz) * k.dz;
-    vel[3 * i] = q.vx; vel[3 * i + 1] = q.vy; vel[3 * i + 2] = q.vz;
+    pos[nd * i] = ((double)ci + (double)q.ox) * k.dx;
+    pos[nd * i + 1] = ((double)cj + (double)q.oy) * k.dy;
+    vel[nd * i] = q.vx; vel[nd * i + 1] = q.vy;
+    if (nd == 3) {
+      pos[3 * i + 2] = ((double)ck + (double)q.oz) * k.dz;
+      vel[3 * i + 2] = q.vz;
+    }
   }
 }
 
@@ -1171,6 +1201,7 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   const EcsParams &p = ctx->p;
   PartK k;
   memset(&k, 0, sizeof k);
+  k.ndim = p.ndim;
   k.Nx = p.Nx; k.Ny = p.Ny; k.Nz = p.Nz;
   for (int d = 0; d < 3; d++) k.bc[d] = p.bc[d] == ECS_BC_PERIODIC ? ECS_BC_PERIODIC : ECS_BC_INJECT_REFLECT;
   k.ncell = ctx->ncell;
@@ -1356,6 +1387,7 @@ __global__ void k_init_ions(InitK ik, PartK k, int64_t n, int fp64, float4 *__re
       if (pos[d] >= ik.L[d]) pos[d] = nextafter(ik.L[d], 0.0);
     }
     init_velocity(ik, i, vel);
+    if (k.ndim == 2) pos[2] = vel[2] = 0.0;
     if (fp64) {
       px[i] = pos[0]; py[i] = pos[1]; pz[i] = pos[2];
       vx[i] = vel[0]; vy[i] = vel[1]; vz[i] = vel[2];
@@ -1440,6 +1472,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
   int rc = ensure_xfer(ctx);
   if (rc) return rc;
   const int64_t chunk = ctx->stage_n;
+  const int nd = ctx->p.ndim == 2 ? 2 : 3;  // components an ion in the host arrays
   PartK k = make_k(ctx, 0.0);
   // the previous contents of the ion buffer may still be in use
   ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
@@ -1450,16 +1483,16 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
     const int64_t n = np - off < chunk ? np - off : chunk;
     double *st = ctx->stage[q];
     if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));  // buffer q free
-    ECS_CUDA(ctx, cudaMemcpyAsync(st, pos + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
-    ECS_CUDA(ctx, cudaMemcpyAsync(st + 3 * n, vel + 3 * off, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaMemcpyAsync(st, pos + nd * off, (size_t)n * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaMemcpyAsync(st + nd * n, vel + nd * off, (size_t)n * nd * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
     ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_copy[q], 0));
     unsigned int g = grid_blocks(ctx, n, 8);
     if (ctx->prec == ECS_PREC_FP64) {
-      k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, st, st + 3 * n, ctx->px + off, ctx->py + off,
+      k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, nd, st, st + nd * n, ctx->px + off, ctx->py + off,
                                                    ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, k, st, st + 3 * n, ctx->ions[ctx->cur] + 2 * off);
+      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, nd, k, st, st + nd * n, ctx->ions[ctx->cur] + 2 * off);
     }
     ECS_LAUNCHED(ctx);
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
@@ -1550,6 +1583,7 @@ int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
   int rc = ensure_xfer(ctx);
   if (rc) return rc;
   const int64_t chunk = ctx->stage_n;
+  const int nd = ctx->p.ndim == 2 ? 2 : 3;
   const int64_t np = ctx->np;
   PartK k = make_k(ctx, 0.0);
   ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
@@ -1562,16 +1596,16 @@ int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
     if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_copy[q], 0));  // buffer q copied out
     unsigned int g = grid_blocks(ctx, n, 8);
     if (ctx->prec == ECS_PREC_FP64) {
-      k_soa_to_aos64<<<g, kBlock, 0, ctx->xs[0]>>>(n, st, st + 3 * n, ctx->px + off, ctx->py + off,
+      k_soa_to_aos64<<<g, kBlock, 0, ctx->xs[0]>>>(n, nd, st, st + nd * n, ctx->px + off, ctx->py + off,
                                                   ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      k_mixed_to_aos<<<g, kBlock, 0, ctx->xs[0]>>>(n, k, st, st + 3 * n, ctx->ions[ctx->cur] + 2 * off);
+      k_mixed_to_aos<<<g, kBlock, 0, ctx->xs[0]>>>(n, nd, k, st, st + nd * n, ctx->ions[ctx->cur] + 2 * off);
     }
     ECS_LAUNCHED(ctx);
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->xs[0]));
     ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));
-    if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + 3 * off, st, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
-    if (vel) ECS_CUDA(ctx, cudaMemcpyAsync(vel + 3 * off, st + 3 * n, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
+    if (pos) ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * off, st, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
+    if (vel) ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * off, st + nd * n, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[1]));
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
   }
   return ECS_OK;
@@ -1691,8 +1725,11 @@ int ecs_part_collide(EcsCtx *ctx, double dt) {
 }
 
 // Whether the pass that moves the ions now is followed by a cell sort.
+// The tile kernel's windows are 3-D, so 2-D ions stay unsorted (order-free
+// kernel).
 static bool sort_due(const EcsCtx *ctx) {
-  return ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && ctx->steps_since_sort + 1 >= ctx->sort_every;
+  return ctx->prec == ECS_PREC_MIXED && ctx->p.ndim == 3 && ctx->sort_every > 0 &&
+         ctx->steps_since_sort + 1 >= ctx->sort_every;
 }
 
 // Scan of the cell counts and the scatter into the other buffer.
@@ -1764,7 +1801,7 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
 
 // Full counting sort (count pass included), used after an upload.
 int ecs_part_sort(EcsCtx *ctx) {
-  if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0) return ECS_OK;
+  if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0 || ctx->p.ndim != 3) return ECS_OK;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
   const PartK k = make_k(ctx, 0.0);
   k_sort_count<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, k.tg, ctx->ions[ctx->cur],

@@ -100,7 +100,8 @@ __global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z, int S) {
   if (col >= ncol) return;
   const int i = col % g.nx, j = col / g.nx;
   const size_t plane = (size_t)g.nx * g.ny;
-  const bool cyc = g.bc[2] == 0;
+  // a one-cell column (2-D) has no z coupling: the plain solve, no periodic closure
+  const bool cyc = g.bc[2] == 0 && g.nz > 1;
   const int N = g.nz;
   T v[11];
   row11(n, o, i, j, 0, v);
@@ -944,10 +945,16 @@ int mg_alloc(EcsCtx *ctx) {
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_a0g, (size_t)nx * ny * sizeof(T)));
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_qden, (size_t)nx * ny * sizeof(T)));
     mg.lv.push_back(L);
-    bool even = (nx % 2 == 0) && (ny % 2 == 0) && (nz % 2 == 0);
-    if (!even || std::min(nx, std::min(ny, nz)) < 8 || mg.lv.size() >= 12) break;
-    nx /= 2; ny /= 2; nz /= 2;
-    hx *= 2; hy *= 2; hz *= 2;
+    // a 2-D grid (nz = 1) coarsens in x and y only
+    const bool flat = nz == 1;
+    bool even = (nx % 2 == 0) && (ny % 2 == 0) && (flat || nz % 2 == 0);
+    if (!even || std::min(nx, std::min(ny, flat ? nx : nz)) < 8 || mg.lv.size() >= 12) break;
+    nx /= 2; ny /= 2;
+    hx *= 2; hy *= 2;
+    if (!flat) {
+      nz /= 2;
+      hz *= 2;
+    }
   }
   const size_t nc = mg.lv.back().n;
   if (nc <= (size_t)kDirectMax) {

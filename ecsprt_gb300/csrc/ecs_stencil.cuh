@@ -153,7 +153,9 @@ static inline OpK make_op(const EcsParams &p, int nx, int ny, int nz, double hx,
   double hod = 1.0 / (8.0 * hy * hx);
   o.sxx = scale * hxx;
   o.syy = scale * hyy;
-  o.szz = scale * (1 + kappa * kappa) * hzz;
+  // 2-D (ComputeFullLHS2D src/lhs.c:194-335, ComputeLaplacianLHS2D
+  // src/lhs.c:26-97): the same in-plane entries, no z coupling
+  o.szz = p.ndim == 2 ? 0.0 : scale * (1 + kappa * kappa) * hzz;
   o.sod = scale * kappa * hod;
   o.fxx = (float)o.sxx; o.fyy = (float)o.syy; o.fzz = (float)o.szz; o.fod = (float)o.sod;
   o.unit = lap ? 1 : 0;

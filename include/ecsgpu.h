@@ -110,7 +110,10 @@ const char *ecs_last_error(const EcsCtx *ctx);
 
 /* ---- context lifecycle -------------------------------------------------- */
 /* np_capacity bounds the ion count; stream is a cudaStream_t (NULL: the
-   context creates its own non-blocking stream). */
+   context creates its own non-blocking stream).  ndim = 2 (-ndim 2:
+   BorisMoverBz2D, Collect2DFluidMoments, ComputeFullLHS2D/RHS2D) takes
+   Nz = 1 and no collisions (the reference's ScatterElastic reads an unset
+   z component in 2-D): ECS_ERR_UNSUPPORTED when mn > 0. */
 int ecs_ctx_create(const EcsParams *params, int precision, int64_t np_capacity,
                    void *stream, EcsCtx **out);
 int ecs_ctx_destroy(EcsCtx *ctx);
@@ -130,7 +133,8 @@ int ecs_set_warm_start(EcsCtx *ctx, int warm);
 int ecs_set_solver_graphs(EcsCtx *ctx, int on);
 
 /* ---- particles (host arrays in the reference's DMSwarm layout) ---------- */
-/* pos/vel are AoS FP64: pos[ip*3+d], vel[ip*3+d] (src/velocities.c:342-356). */
+/* pos/vel are AoS FP64: pos[ip*ndim+d], vel[ip*ndim+d] (src/velocities.c:342-356;
+   ndim = 2 for -ndim 2, src/velocities.c:254-266). */
 int ecs_particles_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
 int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel);
 int64_t ecs_particles_count(const EcsCtx *ctx);

@@ -49,6 +49,7 @@ typedef struct {
   double n0;           /* background density (-n0) */
   int lhs_type;        /* LHSType src/global.h: 0 identity, 1 laplacian, 2 full */
   int rhs_type;        /* RHSType: 0 constant, 1 sinusoidal, 2 full */
+  int ndim;            /* 2 or 3; a 2-D grid is [1][Ny][Nx] */
 } OrcParams;
 
 static inline int wrapi(int i, int n) { return ((i % n) + n) % n; }
@@ -287,6 +288,174 @@ int orc_collect_fixed(const OrcParams *p, int np, const double *pos, const doubl
 }
 
 /* ------------------------------------------------------------------------ */
+/* 2-D particle phase (-ndim 2): positions and velocities are [np][2].       */
+/* ------------------------------------------------------------------------ */
+/* DifferenceVector2D src/vector-math.c:529-593: bilinear, no weight swap,   */
+/* the backward difference at index N as in 3-D.                             */
+static void difference_vector2d(const OrcParams *p, const double *F, double x0, double y0, double f[2]) {
+  int Nx = p->Nx, Ny = p->Ny;
+  int ixl = (int)x0, ixh = ixl + 1, iyl = (int)y0, iyh = iyl + 1;
+  double wxh = x0 - (double)ixl, wyh = y0 - (double)iyl;
+  double hh, lh, hl, ll, Ewh, Ewl;
+#define PHI2(j, i) node_val(p, F, 0, (j), (i))
+  if (ixl >= 0) {
+    hl = PHI2(iyh, ixl + 1) - PHI2(iyh, ixl - 1);
+    ll = PHI2(iyl, ixl + 1) - PHI2(iyl, ixl - 1);
+  } else {
+    hl = -1.0 * PHI2(iyh, ixl + 2) + 4.0 * PHI2(iyh, ixl + 1) - 3.0 * PHI2(iyh, ixl);
+    ll = -1.0 * PHI2(iyl, ixl + 2) + 4.0 * PHI2(iyl, ixl + 1) - 3.0 * PHI2(iyl, ixl);
+  }
+  if (ixh < Nx) {
+    hh = PHI2(iyh, ixh + 1) - PHI2(iyh, ixh - 1);
+    lh = PHI2(iyl, ixh + 1) - PHI2(iyl, ixh - 1);
+  } else {
+    hh = +3.0 * PHI2(iyh, ixh) - 4.0 * PHI2(iyh, ixh - 1) + 1.0 * PHI2(iyh, ixh - 2);
+    lh = +3.0 * PHI2(iyl, ixh) - 4.0 * PHI2(iyl, ixh - 1) + 1.0 * PHI2(iyl, ixh - 2);
+  }
+  Ewh = lh + wyh * (hh - lh);
+  Ewl = ll + wyh * (hl - ll);
+  f[0] = Ewl + wxh * (Ewh - Ewl);
+  if (iyl >= 0) {
+    lh = PHI2(iyl + 1, ixh) - PHI2(iyl - 1, ixh);
+    ll = PHI2(iyl + 1, ixl) - PHI2(iyl - 1, ixl);
+  } else {
+    lh = -1.0 * PHI2(iyl + 2, ixh) + 4.0 * PHI2(iyl + 1, ixh) - 3.0 * PHI2(iyl, ixh);
+    ll = -1.0 * PHI2(iyl + 2, ixl) + 4.0 * PHI2(iyl + 1, ixl) - 3.0 * PHI2(iyl, ixl);
+  }
+  if (iyh < Ny) {
+    hh = PHI2(iyh + 1, ixh) - PHI2(iyh - 1, ixh);
+    hl = PHI2(iyh + 1, ixl) - PHI2(iyh - 1, ixl);
+  } else {
+    hh = +3.0 * PHI2(iyh, ixh) - 4.0 * PHI2(iyh - 1, ixh) + 1.0 * PHI2(iyh - 2, ixh);
+    hl = +3.0 * PHI2(iyh, ixl) - 4.0 * PHI2(iyh - 1, ixl) + 1.0 * PHI2(iyh - 2, ixl);
+  }
+#undef PHI2
+  Ewh = lh + wyh * (hh - lh);
+  Ewl = ll + wyh * (hl - ll);
+  f[1] = Ewl + wxh * (Ewh - Ewl);
+}
+
+/* BorisMoverBz2D src/velocities.c:186-277 (the half E-kick as in 3-D). */
+int orc_push2d(const OrcParams *p, int np, const double *pos, double *vel, const double *phi, double dt) {
+  double tscale = 0.5 * (p->qi / p->mi) * dt;
+  double t = tscale * p->B0;
+  double s = 2.0 * t / (1 + t * t);
+  double h[2] = {1.0 / p->dx, 1.0 / p->dy};
+  double Escale[2];
+  for (int d = 0; d < 2; d++) Escale[d] = -0.5 * h[d] * tscale;
+  for (int ip = 0; ip < np; ip++) {
+    double E[2];
+    double x = pos[ip * 2 + 0] / p->dx, y = pos[ip * 2 + 1] / p->dy;
+    difference_vector2d(p, phi, x, y, E);
+    double vxm = vel[ip * 2 + 0] + Escale[0] * E[0];
+    double vym = vel[ip * 2 + 1] + Escale[1] * E[1];
+    double vxt = vxm + vym * t;
+    double vyp = vym - vxt * s;
+    double vxp = vxt + vyp * t;
+    vel[ip * 2 + 0] = vxp;
+    vel[ip * 2 + 1] = vyp;
+  }
+  return 0;
+}
+
+/* UpdatePositions + Apply2DBC (src/positions.c:455-459, src/boundaries.c:   */
+/* 35-40): periodic x and y.                                                  */
+int orc_move2d(const OrcParams *p, int np, double *pos, double *vel, double dt) {
+  double r0[2] = {p->x0, p->y0}, r1v[2] = {p->x1, p->y1}, L[2] = {p->Lx, p->Ly};
+  for (int ip = 0; ip < np; ip++) {
+    for (int d = 0; d < 2; d++) pos[ip * 2 + d] += vel[ip * 2 + d] * dt;
+    for (int d = 0; d < 2; d++) {
+      double r = pos[ip * 2 + d];
+      if (r < r0[d]) r += L[d];
+      if (r >= r1v[d]) r -= L[d];
+      pos[ip * 2 + d] = r;
+    }
+  }
+  return 0;
+}
+
+/* Bilinear weights of Collect2DFluidMoments src/moments.c:59-78, corners    */
+/* b = yb*2 + xb.                                                             */
+static void cic_weights2d(double x, double y, int idx[2], double w[4]) {
+  int ixl = (int)x, iyl = (int)y;
+  double wxh = x - (double)ixl, wxl = 1.0 - wxh;
+  double wyh = y - (double)iyl, wyl = 1.0 - wyh;
+  idx[0] = ixl; idx[1] = iyl;
+  w[3] = wyh * wxh;
+  w[1] = wyl * wxh;
+  w[2] = wyh * wxl;
+  w[0] = wyl * wxl;
+}
+
+/* Collect2DFluidMoments src/moments.c:5-105: particle-order sums into the    */
+/* ghosted local array, ghost fold in local-array order; out [1][Ny][Nx][4]   */
+/* with Gz = 0.                                                               */
+int orc_collect2d(const OrcParams *p, int np, const double *pos, const double *vel, double *out) {
+  int gx = p->Nx + 2, gy = p->Ny + 2;
+  double *loc = calloc((size_t)gx * gy * 4, sizeof(double));
+  if (!loc) return -1;
+  static const int order[4] = {3, 1, 2, 0}; /* hh, lh, hl, ll */
+  for (int ip = 0; ip < np; ip++) {
+    int idx[2];
+    double w[4];
+    cic_weights2d(pos[ip * 2 + 0] / p->dx, pos[ip * 2 + 1] / p->dy, idx, w);
+    for (int q = 0; q < 4; q++) {
+      int b = order[q];
+      int i = idx[0] + (b & 1) + 1, j = idx[1] + (b >> 1) + 1;
+      if (i < 0 || i >= gx || j < 0 || j >= gy) continue;
+      loc[((size_t)j * gx + i) * 4] += w[b];
+    }
+    for (int d = 0; d < 2; d++) {
+      double v = vel[ip * 2 + d];
+      for (int q = 0; q < 4; q++) {
+        int b = order[q];
+        int i = idx[0] + (b & 1) + 1, j = idx[1] + (b >> 1) + 1;
+        if (i < 0 || i >= gx || j < 0 || j >= gy) continue;
+        loc[((size_t)j * gx + i) * 4 + 1 + d] += v * w[b];
+      }
+    }
+  }
+  memset(out, 0, sizeof(double) * (size_t)p->Nx * p->Ny * 4);
+  for (int jj = 0; jj < gy; jj++) {
+    int j = jj - 1;
+    if (j < 0 || j >= p->Ny) { if (p->bc[1]) continue; j = wrapi(j, p->Ny); }
+    for (int ii = 0; ii < gx; ii++) {
+      int i = ii - 1;
+      if (i < 0 || i >= p->Nx) { if (p->bc[0]) continue; i = wrapi(i, p->Nx); }
+      const double *src = loc + ((size_t)jj * gx + ii) * 4;
+      double *dst = out + ((size_t)j * p->Nx + i) * 4;
+      for (int c = 0; c < 4; c++) dst[c] += src[c];
+    }
+  }
+  free(loc);
+  return 0;
+}
+
+/* The fixed-point deposit of orc_collect_fixed for 2-D ions. */
+int orc_collect2d_fixed(const OrcParams *p, int np, const double *pos, const double *vel, int Sn, int Sf,
+                        double *out) {
+  size_t ncell = (size_t)p->Nx * p->Ny;
+  int64_t *acc = calloc(ncell * 4, sizeof(int64_t));
+  if (!acc) return -1;
+  double sc = ldexp(1.0, Sn), scf = ldexp(1.0, Sf);
+  for (int ip = 0; ip < np; ip++) {
+    int idx[2];
+    double w[4];
+    cic_weights2d(pos[ip * 2 + 0] / p->dx, pos[ip * 2 + 1] / p->dy, idx, w);
+    for (int b = 0; b < 4; b++) {
+      int i = wrapi(idx[0] + (b & 1), p->Nx), j = wrapi(idx[1] + (b >> 1), p->Ny);
+      int64_t *node = acc + ((size_t)j * p->Nx + i) * 4;
+      node[0] += (int64_t)llrint(w[b] * sc);
+      for (int d = 0; d < 2; d++) node[1 + d] += (int64_t)llrint((vel[ip * 2 + d] * w[b]) * scf);
+    }
+  }
+  double isc = ldexp(1.0, -Sn), iscf = ldexp(1.0, -Sf);
+  for (size_t e = 0; e < ncell * 4; e++) out[e] = (double)acc[e] * ((e % 4) == 0 ? isc : iscf);
+  free(acc);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* RHS: src/rhs.c:259-373 (ComputeFullRHS3D), mean removed as                */
 /* MatNullSpaceRemove does (sequential sum, then subtract the mean).          */
 /* ------------------------------------------------------------------------ */
@@ -317,6 +486,17 @@ static void rhs_constant(const OrcParams *p, double *b) {
    cos(2 pi z) scale, then the constant null space removed. */
 static void rhs_sinusoidal(const OrcParams *p, double *b) {
   const double PI = 3.141592653589793238462643383279502884;
+  if (p->ndim == 2) {  /* ComputeSinusoidalRHS2D src/rhs.c:26-79 */
+    for (int j = 0; j < p->Ny; j++)
+      for (int i = 0; i < p->Nx; i++) {
+        double x = ((double)i + 0.5) * p->dx, y = ((double)j + 0.5) * p->dy;
+        double Cx = cos(2 * PI * x), Cy = cos(2 * PI * y);
+        double val = Cx * Cy;
+        b[(size_t)j * p->Nx + i] = p->n0 * val * p->scale;
+      }
+    null_space_remove(b, (size_t)p->Nx * p->Ny);
+    return;
+  }
   for (int k = 0; k < p->Nz; k++)
     for (int j = 0; j < p->Ny; j++)
       for (int i = 0; i < p->Nx; i++) {
@@ -337,7 +517,37 @@ int orc_rhs(const OrcParams *p, const double *m, double *b) {
   return rhs_full(p, m, b);
 }
 
+/* ComputeFullRHS2D src/rhs.c:151-258 */
+static int rhs_full2d(const OrcParams *p, const double *m, double *b) {
+  double kappa = p->kappa_e;
+  double hx = 1.0 / (2.0 * p->dx), hy = 1.0 / (2.0 * p->dy);
+  double hxx = 1.0 / (p->dx * p->dx), hyy = 1.0 / (p->dy * p->dy);
+  size_t n = (size_t)p->Nx * p->Ny;
+  for (int j = 0; j < p->Ny; j++)
+    for (int i = 0; i < p->Nx; i++) {
+      double nijk = mom(p, m, 0, j, i, 0);
+      double npjk = mom(p, m, 0, j, i + 1, 0), nmjk = mom(p, m, 0, j, i - 1, 0);
+      double nipk = mom(p, m, 0, j + 1, i, 0), nimk = mom(p, m, 0, j - 1, i, 0);
+      double dndx = hx * (npjk - nmjk);
+      double dndy = hy * (nipk - nimk);
+      double d2ndxx = hxx * (npjk - 2 * nijk + nmjk);
+      double d2ndyy = hyy * (nipk - 2 * nijk + nimk);
+      double dGxdx = hx * (mom(p, m, 0, j, i + 1, 1) - mom(p, m, 0, j, i - 1, 1));
+      double dGydy = hy * (mom(p, m, 0, j + 1, i, 2) - mom(p, m, 0, j - 1, i, 2));
+      double Eterm = (dndy - kappa * dndx) * p->E0;
+      double Pterm = p->cth * (d2ndxx + d2ndyy);
+      double Gterm = p->cG * (dGxdx + dGydy);
+      b[(size_t)j * p->Nx + i] = p->scale * (Eterm + Pterm + Gterm);
+    }
+  double s = 0.0;
+  for (size_t e = 0; e < n; e++) s += b[e];
+  s = s / (-(double)n);
+  for (size_t e = 0; e < n; e++) b[e] += s;
+  return 0;
+}
+
 static int rhs_full(const OrcParams *p, const double *m, double *b) {
+  if (p->ndim == 2) return rhs_full2d(p, m, b);
   double kappa = p->kappa_e;
   double hx = 1.0 / (2.0 * p->dx), hy = 1.0 / (2.0 * p->dy), hz = 1.0 / (2.0 * p->dz);
   double hxx = 1.0 / (p->dx * p->dx), hyy = 1.0 / (p->dy * p->dy), hzz = 1.0 / (p->dz * p->dz);
@@ -393,8 +603,13 @@ static int lhs_row_simple(const OrcParams *p, double v[11]) {
   if (p->lhs_type != 1) return 0;
   double vpjk = 1.0 / (p->dx * p->dx), vmjk = 1.0 / (p->dx * p->dx);
   double vipk = 1.0 / (p->dy * p->dy), vimk = 1.0 / (p->dy * p->dy);
+  v[0] = vpjk; v[1] = vmjk; v[2] = vipk; v[3] = vimk;
+  if (p->ndim == 2) {  /* ComputeLaplacianLHS2D src/lhs.c:26-97 */
+    v[10] = -(vpjk + vipk + vmjk + vimk);
+    return 1;
+  }
   double vijp = 1.0 / (p->dz * p->dz), vijm = 1.0 / (p->dz * p->dz);
-  v[0] = vpjk; v[1] = vmjk; v[2] = vipk; v[3] = vimk; v[4] = vijp; v[5] = vijm;
+  v[4] = vijp; v[5] = vijm;
   v[10] = -(vpjk + vipk + vijp + vmjk + vimk + vijm);
   return 1;
 }
@@ -413,6 +628,19 @@ void orc_lhs_row(const OrcParams *p, const double *n, int k, int j, int i, doubl
   double nmjk = dens(p, n, k, j, i - 1), npjk = dens(p, n, k, j, i + 1);
   double nimk = dens(p, n, k, j - 1, i), nipk = dens(p, n, k, j + 1, i);
   double nijm = dens(p, n, k - 1, j, i), nijp = dens(p, n, k + 1, j, i);
+  if (p->ndim == 2) {  /* ComputeFullLHS2D src/lhs.c:194-335: the in-plane 9 entries */
+    v[6] = sod * (nipk - npjk);
+    v[7] = sod * (npjk - nimk);
+    v[8] = sod * (nmjk - nipk);
+    v[9] = sod * (nimk - nmjk);
+    v[0] = sxx * (npjk + nijk) + sod * (nipk - nimk);
+    v[1] = sxx * (nijk + nmjk) - sod * (nipk - nimk);
+    v[2] = syy * (nipk + nijk) - sod * (npjk - nmjk);
+    v[3] = syy * (nijk + nimk) + sod * (npjk - nmjk);
+    v[4] = v[5] = 0.0;
+    v[10] = -(sxx * (npjk + 2 * nijk + nmjk) + syy * (nipk + 2 * nijk + nimk));
+    return;
+  }
   v[6] = sod * (nipk - npjk);
   v[7] = sod * (npjk - nimk);
   v[8] = sod * (nmjk - nipk);

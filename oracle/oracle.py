@@ -30,7 +30,7 @@ class OrcParams(C.Structure):
         ("nui", C.c_double), ("viT", C.c_double), ("vi0", C.c_double * 3),
         ("mn", C.c_double), ("vnT", C.c_double), ("vn0", C.c_double * 3), ("vn0mag", C.c_double),
         ("kappa_e", C.c_double), ("scale", C.c_double), ("cth", C.c_double), ("cG", C.c_double),
-        ("n0", C.c_double), ("lhs_type", C.c_int), ("rhs_type", C.c_int),
+        ("n0", C.c_double), ("lhs_type", C.c_int), ("rhs_type", C.c_int), ("ndim", C.c_int),
     ]
 
 
@@ -66,6 +66,10 @@ def lib():
             "orc_ran3_n": (C.c_int, [C.POINTER(C.c_long), C.c_int, vp]),
             "orc_gasdev_n": (C.c_int, [C.POINTER(C.c_long), C.c_int, vp]),
             "orc_sobol": (C.c_int, [P, C.c_int, vp]),
+            "orc_push2d": (C.c_int, [P, C.c_int, vp, vp, vp, C.c_double]),
+            "orc_move2d": (C.c_int, [P, C.c_int, vp, vp, C.c_double]),
+            "orc_collect2d": (C.c_int, [P, C.c_int, vp, vp, vp]),
+            "orc_collect2d_fixed": (C.c_int, [P, C.c_int, vp, vp, C.c_int, C.c_int, vp]),
             "orc_normal_velocities": (C.c_int, [vp, vp, C.c_int, vp]),
             "orc_collide": (C.c_int, [P, C.c_int, vp, C.c_double, vp]),
             "orc_collision_count": (C.c_int, [P, C.c_int, C.c_double]),
@@ -113,6 +117,7 @@ def params_from(p) -> OrcParams:
               "qi", "mi", "B0", "E0", "nui", "viT", "mn", "vnT", "kappa_e", "scale", "cth", "cG", "n0"):
         setattr(o, k, float(g(k)))
     o.lhs_type, o.rhs_type = int(g("lhs_type")), int(g("rhs_type"))
+    o.ndim = int(g("ndim"))
     o.vi0[0], o.vi0[1], o.vi0[2] = float(g("vi0x")), float(g("vi0y")), float(g("vi0z"))
     o.vn0[0], o.vn0[1], o.vn0[2] = float(g("vn0x")), float(g("vn0y")), float(g("vn0z"))
     o.vn0mag = float(g("vn0"))
@@ -131,20 +136,23 @@ class Oracle:
         vel = np.array(vel, dtype=np.float64, order="C")
         phi = np.ascontiguousarray(phi, dtype=np.float64)
         pos = np.ascontiguousarray(pos, dtype=np.float64)
-        self.L.orc_push(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(phi), dt)
+        f = self.L.orc_push2d if self.p.ndim == 2 else self.L.orc_push
+        f(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(phi), dt)
         return vel
 
     def move(self, pos, vel, dt):
         pos = np.array(pos, dtype=np.float64, order="C")
         vel = np.array(vel, dtype=np.float64, order="C")
-        self.L.orc_move(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), dt)
+        f = self.L.orc_move2d if self.p.ndim == 2 else self.L.orc_move
+        f(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), dt)
         return pos, vel
 
     def collect(self, pos, vel):
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         out = np.zeros(self.shape + (4,))
-        self.L.orc_collect(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(out))
+        f = self.L.orc_collect2d if self.p.ndim == 2 else self.L.orc_collect
+        f(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), _p(out))
         return out
 
     def collect_mt(self, pos, vel):
@@ -158,6 +166,9 @@ class Oracle:
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         out = np.zeros(self.shape + (4,))
+        if self.p.ndim == 2:
+            self.L.orc_collect2d_fixed(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), shift_n, shift_f, _p(out))
+            return out, None
         acc = np.zeros(self.shape + (4,), dtype=np.int64)
         self.L.orc_collect_fixed(C.byref(self.p), pos.shape[0], _p(pos), _p(vel), shift_n, shift_f, _p(out), _p(acc))
         return out, acc

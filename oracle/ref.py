@@ -75,9 +75,9 @@ class Ref:
         self.L.ref_set_particles(_p(pos), _p(vel), pos.shape[0])
 
     def get_particles(self):
-        n = self.np
-        pos = np.zeros((n, 3))
-        vel = np.zeros((n, 3))
+        n, nd = self.np, int(self.params["ndim"])
+        pos = np.zeros((n, nd))
+        vel = np.zeros((n, nd))
         self.L.ref_get_particles(_p(pos), _p(vel))
         return pos, vel
 

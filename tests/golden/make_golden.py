@@ -21,6 +21,11 @@ Cases:
        kappa_e ~ 88) on tests/grid3D.ini spacing (dx = 0.5) at 16^3, one ion
        per cell, dt = 1e-5 as in tests/test_all.sh.
   rng  ran1 / ran3 / gasdev streams and Sobol points from a fresh process.
+  twod -ndim 2 on an 8x6 grid (dx = 0.5, dy = 1), collisions off, 4 Sobol
+       ions per cell plus hand-placed ions in the last cells (backward
+       differences) and on the bounds: push, move, deposit, RHS and the
+       9-point operator (dense), and the 5-point Laplacian with the
+       sinusoidal RHS.
   ops  the other operator options on a 6x5x4 grid (dx = 0.1, dy = 0.125,
        dz = 0.2, n0 = 2.5): RHS and dense LHS of -lhs laplacian -rhs
        sinusoidal, of -lhs laplacian -rhs constant with a reflecting z, of
@@ -177,6 +182,44 @@ def case_rng():
     return out
 
 
+def case_twod():
+    opts = "-ndim 2 -Nx 8 -Ny 6 -dx 0.5 -dy 1.0 -mn 0 " + C1_PHYS
+    R = refmod.Ref(opts, 4 * 48)
+    R.init_positions(0)
+    R.init_velocities()
+    pos, vel = R.get_particles()
+    out = {"init_pos": pos.copy(), "init_vel": vel.copy()}
+    extra = np.array([[3.99, 5.5], [0.0, 0.0], [0.5, 1.0], [3.999, 5.999], [0.01, 3.3], [3.75, 0.25]])
+    pos = np.concatenate([pos[: pos.shape[0] - extra.shape[0]], extra])
+    vel = vel.copy()
+    vel[-3] = [0.5, 0.4]    # crosses both upper bounds
+    vel[-2] = [-0.5, 0.1]   # crosses x = 0
+    phi = smooth_phi(R.shape, 31, amp=2.0)
+    out.update({"pos0": pos.copy(), "vel0": vel.copy(), "phi": phi.copy(), "dt": np.float64(0.1)})
+    R.set_particles(pos, vel)
+    R.set_phi(phi)
+    R.push(0.1)
+    _, vpush = R.get_particles()
+    out["vel_push"] = vpush.copy()
+    R.update_positions(0.1)
+    pmove, vmove = R.get_particles()
+    out["pos_move"] = pmove.copy()
+    out["vel_move"] = vmove.copy()
+    R.collect()
+    out["moments"] = R.get_moments()
+    out["rhs"] = R.rhs()
+    out["lhs"] = R.lhs_dense()
+    out["opts"] = opts
+    out["params"] = json.dumps(R.params)
+    opts_lap = "-ndim 2 -Nx 8 -Ny 6 -dx 0.1 -dy 0.125 -n0 2.5 -mn 0 -lhs laplacian -rhs sinusoidal " + C1_PHYS
+    R2 = refmod.Ref(opts_lap, 8)
+    out["lap_rhs"] = R2.rhs()
+    out["lap_lhs"] = R2.lhs_dense()
+    out["lap_opts"] = opts_lap
+    out["lap_params"] = json.dumps(R2.params)
+    return out
+
+
 OPS_BASE = "-Nx 6 -Ny 5 -Nz 4 -dx 0.1 -dy 0.125 -dz 0.2 -n0 2.5 " + C1_PHYS
 OPS_VARIANTS = {
     "lap_sin": "-lhs laplacian -rhs sinusoidal",
@@ -201,7 +244,7 @@ def case_ops():
     return out
 
 
-CASES = {"c1": case_c1, "edge": case_edge, "fb": case_fb, "rng": case_rng, "ops": case_ops}
+CASES = {"c1": case_c1, "edge": case_edge, "fb": case_fb, "rng": case_rng, "ops": case_ops, "twod": case_twod}
 
 
 def main():

@@ -143,3 +143,26 @@ def test_operator_options_bit_exact(built, variant):
     m[..., 0] = dens
     eq(O.rhs(m), d[f"{variant}_rhs"])
     eq(O.lhs_dense(dens), d[f"{variant}_lhs"])
+
+
+def test_two_d_bit_exact(built):
+    """-ndim 2 (BorisMoverBz2D + DifferenceVector2D, UpdatePositions +
+    Apply2DBC, Collect2DFluidMoments, ComputeFullRHS2D, ComputeFullLHS2D,
+    ComputeLaplacianLHS2D, ComputeSinusoidalRHS2D) against the reference."""
+    import json
+
+    from conftest import GOLDEN
+    d = np.load(GOLDEN / "twod.npz")
+    O = orc.Oracle(json.loads(str(d["params"])))
+    vel = O.push(d["pos0"], d["vel0"], d["phi"], float(d["dt"]))
+    eq(vel, d["vel_push"])
+    pos, vel = O.move(d["pos0"], d["vel_push"], float(d["dt"]))
+    eq(pos, d["pos_move"])
+    eq(vel, d["vel_move"])
+    m = O.collect(d["pos_move"], d["vel_move"])
+    eq(m, d["moments"])
+    eq(O.rhs(d["moments"]), d["rhs"])
+    eq(O.lhs_dense(d["moments"][..., 0]), d["lhs"])
+    O2 = orc.Oracle(json.loads(str(d["lap_params"])))
+    eq(O2.rhs(np.zeros(O2.shape + (4,))), d["lap_rhs"])
+    eq(O2.lhs_dense(np.zeros(O2.shape)), d["lap_lhs"])
