@@ -75,9 +75,26 @@ PetscErrorCode EcsGpuApply3DBC(PetscInt np, PetscReal *pos, PetscReal *vel, void
 PetscErrorCode EcsGpuCollect3D(void *opts);
 PetscErrorCode EcsGpuFullLHS3D(KSP ksp, Mat J, Mat A, void *opts);
 PetscErrorCode EcsGpuFullRHS3D(KSP ksp, Vec b, void *opts);
+/* 2-D (src/velocities.c:186, src/boundaries.c:35, src/moments.c:5,
+   src/lhs.c:194, src/rhs.c:151) and the other operator options
+   (src/lhs.c:11-191, src/rhs.c:6-148). */
+PetscErrorCode EcsGpuPushBz2D(PetscReal dt, void *opts);
+PetscErrorCode EcsGpuApply2DBC(PetscInt np, PetscReal *pos, PetscReal *vel, void *opts);
+PetscErrorCode EcsGpuCollect2D(void *opts);
+PetscErrorCode EcsGpuFullLHS2D(KSP ksp, Mat J, Mat A, void *opts);
+PetscErrorCode EcsGpuFullRHS2D(KSP ksp, Vec b, void *opts);
+PetscErrorCode EcsGpuIdentityLHS(KSP ksp, Mat J, Mat A, void *opts);
+PetscErrorCode EcsGpuLaplacianLHS2D(KSP ksp, Mat J, Mat A, void *opts);
+PetscErrorCode EcsGpuLaplacianLHS3D(KSP ksp, Mat J, Mat A, void *opts);
+PetscErrorCode EcsGpuConstantRHS(KSP ksp, Vec b, void *opts);
+PetscErrorCode EcsGpuSinusoidalRHS2D(KSP ksp, Vec b, void *opts);
+PetscErrorCode EcsGpuSinusoidalRHS3D(KSP ksp, Vec b, void *opts);
 
-/* SetUpContext analogue: fill the slots with the GPU operators. */
+/* SetUpContext analogue: fill the slots with the GPU operators (3-D, full). */
 void EcsGpuBindOperators(EcsOperators *ops);
+/* The same by the parameters' ndim, lhs_type and rhs_type, as SetUpContext's
+   switches (src/setup.c:23-105); ECS_ERR_INVALID for unknown types. */
+int EcsGpuBindOperatorsFor(EcsOperators *ops, const EcsParams *p);
 
 /* Stage wrappers with the reference's semantics. */
 PetscErrorCode EcsGpuUpdateVelocities(const EcsOperators *ops, PetscInt ndim, PetscReal dt,

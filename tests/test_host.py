@@ -116,6 +116,15 @@ def test_gpu_library_exports_every_declared_symbol(built):
     assert set(names) <= bound, set(names) - bound
 
 
+def test_gpu_library_exports_operator_slots(built):
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "ecs_compat.h").read_text(), flags=re.S)
+    names = sorted(set(re.findall(r"\b(EcsGpu[A-Za-z0-9]+)\s*\(", text)))
+    assert len(names) >= 20
+    lib = ctypes.CDLL(str(_lib.GPU_LIB_PATH))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
 def test_host_library_exports_every_declared_symbol(built):
     lib = ctypes.CDLL(str(_lib.HOST_LIB_PATH))
     names = _declared("ecs_host.h")
@@ -136,3 +145,28 @@ def test_device_bytes_estimate(built):
     b_fp64 = _lib.gpu().ecs_ctx_device_bytes(ctypes.byref(p), 0, 134217728)
     assert 7e9 < b_mixed < 12e9
     assert 6e9 < b_fp64 < 12e9
+
+
+@pytest.mark.parametrize("opts,expect", [
+    ("", ("EcsGpuApply3DBC", "EcsGpuCollect3D", "EcsGpuPushBz3D", "EcsGpuFullLHS3D", "EcsGpuFullRHS3D")),
+    ("-ndim 2 -mn 0", ("EcsGpuApply2DBC", "EcsGpuCollect2D", "EcsGpuPushBz2D", "EcsGpuFullLHS2D", "EcsGpuFullRHS2D")),
+    ("-lhs laplacian -rhs sinusoidal", ("EcsGpuApply3DBC", "EcsGpuCollect3D", "EcsGpuPushBz3D",
+                                        "EcsGpuLaplacianLHS3D", "EcsGpuSinusoidalRHS3D")),
+    ("-ndim 2 -lhs identity -rhs constant", ("EcsGpuApply2DBC", "EcsGpuCollect2D", "EcsGpuPushBz2D",
+                                             "EcsGpuIdentityLHS", "EcsGpuConstantRHS")),
+])
+def test_operator_binding_follows_setup(built, opts, expect):
+    """EcsGpuBindOperatorsFor fills the slots by SetUpContext's rules
+    (src/setup.c:23-105)."""
+    lib = ctypes.CDLL(str(_lib.GPU_LIB_PATH))
+
+    class Ops(ctypes.Structure):
+        _fields_ = [(n, ctypes.c_void_p) for n in ("applyBC", "collect", "push", "collide", "lhs", "rhs")]
+
+    p = E.params_from_options(opts)
+    ops = Ops()
+    assert lib.EcsGpuBindOperatorsFor(ctypes.byref(ops), ctypes.byref(p)) == 0
+    addr = lambda n: ctypes.cast(getattr(lib, n), ctypes.c_void_p).value
+    got = (ops.applyBC, ops.collect, ops.push, ops.lhs, ops.rhs)
+    assert got == tuple(addr(n) for n in expect)
+    assert ops.collide == addr("EcsGpuScatterElastic")
