@@ -92,36 +92,51 @@ static inline int seg_len(int N) {
   return 64;
 }
 
+// The z entries of every row (lower, upper, diagonal), one thread per cell:
+// the parallel half of the z-line set-up.
 template <typename T>
-__global__ void k_zline_setup(OpK o, const T *__restrict__ n, ZlP<T> z, int S) {
-  const GridG &g = o.g;
+__global__ void k_zline_rows(OpK o, const T *__restrict__ n, T *__restrict__ lo, T *__restrict__ up,
+                             T *__restrict__ dg) {
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  T v[11];
+  row11(n, o, i, j, k, v);
+  const unsigned c = lin3(o.g, i, j, k);
+  lo[c] = v[5];
+  up[c] = v[4];
+  dg[c] = v[10];
+}
+
+// Factorisation of every column's z tridiagonal (one thread a column) from
+// the rows of k_zline_rows.
+template <typename T>
+__global__ void k_zline_setup(GridG g, const T *__restrict__ lo, const T *__restrict__ up,
+                              const T *__restrict__ dg, ZlP<T> z, int S) {
   const int ncol = g.nx * g.ny;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
-  const int i = col % g.nx, j = col / g.nx;
   const size_t plane = (size_t)g.nx * g.ny;
   // a one-cell column (2-D) has no z coupling: the plain solve, no periodic closure
   const bool cyc = g.bc[2] == 0 && g.nz > 1;
   const int N = g.nz;
-  T v[11];
-  row11(n, o, i, j, 0, v);
-  const T lo0 = cyc ? v[5] : T(0), d0 = v[10];
+  const T lo0 = cyc ? __ldg(&lo[col]) : T(0), d0 = __ldg(&dg[col]);
   const T gamma = -d0;
   T cp_prev = T(0), dq_prev = T(0), fprod = T(1);
   // forward: factor T' and forward-substitute u = (gamma, 0, .., up_{N-1})
+#pragma unroll 4
   for (int k = 0; k < N; k++) {
-    row11(n, o, i, j, k, v);
-    T a = (k == 0) ? T(0) : v[5];
-    T up = (k == N - 1) ? T(0) : v[4];
-    T bb = v[10];
+    const size_t c = (size_t)k * plane + col;
+    const T lk = __ldg(&lo[c]), uk = __ldg(&up[c]), dk = __ldg(&dg[c]);
+    T a = (k == 0) ? T(0) : lk;
+    T upk = (k == N - 1) ? T(0) : uk;
+    T bb = dk;
     if (cyc && k == 0) bb = d0 - gamma;
-    if (cyc && k == N - 1) bb = v[10] - v[4] * lo0 / gamma;
+    if (cyc && k == N - 1) bb = dk - uk * lo0 / gamma;
     T m = bb - a * cp_prev;
     T minv = T(1) / m;
-    T cp = up * minv;
-    T u = cyc ? ((k == 0) ? gamma : ((k == N - 1) ? v[4] : T(0))) : T(0);
+    T cp = upk * minv;
+    T u = cyc ? ((k == 0) ? gamma : ((k == N - 1) ? uk : T(0))) : T(0);
     T dq = (u - a * dq_prev) * minv;
-    size_t c = (size_t)k * plane + col;
     z.a[c] = a;
     z.cp[c] = cp;
     z.minv[c] = minv;
@@ -322,21 +337,24 @@ __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__
 template <typename T>
 struct SmallLevel {
   OpK o;
-  const T *dens;
-  ZlP<T> z;
+  const T *dens;   // in global memory, staged at sd
+  ZlP<T> z;        // in global memory, staged at sa, sc, sm, sq (cells) and s0, sqd (columns)
   int sx, sb, sr, st;
+  int sd, sa, sc, sm, sq, s0, sqd;
 };
 constexpr int kMaxSmall = 8;
 template <typename T>
 struct SmallCycle {
   int nl;
-  const T *cinv;  // transposed inverse of the coarsest operator, or nullptr
+  const T *cinv;  // transposed inverse of the coarsest operator, or nullptr; staged at scinv
+  int scinv;
   SmallLevel<T> lv[kMaxSmall];
 };
 constexpr int kSmallThreads = 1024;
 
 // Thomas solve of one column with all vectors in shared memory: rin (right-
 // hand side) may be the same array as dp (the substitution scratch).
+// One column's z-line solve with the factors staged in shared memory.
 template <typename T>
 __device__ __forceinline__ void zline_col_s(const GridG &g, const ZlP<T> &z, const T *rin, T *dp,
                                             const T *xo, T *xn, T omega, int col) {
@@ -344,40 +362,57 @@ __device__ __forceinline__ void zline_col_s(const GridG &g, const ZlP<T> &z, con
   T d = T(0);
   for (int k = 0; k < N; k++) {
     const int c = k * plane + col;
-    d = (rin[c] - __ldg(&z.a[c]) * d) * __ldg(&z.minv[c]);
+    d = (rin[c] - z.a[c] * d) * z.minv[c];
     dp[c] = d;
   }
   const T yN = d;
   T y = d;
   for (int k = N - 2; k >= 0; k--) {
     const int c = k * plane + col;
-    y = dp[c] - __ldg(&z.cp[c]) * y;
+    y = dp[c] - z.cp[c] * y;
     dp[c] = y;
   }
-  const T s = (y + __ldg(&z.a0g[col]) * yN) * __ldg(&z.qden[col]);
+  const T s = (y + z.a0g[col] * yN) * z.qden[col];
   for (int k = 0; k < N; k++) {
     const int c = k * plane + col;
     const T ov = xo ? xo[c] : T(0);
-    xn[c] = ov + omega * ((dp[c] - s * __ldg(&z.q[c])) - ov);
+    xn[c] = ov + omega * ((dp[c] - s * z.q[c]) - ov);
   }
+}
+
+// A small level's density and z-line factors as staged in shared memory.
+template <typename T>
+struct SmallView {
+  const T *dens;
+  ZlP<T> z;
+};
+template <typename T>
+__device__ __forceinline__ SmallView<T> staged(const SmallLevel<T> &L, T *sm) {
+  SmallView<T> v;
+  v.dens = sm + L.sd;
+  v.z = L.z;
+  v.z.a = sm + L.sa; v.z.cp = sm + L.sc; v.z.minv = sm + L.sm; v.z.q = sm + L.sq;
+  v.z.a0g = sm + L.s0; v.z.qden = sm + L.sqd;
+  return v;
 }
 
 // One damped z-line Jacobi sweep of level L from xo (nullptr: zero) into xn.
 template <typename T>
 __device__ void blk_sweep(const SmallLevel<T> &L, T *sm, const T *b, const T *xo, T *xn, T omega) {
   const GridG &g = L.o.g;
+  const SmallView<T> v = staged(L, sm);
   T *r = sm + L.sr;
   const T *rin = b;
   if (xo) {
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      r[c] = zline_rhs_at(L.dens, b, xo, L.o, i, j, k, c);
+      r[c] = zline_rhs_at(v.dens, b, xo, L.o, i, j, k, c);
     }
     __syncthreads();
     rin = r;
   }
-  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x) zline_col_s<T>(g, L.z, rin, r, xo, xn, omega, col);
+  for (int col = threadIdx.x; col < g.nx * g.ny; col += blockDim.x) zline_col_s<T>(g, v.z, rin, r, xo, xn, omega, col);
   __syncthreads();
 }
 
@@ -388,6 +423,27 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
   extern __shared__ unsigned char small_smem[];
   T *sm = reinterpret_cast<T *>(small_smem);
   const int nl = sc.nl;
+  // stage the levels' densities and z-line factors, the coarse inverse and
+  // the right-hand side: every later load is a shared-memory load
+  for (int l = 0; l < nl; l++) {
+    const SmallLevel<T> &L = sc.lv[l];
+    const unsigned n = (unsigned)L.o.g.n, ncol = (unsigned)(L.o.g.nx * L.o.g.ny);
+    for (unsigned c = threadIdx.x; c < n; c += blockDim.x) {
+      sm[L.sd + c] = __ldg(&L.dens[c]);
+      sm[L.sa + c] = __ldg(&L.z.a[c]);
+      sm[L.sc + c] = __ldg(&L.z.cp[c]);
+      sm[L.sm + c] = __ldg(&L.z.minv[c]);
+      sm[L.sq + c] = __ldg(&L.z.q[c]);
+    }
+    for (unsigned c = threadIdx.x; c < ncol; c += blockDim.x) {
+      sm[L.s0 + c] = __ldg(&L.z.a0g[c]);
+      sm[L.sqd + c] = __ldg(&L.z.qden[c]);
+    }
+  }
+  if (sc.cinv) {
+    const unsigned nn = (unsigned)(sc.lv[nl - 1].o.g.n * sc.lv[nl - 1].o.g.n);
+    for (unsigned e = threadIdx.x; e < nn; e += blockDim.x) sm[sc.scinv + e] = __ldg(&sc.cinv[e]);
+  }
   {
     const SmallLevel<T> &L = sc.lv[0];
     for (unsigned c = threadIdx.x; c < L.o.g.n; c += blockDim.x) sm[L.sb + c] = b_in[c];
@@ -399,10 +455,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
     const GridG &g = L.o.g;
     T *b = sm + L.sb, *t = sm + L.st, *r = sm + L.sr;
     blk_sweep(L, sm, b, (const T *)nullptr, t, omega);
+    const T *dl = sm + L.sd;
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      r[c] = b[c] - apply_row(L.dens, (const T *)t, L.o, i, j, k);
+      r[c] = b[c] - apply_row(dl, (const T *)t, L.o, i, j, k);
     }
     __syncthreads();
     const SmallLevel<T> &C = sc.lv[l + 1];
@@ -420,9 +477,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
     const SmallLevel<T> &L = sc.lv[nl - 1];
     const int n = (int)L.o.g.n;
     const T *b = sm + L.sb;
+    const T *ci = sm + sc.scinv;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
       T acc = T(0);
-      for (int k = 0; k < n; k++) acc += __ldg(&sc.cinv[(size_t)k * n + r]) * b[k];
+      for (int k = 0; k < n; k++) acc += ci[k * n + r] * b[k];
       sm[L.sx + r] = acc;
     }
     __syncthreads();
@@ -978,7 +1036,7 @@ OpK op_level(const EcsCtx *ctx, const MgLevel<T> &L) {
 }
 GridG grid_level(const EcsCtx *ctx, int nx, int ny, int nz) { return make_grid(ctx->p, nx, ny, nz); }
 
-constexpr int kColBlock = 128;
+constexpr int kColBlock = 32;  // one warp a block: the columns spread over the SMs
 constexpr int kCoarseSweeps = 21;
 template <typename T>
 constexpr T kOmega() { return T(0.8); }
@@ -1005,9 +1063,12 @@ int mg_setup(EcsCtx *ctx) {
         grid_level(ctx, F.nx, F.ny, F.nz), grid_level(ctx, C.nx, C.ny, C.nz), F.dens, C.dens);
     ECS_LAUNCHED(ctx);
   }
-  for (auto &L : mg.lv) {
-    int ncol = L.nx * L.ny;
-    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(op_level(ctx, L), L.dens, zl_of(L),
+  for (auto &L : mg.lv) {  // the level's x, b and r are free here: they hold the rows
+    const int ncol = L.nx * L.ny;
+    const OpK o = op_level(ctx, L);
+    k_zline_rows<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, L.x, L.b, L.r);
+    ECS_LAUNCHED(ctx);
+    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(o.g, L.x, L.b, L.r, zl_of(L),
                                                                                seg_len<T>(L.nz));
     ECS_LAUNCHED(ctx);
   }
@@ -1054,12 +1115,15 @@ int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
 constexpr size_t kSmallCells = 512;
 constexpr size_t kSmallSmem = 200 * 1024;  // shared memory of the single-block cycle
 
-// Shared memory of a single-block cycle over levels l.. (4 vectors a level).
+// Shared memory of a single-block cycle over levels l..: per level 4
+// vectors, the staged density and 4 z-line factor arrays, 2 column arrays;
+// the coarse inverse.
 template <typename T>
 size_t small_bytes(const Multigrid<T> &mg, size_t l) {
-  size_t cells = 0;
-  for (size_t q = l; q < mg.lv.size(); q++) cells += mg.lv[q].n;
-  return cells * 4 * sizeof(T);
+  size_t words = 0;
+  for (size_t q = l; q < mg.lv.size(); q++) words += mg.lv[q].n * 9 + (size_t)mg.lv[q].nx * mg.lv[q].ny * 2;
+  if (mg.cinv) words += mg.lv.back().n * mg.lv.back().n;
+  return words * sizeof(T);
 }
 
 // One V(1,1) cycle on level l: xout = M(l) b, zero initial guess.  Levels of
@@ -1076,13 +1140,18 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
     int off = 0;
     for (int q = 0; q < sc.nl; q++) {
       MgLevel<T> &M = mg.lv[l + q];
-      sc.lv[q].o = op_level(ctx, M);
-      sc.lv[q].dens = M.dens;
-      sc.lv[q].z = zl_of(M);
-      const int nq = (int)M.n;
-      sc.lv[q].sx = off; sc.lv[q].sb = off + nq; sc.lv[q].sr = off + 2 * nq; sc.lv[q].st = off + 3 * nq;
-      off += 4 * nq;
+      SmallLevel<T> &S = sc.lv[q];
+      S.o = op_level(ctx, M);
+      S.dens = M.dens;
+      S.z = zl_of(M);
+      const int nq = (int)M.n, nc = M.nx * M.ny;
+      S.sx = off; S.sb = off + nq; S.sr = off + 2 * nq; S.st = off + 3 * nq;
+      S.sd = off + 4 * nq; S.sa = off + 5 * nq; S.sc = off + 6 * nq; S.sm = off + 7 * nq; S.sq = off + 8 * nq;
+      S.s0 = off + 9 * nq; S.sqd = off + 9 * nq + nc;
+      off += 9 * nq + 2 * nc;
     }
+    sc.scinv = off;
+    if (sc.cinv) off += (int)(mg.lv.back().n * mg.lv.back().n);
     const size_t bytes = (size_t)off * sizeof(T);
     static std::atomic<bool> attr_set[2];  // zero-initialised: false
     if (!attr_set[sizeof(T) == 8]) {
