@@ -486,12 +486,13 @@ int64_t ecs_launch_count(const EcsCtx *ctx) { return ctx ? ctx->launches : -1; }
 int ecs_fix_shifts(const EcsParams *p, int precision, int32_t *shift_density, int32_t *shift_flux) {
   if (!p || !shift_density || !shift_flux) return ECS_ERR_INVALID;
   int S = precision == ECS_PREC_FP64 ? ECS_FIX_SHIFT_FP64 : ECS_FIX_SHIFT_MIXED;
+  int Sf = precision == ECS_PREC_FP64 ? ECS_FIX_SHIFT_FP64 : ECS_FIX_SHIFT_MIXED_FLUX;
   double vmax = 16.0 * (p->viT + p->vi0);
   int ev = vmax > 0.0 ? (int)ceil(log2(vmax)) : 0;
   if (ev < -8) ev = -8;
   if (ev > 40) ev = 40;
   *shift_density = S;
-  *shift_flux = S - ev;
+  *shift_flux = Sf - ev;
   return ECS_OK;
 }
 

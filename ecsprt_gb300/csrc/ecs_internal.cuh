@@ -15,10 +15,13 @@
 // Fixed-point scales of the deposit accumulators: contributions are rounded
 // to integer multiples of 2^-S and summed exactly in int64, which makes the
 // moments independent of the order in which particles are processed.  The
-// density uses S = ECS_FIX_SHIFT_*; the flux uses S - e_v, where 2^e_v bounds
-// |v| (ecs_fix_shifts), so every contribution is at most 2^S in magnitude.
+// density uses S = ECS_FIX_SHIFT_*; the flux uses S_f - e_v, where 2^e_v
+// bounds |v| (ecs_fix_shifts), so every flux contribution is at most 2^S_f in
+// magnitude: S_f = S on the FP64 path, ECS_FIX_SHIFT_MIXED_FLUX on the mixed
+// path (one int32 word a flux contribution in the tile window).
 #define ECS_FIX_SHIFT_FP64 48
 #define ECS_FIX_SHIFT_MIXED 38
+#define ECS_FIX_SHIFT_MIXED_FLUX 22
 
 // Cell tiles of the mixed path (the deposit accumulates a tile in shared
 // memory).

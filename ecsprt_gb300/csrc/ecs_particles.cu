@@ -71,9 +71,10 @@ struct FixScale64 {
 //   rint(v 2^S) = H 2^B + rint(r)   (2^B H is even, so ties round alike).
 // Both integers come from adding the bias 1.5 * 2^23: for |t| <= 2^22,
 // fl(t + bias) lies in [2^23, 2^24], where the spacing of floats is 1, so
-// the addition rounds t to the nearest integer (ties to even) and the bit
-// pattern of the sum is bits(bias) + rint(t).  H and rint(r) are each summed
-// in int32: over at most kWindowMax contributions they cannot overflow.
+// the addition rounds t to the nearest integer (ties to even; the bias is
+// even) and the bit pattern of the sum is bits(bias) + rint(t).  H and
+// rint(r) are each summed in int32: over at most kWindowMax contributions
+// they cannot overflow.  This is the density's representation.
 constexpr float kFixBias = 12582912.0f;  // 1.5 * 2^23
 constexpr unsigned kFixBiasBits = 0x4B400000u;
 constexpr int kFixSplit = 19;
@@ -102,6 +103,24 @@ __device__ __forceinline__ long long fix_unbias(unsigned hi_sum, unsigned lo_sum
   return fix_join((int)(hi_sum - (unsigned)n * kFixBiasBits), (int)(lo_sum - (unsigned)n * kFixBiasBits));
 }
 
+// The flux in one word: rint(v 2^S) with |v 2^S| <= 2^22 (S = 22 - e_v on
+// the mixed path, 2^e_v bounding |v|), from one FP32 multiply-add of the
+// same bias (the fused product v 2^S is exact, then rounded once; the bias
+// trick needs |t| <= 2^22).  The tile kernel's window sums these words in
+// int32 only for ions whose velocity components are within 2^(e_v - 3)
+// (words <= 2^19: kWindowMax x 2^19 < 2^31); faster ions add theirs to the
+// int64 accumulators directly.
+struct FixWord32 {
+  float s;  // 2^S
+  __device__ __forceinline__ int word(float v) const {
+    return (int)(__float_as_uint(__fmaf_rn(v, s, kFixBias)) - kFixBiasBits);
+  }
+  // the biased word bits(bias) + rint(v 2^S) in a 64-bit tile entry
+  __device__ __forceinline__ long long put(float v) const {
+    return (long long)__float_as_uint(__fmaf_rn(v, s, kFixBias));
+  }
+};
+
 // Exact sum of the tile entries q in `m` (bit mask of lanes).
 __device__ __forceinline__ long long group_sum(const long long *row, unsigned m, const FixScale64 &) {
   long long sum = 0;
@@ -124,6 +143,16 @@ __device__ __forceinline__ long long group_sum(const long long *row, unsigned m,
   }
   return fix_unbias(hs, ls, n);
 }
+__device__ __forceinline__ long long group_sum(const long long *row, unsigned m, const FixWord32 &) {
+  const int n = __popc(m);
+  unsigned sum = 0;
+  while (m) {
+    const int q = __ffs(m) - 1;
+    m &= m - 1;
+    sum += (unsigned)row[q];
+  }
+  return (long long)(int)(sum - (unsigned)n * kFixBiasBits);
+}
 __device__ __forceinline__ long long full_sum(const long long *row, const FixScale64 &) {
   long long sum = 0;
 #pragma unroll
@@ -139,6 +168,12 @@ __device__ __forceinline__ long long full_sum(const long long *row, const FixSca
     ls += (unsigned)(e >> 32);
   }
   return fix_unbias(hs, ls, 32);
+}
+__device__ __forceinline__ long long full_sum(const long long *row, const FixWord32 &) {
+  unsigned sum = 0;
+#pragma unroll
+  for (int q = 0; q < 32; q++) sum += (unsigned)row[q];
+  return (long long)(int)(sum - 32u * kFixBiasBits);
 }
 
 
@@ -166,9 +201,11 @@ struct PartK {
   // fixed-point scales of the deposit: density 2^Sn, flux 2^Sf (Sf = Sn - e_v
   // for the velocity bound 2^e_v), and the bound itself
   double fixn64, fixf64;
-  FixScale32 fixn32, fixf32;
+  FixScale32 fixn32;  // density: two words
+  FixWord32 fixf32;   // flux: one word
   double vmax;
   float vmaxf;
+  float vwinf;  // vmax / 8: velocity components of ions deposited through the tile window
   TileG tg;
 };
 
@@ -198,22 +235,22 @@ __device__ __forceinline__ long long corner_node(const PartK &k, int i, int j, i
 // warp must call this together.
 constexpr int kTileStride = 33;
 
-template <typename T, typename Fix>
+template <typename T, typename FixN, typename FixF>
 __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long long *tile, const PartK &k,
                                              bool active, int i, int j, int kk, T wxh, T wyh,
-                                             T wzh, T v0, T v1, T v2, const Fix &fn, const Fix &ff) {
+                                             T wzh, T v0, T v1, T v2, const FixN &fn, const FixF &ff) {
   const int lane = threadIdx.x & 31;
   const T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
   // inactive lanes contribute the zero entry (bias included for FP32)
-  const long long zero = fn.put(T(0));
+  const long long zero_n = fn.put(T(0)), zero_f = ff.put(T(0));
 #pragma unroll
   for (int b = 0; b < 8; b++) {
     const T wz = (b & 4) ? wzh : wzl, wy = (b & 2) ? wyh : wyl, wx = (b & 1) ? wxh : wxl;
     const T w = wz * wy * wx;
-    tile[(b + 0) * kTileStride + lane] = active ? fn.put(w) : zero;
-    tile[(b + 8) * kTileStride + lane] = active ? ff.put(v0 * w) : zero;
-    tile[(b + 16) * kTileStride + lane] = active ? ff.put(v1 * w) : zero;
-    tile[(b + 24) * kTileStride + lane] = active ? ff.put(v2 * w) : zero;
+    tile[(b + 0) * kTileStride + lane] = active ? fn.put(w) : zero_n;
+    tile[(b + 8) * kTileStride + lane] = active ? ff.put(v0 * w) : zero_f;
+    tile[(b + 16) * kTileStride + lane] = active ? ff.put(v1 * w) : zero_f;
+    tile[(b + 24) * kTileStride + lane] = active ? ff.put(v2 * w) : zero_f;
   }
   const int key = active ? (i | (j << 10) | (kk << 20)) : -1;
   const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
@@ -222,7 +259,7 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
   unsigned rem = __ballot_sync(ECS_FULL_MASK, active);
   if (rem == ECS_FULL_MASK && peers == ECS_FULL_MASK) {
     // the whole warp deposits into one cell: plain 32-term sums
-    const long long sum = full_sum(row, fn);
+    const long long sum = lane < 8 ? full_sum(row, fn) : full_sum(row, ff);
     const long long node = corner_node(k, i, j, kk, lane & 7);
     if (node >= 0 && sum != 0)
       atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
@@ -235,7 +272,7 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
     const int gj = __shfl_sync(ECS_FULL_MASK, j, lead);
     const int gk = __shfl_sync(ECS_FULL_MASK, kk, lead);
     rem &= ~grp;
-    const long long sum = group_sum(row, grp, fn);
+    const long long sum = lane < 8 ? group_sum(row, grp, fn) : group_sum(row, grp, ff);
     const long long node = corner_node(k, gi, gj, gk, lane & 7);
     if (node >= 0 && sum != 0)
       atomicAdd((unsigned long long *)&acc[(size_t)(lane >> 3) * k.ncell + node], (unsigned long long)sum);
@@ -730,6 +767,9 @@ __device__ __forceinline__ bool bound_axis(int bc, int N, int &c, float &o, floa
     o = 1.0f - o;
   }
   if (o >= 1.0f) { o = 0.0f; c += 1; }
+  // a position exactly on the upper wall mirrors onto itself: keep it in the
+  // last cell, one FP32 step below the wall
+  if (c == N) { c = N - 1; o = 0x1.fffffep-1f; }
   v = -v;
   return c >= 0 && c < N;
 }
@@ -753,7 +793,7 @@ constexpr int kCX = ECS_TILE_X + 2, kCY = ECS_TILE_Y + 2, kCZ = ECS_TILE_Z + 2; 
 constexpr int kWCells = kCX * kCY * kCZ;
 // |H| <= 2^19 and |rint(r)| <= 2^18, so 4000 contributions to one word stay
 // below 2^31
-constexpr int kWindowMax = 4000;
+constexpr int kWindowMax = 4000;  // ions between window flushes (flux words <= 2^19: 4000 x 2^19 < 2^31)
 
 // Push (src/velocities.c:281-371), collisions (src/collisions.c:9-167) and
 // move + boundary conditions (src/positions.c:436-472) of one ion, in the
@@ -865,7 +905,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
 __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
                                                      int32_t *__restrict__ count, EcsDevStatus *st) {
-  __shared__ int win[4][2][kWPad];  // [field][H, rint(r)][node, padded strides]
+  __shared__ int win[5][kWPad];  // [density H, density rint(r), flux x, y, z][node, padded strides]
   __shared__ int wcnt[kWCells];
   __shared__ float4 ewin[kWNodes];    // difference numerators of the window's nodes
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -890,7 +930,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
       const int seg = (L + 31) >> 5;               // lane segment
       const int sub = (seg + kBlock / 32 - 1) / (kBlock / 32);  // a warp's run inside each segment
       if (mode & 8)
-        for (int e = threadIdx.x; e < 8 * kWPad; e += blockDim.x) (&win[0][0][0])[e] = 0;
+        for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0;
       if (count)
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
       __syncthreads();
@@ -911,35 +951,35 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
           if (mode & 8) {
             const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
             const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
-            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
+            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ && fabsf(q.vx) <= k.vwinf &&
+                fabsf(q.vy) <= k.vwinf && fabsf(q.vz) <= k.vwinf) {
               const int n0 = lk * kSZ + lj * kSY + li;
 #pragma unroll
               for (int bc = 0; bc < 8; bc++) {
                 const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
                 const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
                 const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
+                int hi, lo;
+                k.fixn32.split(val[0], hi, lo);
+                atomicAdd(&win[0][nb], hi);
+                atomicAdd(&win[1][nb], lo);
 #pragma unroll
-                for (int f = 0; f < 4; f++) {
-                  int hi, lo;
-                  (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
-                  atomicAdd(&win[f][0][nb], hi);
-                  atomicAdd(&win[f][1][nb], lo);
-                }
+                for (int f = 1; f < 4; f++) atomicAdd(&win[1 + f][nb], k.fixf32.word(val[f]));
               }
-            } else {  // outside the window: straight into the global accumulators
+            } else {  // outside the window, or fast: straight into the global accumulators
 #pragma unroll 1
               for (int bc = 0; bc < 8; bc++) {
                 const long long gnode = corner_node(k, q.i, q.j, q.kk, bc);
                 if (gnode < 0) continue;
                 const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
                 const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
+                int hi, lo;
+                k.fixn32.split(val[0], hi, lo);
+                atomicAdd((unsigned long long *)&acc[gnode], (unsigned long long)fix_join(hi, lo));
 #pragma unroll
-                for (int f = 0; f < 4; f++) {
-                  int hi, lo;
-                  (f == 0 ? k.fixn32 : k.fixf32).split(val[f], hi, lo);
+                for (int f = 1; f < 4; f++)
                   atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + gnode],
-                            (unsigned long long)fix_join(hi, lo));
-                }
+                            (unsigned long long)(long long)k.fixf32.word(val[f]));
               }
             }
           }
@@ -960,7 +1000,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
           unsigned long long *dst = (unsigned long long *)acc + ((size_t)gz * k.Ny + gy) * k.Nx + gx;
 #pragma unroll
           for (int f = 0; f < 4; f++) {
-            const long long v = fix_join(win[f][0][np_], win[f][1][np_]);
+            const long long v = f == 0 ? fix_join(win[0][np_], win[1][np_]) : (long long)win[1 + f][np_];
             if (v != 0) atomicAdd(dst + (size_t)f * k.ncell, (unsigned long long)v);
           }
         }
@@ -1251,9 +1291,11 @@ PartK make_k(const EcsCtx *ctx, double dt) {
   k.fixn64 = ldexp(1.0, ctx->shift_n);
   k.fixf64 = ldexp(1.0, ctx->shift_f);
   k.fixn32 = {ldexpf(1.0f, ctx->shift_n), ldexpf(1.0f, ctx->shift_n - kFixSplit), -ldexpf(1.0f, kFixSplit - ctx->shift_n)};
-  k.fixf32 = {ldexpf(1.0f, ctx->shift_f), ldexpf(1.0f, ctx->shift_f - kFixSplit), -ldexpf(1.0f, kFixSplit - ctx->shift_f)};
-  k.vmax = ldexp(1.0, ctx->shift_n - ctx->shift_f);
+  k.fixf32 = {ldexpf(1.0f, ctx->shift_f)};
+  // the velocity bound 2^e_v behind the flux scale (ecs_fix_shifts)
+  k.vmax = ldexp(1.0, (ctx->prec == ECS_PREC_FP64 ? ECS_FIX_SHIFT_FP64 : ECS_FIX_SHIFT_MIXED_FLUX) - ctx->shift_f);
   k.vmaxf = (float)k.vmax;
+  k.vwinf = (float)(k.vmax / 8.0);
   k.tg = {ctx->ntile[0], ctx->ntile[1], ctx->ntile[2]};
   return k;
 }

@@ -221,8 +221,10 @@ int64_t ecs_launch_count(const EcsCtx *ctx);
 
 /* Fixed-point shifts of the deposition for these parameters: density
    contributions are rounded to multiples of 2^-shift_density and flux
-   contributions to multiples of 2^-shift_flux; |v| above
-   2^(shift_density - shift_flux) makes a deposit report ECS_ERR_RANGE. */
+   contributions to multiples of 2^-shift_flux.  The flux shift is
+   S_f - e_v, with S_f = 48 (FP64) or 22 (mixed) and 2^e_v the velocity bound
+   (16 (viT + vi0) rounded up to a power of two); |v| above 2^e_v makes a
+   deposit report ECS_ERR_RANGE. */
 int ecs_fix_shifts(const EcsParams *params, int precision, int32_t *shift_density, int32_t *shift_flux);
 
 #ifdef __cplusplus
