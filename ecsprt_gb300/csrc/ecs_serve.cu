@@ -40,6 +40,7 @@ bool same_params(const EcsParams &a, const EcsParams &b) {
 
 struct Slot {
   EcsCtx *ctx = nullptr;
+  cudaStream_t stream = nullptr;  // the slot's own stream, prioritised by grid size
   EcsParams p;
   int kind = ECS_SERVE_SOLVE;
   int64_t bytes = 0;
@@ -72,6 +73,7 @@ struct Job {
 struct EcsServer {
   EcsServeConfig cfg;
   int device = 0;
+  int prio_least = 0, prio_greatest = 0;  // the device's stream priority range
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Job *> pending;  // submitted, not admitted (served in order)
@@ -159,6 +161,33 @@ Job *take_work(EcsServer *s, std::vector<Slot *> &evict) {
   return nullptr;
 }
 
+// A slot's context on a stream of its own whose priority grows with the
+// grid (8 cells a step of the range from 2^15 cells on): a large solve is not
+// starved by the small ones around it, which keeps the latency tail short.
+int create_slot_ctx(EcsServer *s, Slot *sl, const EcsParams &p, int64_t np) {
+  const int64_t n = (int64_t)p.Nx * p.Ny * p.Nz;
+  int level = 0;
+  for (int64_t c = (int64_t)1 << 15; c < n && level < 8; c <<= 3) level++;
+  int prio = s->prio_least - level;  // numerically smaller is higher priority
+  if (prio < s->prio_greatest) prio = s->prio_greatest;
+  if (cudaStreamCreateWithPriority(&sl->stream, cudaStreamNonBlocking, prio) != cudaSuccess) {
+    cudaGetLastError();
+    sl->stream = nullptr;
+  }
+  const int rc = ecs_ctx_create(&p, s->cfg.precision, np, sl->stream, &sl->ctx);
+  if (rc && sl->stream) {
+    cudaStreamDestroy(sl->stream);
+    sl->stream = nullptr;
+  }
+  return rc;
+}
+void destroy_slot_ctx(Slot *sl) {
+  if (sl->ctx) ecs_ctx_destroy(sl->ctx);
+  if (sl->stream) cudaStreamDestroy(sl->stream);
+  sl->ctx = nullptr;
+  sl->stream = nullptr;
+}
+
 void fail(Job *j, int rc, const char *msg) {
   j->status = rc;
   snprintf(j->message, sizeof j->message, "%s", msg ? msg : ecs_status_string(rc));
@@ -180,7 +209,7 @@ void run_solve(EcsServer *s, Job *j) {
   Slot *sl = j->slot;
   int rc;
   if (j->fresh) {
-    if ((rc = ecs_ctx_create(&j->p, s->cfg.precision, 0, nullptr, &sl->ctx))) {
+    if ((rc = create_slot_ctx(s, sl, j->p, 0))) {
       fail(j, rc, ecs_last_error(nullptr));
       return;
     }
@@ -205,7 +234,7 @@ void run_sim_step(EcsServer *s, Job *j) {
   const EcsSimRequest &r = j->sim;
   int rc;
   if (j->fresh) {
-    if ((rc = ecs_ctx_create(&j->p, s->cfg.precision, r.np, nullptr, &sl->ctx))) {
+    if ((rc = create_slot_ctx(s, sl, j->p, r.np))) {
       fail(j, rc, ecs_last_error(nullptr));
       return;
     }
@@ -270,7 +299,7 @@ void worker_main(EcsServer *s) {
     s->peak_running = std::max(s->peak_running, s->running);
     lk.unlock();
     for (Slot *e : evict) {
-      ecs_ctx_destroy(e->ctx);
+      destroy_slot_ctx(e);
       delete e;
     }
     if (j->kind == ECS_SERVE_SOLVE) run_solve(s, j);
@@ -280,10 +309,7 @@ void worker_main(EcsServer *s) {
     const bool finished = j->kind == ECS_SERVE_SOLVE || j->status != ECS_OK || j->steps_done >= j->sim.nsteps;
     // a simulation's slot, or a slot whose context never came up, goes away
     const bool drop = finished && (j->kind == ECS_SERVE_SIM || !sl->ctx);
-    if (drop && sl->ctx) {
-      ecs_ctx_destroy(sl->ctx);
-      sl->ctx = nullptr;
-    }
+    if (drop) destroy_slot_ctx(sl);
     const double t_end = now_s();
     lk.lock();
     s->launches += nl - sl->launches_seen;
@@ -361,6 +387,10 @@ int ecs_serve_create(const EcsServeConfig *cfg, EcsServer **out) {
   if (!s) return ECS_ERR_NOMEM;
   s->cfg = *cfg;
   cudaGetDevice(&s->device);
+  if (cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest) != cudaSuccess) {
+    cudaGetLastError();
+    s->prio_least = s->prio_greatest = 0;
+  }
   for (int w = 0; w < cfg->max_inflight; w++) s->workers.emplace_back(worker_main, s);
   *out = s;
   return ECS_OK;
@@ -377,7 +407,7 @@ int ecs_serve_destroy(EcsServer *s) {
   for (Job *j : s->pending) delete j;
   for (Job *j : s->ready) delete j;
   for (Slot *sl : s->slots) {
-    if (sl->ctx) ecs_ctx_destroy(sl->ctx);
+    destroy_slot_ctx(sl);
     delete sl;
   }
   delete s;

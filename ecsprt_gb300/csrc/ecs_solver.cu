@@ -522,6 +522,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
 // ---- direct solve of the coarsest level -----------------------------------------
 constexpr int kDirectMax = 128;           // largest coarsest level solved directly
 constexpr size_t kInverseSmem = 160 * 1024;  // shared memory of its Gauss-Jordan work matrix
+// One block of 32 warps (fewer warps make a pivot step slower: the row
+// updates dominate, not the barriers).
+constexpr int kInvThreads = 1024;
 
 // invT = (A + sigma 1 1^T)^-1, transposed (invT[k n + r] = inv[r][k]), by
 // Gauss-Jordan elimination with partial pivoting on M = [A | I] (n x 2n, in
@@ -530,7 +533,7 @@ constexpr size_t kInverseSmem = 160 * 1024;  // shared memory of its Gauss-Jorda
 // operator is regular.  Pivot ties go to the lowest row, so the result is
 // reproducible.
 template <typename T>
-__global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restrict__ dens, int regularize,
+__global__ void __launch_bounds__(kInvThreads) k_coarse_inverse(OpK o, const T *__restrict__ dens, int regularize,
                                                          T *__restrict__ Mg, T *__restrict__ invT) {
   extern __shared__ unsigned char inv_smem[];
   T *M = Mg ? Mg : reinterpret_cast<T *>(inv_smem);  // work matrix in shared memory when it fits
@@ -574,8 +577,7 @@ __global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restr
     for (int e = tid; e < n * n; e += bs) M[(size_t)(e / n) * w + (e % n)] += sigma;
     __syncthreads();
   }
-  // elimination with a 32 x 32 thread grid: rows by threadIdx.y, columns by
-  // threadIdx.x (the block is launched as 32 x 32)
+  // elimination: rows by warp, columns by lane
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int c = 0; c < n; c++) {
     // pivot: largest |M[r][c]|, r >= c, lowest row on ties (warp 0)
@@ -610,7 +612,7 @@ __global__ void __launch_bounds__(1024) k_coarse_inverse(OpK o, const T *__restr
     for (int e = threadIdx.x; e < w; e += blockDim.x) M[(size_t)c * w + e] *= ip;
     for (int r = threadIdx.x; r < n; r += blockDim.x) fac[r] = r == c ? T(0) : M[(size_t)r * w + c];
     __syncthreads();
-    for (int r = ty; r < n; r += 32) {
+    for (int r = ty; r < n; r += bs >> 5) {
       const T f = fac[r];
       if (f != T(0))
         for (int q = tx; q < w; q += 32) M[(size_t)r * w + q] -= f * M[(size_t)c * w + q];
@@ -1081,7 +1083,7 @@ int mg_setup(EcsCtx *ctx) {
       ECS_CUDA(ctx, cudaFuncSetAttribute(k_coarse_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInverseSmem));
       attr_set[sizeof(T) == 8] = true;
     }
-    k_coarse_inverse<T><<<1, 1024, in_smem ? bytes : 0, ctx->stream>>>(
+    k_coarse_inverse<T><<<1, kInvThreads, in_smem ? bytes : 0, ctx->stream>>>(
         op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, in_smem ? nullptr : mg.cwork, mg.cinv);
     ECS_LAUNCHED(ctx);
   }
