@@ -53,6 +53,8 @@ struct KrylovDev {
   double h1[kSlots], h2[kSlots];
   double H[(kKrylovMax + 1) * kKrylovMax];
   double cs[kKrylovMax], sn[kKrylovMax], g[kKrylovMax + 1], y[kKrylovMax];
+  // completion tickets of the grid-wide reductions (0 between launches)
+  unsigned int ticket[8];
 };
 
 // ---- operator ------------------------------------------------------------------
@@ -648,6 +650,104 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// W consecutive elements of a vector.  W = kPack<T> (4 floats, 2 doubles)
+// moves them with one 16-byte access: the caller guarantees the alignment
+// (a basis vector of n cells starts on a 16-byte boundary when n % 4 == 0);
+// W = 1 is the plain form.
+template <typename T>
+constexpr int kPack = 16 / (int)sizeof(T);
+template <typename T, int W>
+struct Pack {
+  T v[W];
+};
+template <typename T, int W>
+__device__ __forceinline__ Pack<T, W> ld_pack(const T *__restrict__ p) {
+  Pack<T, W> r;
+  if constexpr (W == 4 && sizeof(T) == 4) {
+    const float4 f = *reinterpret_cast<const float4 *>(p);
+    r.v[0] = f.x; r.v[1] = f.y; r.v[2] = f.z; r.v[3] = f.w;
+  } else if constexpr (W == 2 && sizeof(T) == 8) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    r.v[0] = a.x; r.v[1] = a.y;
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; i++) r.v[i] = p[i];
+  }
+  return r;
+}
+template <typename T, int W>
+__device__ __forceinline__ void st_pack(T *__restrict__ p, const Pack<T, W> &r) {
+  if constexpr (W == 4 && sizeof(T) == 4) {
+    *reinterpret_cast<float4 *>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else if constexpr (W == 2 && sizeof(T) == 8) {
+    *reinterpret_cast<double2 *>(p) = make_double2(r.v[0], r.v[1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; i++) p[i] = r.v[i];
+  }
+}
+
+// Completion ticket of a grid-wide reduction: true in the block that
+// finishes last, to which every block's partials (written before the call)
+// are then visible; it reads them through L2 (__ldcg).  That block puts the
+// counter back to 0 for the next launch.  No block waits on another.
+__device__ __forceinline__ bool last_block(unsigned int *ticket) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(ticket, 1u);
+    last = t == gridDim.x - 1;
+    if (last) {
+      *ticket = 0u;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  return last != 0;
+}
+
+// partial[blockIdx.x] = the block's sum of the threads' values (Kahan runs
+// in T, warps in T, the block's warps in FP64).
+template <typename T>
+__device__ __forceinline__ void block_partial(const KSum<T> &acc, double *__restrict__ partial) {
+  __shared__ double sh[32];
+  const T t = warp_sum(acc.value());
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+    partial[blockIdx.x] = u;
+  }
+}
+
+// Sum of partial[0..nb) in a fixed order, valid in thread 0 (the last block).
+__device__ __forceinline__ double partials_total(const double *partial, int nb) {
+  __shared__ double sh[32];
+  double t = 0.0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += __ldcg(partial + q);
+  t = warp_sum(t);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  double u = 0.0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
+  return u;
+}
+
+// out[q] = sum over blocks of slot q's partials (partial[q * nb + b]), one
+// warp a slot, for slots 0..ns.
+__device__ __forceinline__ void slot_totals(const double *partial, int ns, int nb, double *out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int q = warp; q < ns; q += (int)(blockDim.x >> 5)) {
+    double t = 0.0;
+    for (int b = lane; b < nb; b += 32) t += __ldcg(partial + (size_t)q * nb + b);
+    t = warp_sum(t);
+    if (lane == 0) out[q] = t;
+  }
+}
+
 // x64 += a * e (e in T)
 template <typename T>
 __global__ void k_axpy64(size_t n, double a, const T *__restrict__ e, double *__restrict__ x) {
@@ -660,37 +760,6 @@ __global__ void k_scale_to(size_t n, const double *__restrict__ s, const double 
   const T a = (T)scale[0];
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     d[q] = (T)s[q] * a;
-}
-// partial[block] = sum of v over the block's elements (FP64 accumulation)
-template <typename T>
-__global__ void k_sum_partial(size_t n, const T *__restrict__ v, double *__restrict__ partial) {
-  __shared__ double sh[32];
-  KSum<T> acc;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-    acc.add(v[e]);
-  const T t = warp_sum(acc.value());
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double u = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
-    partial[blockIdx.x] = u;
-  }
-}
-// out[0] = (sum of partial[0..nb)) / div, one block, fixed order
-__global__ void __launch_bounds__(1024) k_final_sum(int nb, const double *__restrict__ partial, double div,
-                                                    double *__restrict__ out) {
-  __shared__ double sh[32];
-  double t = 0.0;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double u = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
-    out[0] = u / div;
-  }
 }
 // v -= value[0]
 template <typename T>
@@ -723,86 +792,47 @@ __device__ __forceinline__ void block_chunk(const KSum<T> (&acc)[kChunk], int v0
   __syncthreads();
 }
 
-// Pass 1 of classical Gram-Schmidt: partial dots of V_0..V_j with w = V_{j+1}.
-template <typename T>
-__global__ void __launch_bounds__(kB) k_dots1(size_t n, const T *__restrict__ V, const KrylovDev *__restrict__ kd,
-                                              double *__restrict__ partial) {
+// Pass 1 of classical Gram-Schmidt: dots of V_0..V_j with w = V_{j+1}.
+// Block partials, then the last block forms h1[q] (one warp a slot).  Packs
+// of W cells; one resident wave of blocks (4 an SM), so that every thread
+// has its loads of several packs in flight.
+template <typename T, int W>
+__global__ void __launch_bounds__(kB, 4) k_dots1(size_t n, const T *__restrict__ V, KrylovDev *__restrict__ kd,
+                                                 double *__restrict__ partial) {
   const int nv = kd->j + 1;
   const T *w = V + (size_t)nv * n;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t nw = n / W, stride = (size_t)gridDim.x * blockDim.x;
   for (int v0 = 0; v0 < nv; v0 += kChunk) {
     KSum<T> acc[kChunk];
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-      const T we = w[e];
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += stride) {
+      const Pack<T, W> we = ld_pack<T, W>(w + e * W);
 #pragma unroll
       for (int q = 0; q < kChunk; q++)
-        if (v0 + q < nv) acc[q].add(V[(size_t)(v0 + q) * n + e] * we);
+        if (v0 + q < nv) {
+          const Pack<T, W> vq = ld_pack<T, W>(V + (size_t)(v0 + q) * n + e * W);
+#pragma unroll
+          for (int i = 0; i < W; i++) acc[q].add(vq.v[i] * we.v[i]);
+        }
     }
     block_chunk(acc, v0, nv, partial);
   }
+  if (!last_block(&kd->ticket[0])) return;
+  slot_totals(partial, nv, (int)gridDim.x, kd->h1);
 }
 
-// h1[q] = sum of the pass-1 partials of slot q (one warp per slot).
-__global__ void __launch_bounds__(1024) k_dots1_final(KrylovDev *kd, int nb, const double *__restrict__ partial) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nv = kd->j + 1;
-  if (warp >= nv) return;
-  double t = 0.0;
-  for (int b = lane; b < nb; b += 32) t += partial[(size_t)warp * nb + b];
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if (lane == 0) kd->h1[warp] = t;
-}
-
-// w = V_{j+1} - sum_q h1[q] V_q (stored, in the first slot chunk), then
-// pass 2: partial dots of V_0..V_j with the new w (slots 0..j) and of w with
-// itself (slot j+1).
-template <typename T>
-__global__ void __launch_bounds__(kB) k_orth1_dots2(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd,
-                                                    double *__restrict__ partial) {
-  __shared__ T h[kSlots];
-  const int nv = kd->j + 1, nslot = nv + 1;
-  if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h1[threadIdx.x] : T(0);
-  __syncthreads();
-  T *w = V + (size_t)nv * n;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (int v0 = 0; v0 < nslot; v0 += kChunk) {
-    KSum<T> acc[kChunk];
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
-      T s = w[e];
-      if (v0 == 0) {
-        for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
-        w[e] = s;
-      }
-#pragma unroll
-      for (int q = 0; q < kChunk; q++) {
-        const int v = v0 + q;
-        if (v < nv) acc[q].add(V[(size_t)v * n + e] * s);
-        else if (v == nv) acc[q].add(s * s);
-      }
-    }
-    block_chunk(acc, v0, nslot, partial);
-  }
-}
-
-// Arnoldi bookkeeping of step j (one block): reduce the pass-2 partials into
-// h2 and w.w, form column j of the Hessenberg matrix, apply the previous
-// Givens rotations and a new one, update the residual estimate and decide
-// whether the cycle stops.
-__global__ void __launch_bounds__(1024) k_arnoldi(KrylovDev *kd, int nb, const double *__restrict__ partial,
-                                                  cudaGraphConditionalHandle cond, int use_graph) {
+// Arnoldi bookkeeping of step j, in the last block of the pass-2 launch:
+// reduce the pass-2 partials into h2 and w.w, form column j of the
+// Hessenberg matrix, apply the previous Givens rotations and a new one,
+// update the residual estimate and decide whether the cycle stops.
+__device__ __forceinline__ void arnoldi_update(KrylovDev *kd, int nb, const double *partial,
+                                               cudaGraphConditionalHandle cond, int use_graph) {
   __shared__ double red[kSlots];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (kd->done) {  // stopped before this step (b = 0): keep the state
     if (threadIdx.x == 0 && use_graph) cudaGraphSetConditional(cond, 0u);
     return;
   }
   const int j = kd->j, nv = j + 1;
-  if (warp <= nv) {
-    double t = 0.0;
-    for (int b = lane; b < nb; b += 32) t += partial[(size_t)warp * nb + b];
-    for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-    if (lane == 0) red[warp] = t;
-  }
+  slot_totals(partial, nv + 1, nb, red);
   __syncthreads();
   if (threadIdx.x != 0) return;
   const int m = kKrylovMax;
@@ -841,9 +871,54 @@ __global__ void __launch_bounds__(1024) k_arnoldi(KrylovDev *kd, int nb, const d
   if (use_graph) cudaGraphSetConditional(cond, done ? 0u : 1u);
 }
 
+// w = V_{j+1} - sum_q h1[q] V_q (stored, in the first slot chunk), then
+// pass 2: partial dots of V_0..V_j with the new w (slots 0..j) and of w with
+// itself (slot j+1); the last block runs the Arnoldi bookkeeping.
+template <typename T, int W>
+__global__ void __launch_bounds__(kB, 4) k_orth1_dots2(size_t n, T *__restrict__ V, KrylovDev *__restrict__ kd,
+                                                       double *__restrict__ partial, cudaGraphConditionalHandle cond,
+                                                       int use_graph) {
+  __shared__ T h[kSlots];
+  const int nv = kd->j + 1, nslot = nv + 1;
+  if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h1[threadIdx.x] : T(0);
+  __syncthreads();
+  T *w = V + (size_t)nv * n;
+  const size_t nw = n / W, stride = (size_t)gridDim.x * blockDim.x;
+  for (int v0 = 0; v0 < nslot; v0 += kChunk) {
+    KSum<T> acc[kChunk];
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += stride) {
+      Pack<T, W> s = ld_pack<T, W>(w + e * W);
+      if (v0 == 0) {
+        for (int q = 0; q < nv; q++) {
+          const Pack<T, W> vq = ld_pack<T, W>(V + (size_t)q * n + e * W);
+          const T hq = h[q];
+#pragma unroll
+          for (int i = 0; i < W; i++) s.v[i] -= hq * vq.v[i];
+        }
+        st_pack<T, W>(w + e * W, s);
+      }
+#pragma unroll
+      for (int q = 0; q < kChunk; q++) {
+        const int v = v0 + q;
+        if (v < nv) {
+          const Pack<T, W> vq = ld_pack<T, W>(V + (size_t)v * n + e * W);
+#pragma unroll
+          for (int i = 0; i < W; i++) acc[q].add(vq.v[i] * s.v[i]);
+        } else if (v == nv) {
+#pragma unroll
+          for (int i = 0; i < W; i++) acc[q].add(s.v[i] * s.v[i]);
+        }
+      }
+    }
+    block_chunk(acc, v0, nslot, partial);
+  }
+  if (!last_block(&kd->ticket[1])) return;
+  arnoldi_update(kd, (int)gridDim.x, partial, cond, use_graph);
+}
+
 // V_{j+1} = (w - sum_q h2[q] V_q) / h_{j+1,j}, also copied to the
 // preconditioner input vin (j = the step that just finished).
-template <typename T>
+template <typename T, int W>
 __global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd, T *__restrict__ vin) {
   __shared__ T h[kSlots + 1];
   const int j = kd->jprev, nv = j + 1;
@@ -852,77 +927,80 @@ __global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__re
   __syncthreads();
   T *w = V + (size_t)(j + 1) * n;
   const T sc = h[kSlots];
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    T s = w[e];
-    for (int q = 0; q < nv; q++) s -= h[q] * V[(size_t)q * n + e];
-    s *= sc;
-    w[e] = s;
-    vin[e] = s;
+  const size_t nw = n / W;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += (size_t)gridDim.x * blockDim.x) {
+    Pack<T, W> s = ld_pack<T, W>(w + e * W);
+    for (int q = 0; q < nv; q++) {
+      const Pack<T, W> vq = ld_pack<T, W>(V + (size_t)q * n + e * W);
+      const T hq = h[q];
+#pragma unroll
+      for (int i = 0; i < W; i++) s.v[i] -= hq * vq.v[i];
+    }
+#pragma unroll
+    for (int i = 0; i < W; i++) s.v[i] *= sc;
+    st_pack<T, W>(w + e * W, s);
+    st_pack<T, W>(vin + e * W, s);
   }
 }
 
-// Z_j = zb - mean (mean = nullptr: plain copy)
+// Z_j = x - mean (mean = nullptr: x) and V_{j+1} = A Z_j.  Z_j is formed
+// at every stencil point on the fly, with the rounding of the stored value;
+// a mean is removed only on fully periodic grids, which have no ghosts.
 template <typename T>
-__global__ void k_store_z(size_t n, const T *__restrict__ zb, T *__restrict__ Z, const KrylovDev *__restrict__ kd,
-                          const double *__restrict__ mean) {
-  T *z = Z + (size_t)kd->j * n;
-  const T m = mean ? (T)mean[0] : T(0);
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-    z[e] = zb[e] - m;
-}
-
-// V_{j+1} = A Z_j
-template <typename T>
-__global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict__ Z, T *__restrict__ V,
-                            const KrylovDev *__restrict__ kd) {
+__global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict__ x, const double *__restrict__ mean,
+                            T *__restrict__ Z, T *__restrict__ V, const KrylovDev *__restrict__ kd) {
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const int jj = kd->j;
-  const T *x = Z + (size_t)jj * o.g.n;
-  V[(size_t)(jj + 1) * o.g.n + lin3(o.g, i, j, k)] = apply_row(n, x, o, i, j, k);
+  const T m = mean ? (T)mean[0] : T(0);
+  const unsigned c = lin3(o.g, i, j, k);
+  T v[11];
+  row11(n, o, i, j, k, v);
+  T s = T(0);
+#pragma unroll
+  for (int e = 0; e < 11; e++) s += v[e] * (gval(x, o.g, k + off_k(e), j + off_j(e), i + off_i(e)) - m);
+  Z[(size_t)jj * o.g.n + c] = x[c] - m;
+  V[(size_t)(jj + 1) * o.g.n + c] = s;
 }
 
-// Start of a cycle: beta = ||b|| from the ||b||^2 partials.  In a graph it
-// also (re)arms the Arnoldi loop's condition, which keeps its last value
-// between cycles of one launch.
-__global__ void __launch_bounds__(1024) k_cycle_init(KrylovDev *kd, int nb, const double *__restrict__ partial,
-                                                     cudaGraphConditionalHandle cond, int use_graph) {
-  __shared__ double sh[32];
-  double t = 0.0;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  double u = 0.0;
-  for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
-  const double beta = sqrt(u);
-  kd->beta = beta;
-  kd->res = beta;
-  kd->j = 0;
-  kd->jprev = 0;
-  kd->nits = 0;
-  kd->done = !(beta > 0.0) || kd->maxit < 1;
-  kd->inv_scale = beta > 0.0 ? 1.0 / beta : 0.0;
-  for (int q = 0; q <= kKrylovMax; q++) kd->g[q] = 0.0;
-  kd->g[0] = beta;
-  if (use_graph) cudaGraphSetConditional(cond, kd->done ? 0u : 1u);
-}
-
-// partial[block] = sum of b*b over the block (FP64 accumulation of T runs)
-template <typename T>
-__global__ void k_sq_partial(size_t n, const T *__restrict__ b, double *__restrict__ partial) {
-  __shared__ double sh[32];
+// Grid-wide sums of a vector in packs of W, finished by the last block:
+//   kRedMean  out[0] = sum(v) / div
+//   kRedNorm  out[0] = ||v||, out[1] = 1 / ||v|| (0 for v = 0)
+//   kRedBeta  start of an FGMRES cycle: beta = ||v|| into the control block;
+//             in a graph it also (re)arms the Arnoldi loop's condition,
+//             which keeps its last value between cycles of one launch.
+enum { kRedMean = 0, kRedNorm = 1, kRedBeta = 2 };
+template <typename T, int W, int M>
+__global__ void __launch_bounds__(kB) k_reduce(size_t nw, const T *__restrict__ v, double *__restrict__ partial,
+                                               double div, double *out, KrylovDev *kd,
+                                               cudaGraphConditionalHandle cond, int use_graph) {
   KSum<T> acc;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-    acc.add(b[e] * b[e]);
-  const T t = warp_sum(acc.value());
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double u = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
-    partial[blockIdx.x] = u;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += (size_t)gridDim.x * blockDim.x) {
+    const Pack<T, W> p = ld_pack<T, W>(v + e * W);
+#pragma unroll
+    for (int i = 0; i < W; i++) acc.add(M == kRedMean ? p.v[i] : p.v[i] * p.v[i]);
+  }
+  block_partial(acc, partial);
+  if (!last_block(&kd->ticket[2 + M])) return;
+  const double u = partials_total(partial, (int)gridDim.x);
+  if (threadIdx.x != 0) return;
+  if (M == kRedMean) {
+    out[0] = u / div;
+  } else if (M == kRedNorm) {
+    out[0] = sqrt(u);
+    out[1] = u > 0.0 ? 1.0 / sqrt(u) : 0.0;
+  } else {
+    const double beta = sqrt(u);
+    kd->beta = beta;
+    kd->res = beta;
+    kd->j = 0;
+    kd->jprev = 0;
+    kd->nits = 0;
+    kd->done = !(beta > 0.0) || kd->maxit < 1;
+    kd->inv_scale = beta > 0.0 ? 1.0 / beta : 0.0;
+    for (int q = 0; q <= kKrylovMax; q++) kd->g[q] = 0.0;
+    kd->g[0] = beta;
+    if (use_graph) cudaGraphSetConditional(cond, kd->done ? 0u : 1u);
   }
 }
 
@@ -971,7 +1049,30 @@ unsigned int blocks_for(const EcsCtx *ctx, size_t n) {
   if (want > cap) want = cap;
   return (unsigned int)(want ? want : 1);
 }
-unsigned int dot_blocks(const EcsCtx *ctx, size_t n) { return std::min(blocks_for(ctx, n), (unsigned)kDotBlocks); }
+// Grid of a reduction over `units` packs: at most one resident wave (4
+// blocks of kB threads an SM), so that no block starts after another's end.
+unsigned int dot_blocks(const EcsCtx *ctx, size_t units) {
+  size_t want = (units + kB - 1) / kB;
+  want = std::min(want, std::min((size_t)ctx->nsm * 4, (size_t)kDotBlocks));
+  return (unsigned int)(want ? want : 1);
+}
+// Vectors go in packs of 4 cells (16-byte accesses) when every basis vector
+// starts on a 16-byte boundary, i.e. when the cell count is a multiple of 4.
+inline bool packed4(size_t n) { return (n & 3) == 0; }
+
+// A grid-wide sum of v (kRed* mode M) on the context's stream.
+template <typename T, int M>
+int launch_reduce(EcsCtx *ctx, size_t n, const T *v, double div, double *out, cudaGraphConditionalHandle cond,
+                  int use_graph) {
+  KrylovDev *kd = (KrylovDev *)ctx->kdev;
+  constexpr int W = kPack<T>;
+  if (packed4(n))
+    k_reduce<T, W, M><<<dot_blocks(ctx, n / W), kB, 0, ctx->stream>>>(n / W, v, ctx->red, div, out, kd, cond, use_graph);
+  else
+    k_reduce<T, 1, M><<<dot_blocks(ctx, n), kB, 0, ctx->stream>>>(n, v, ctx->red, div, out, kd, cond, use_graph);
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
 
 bool fully_periodic(const EcsCtx *ctx) {
   return ctx->p.bc[0] == ECS_BC_PERIODIC && ctx->p.bc[1] == ECS_BC_PERIODIC && ctx->p.bc[2] == ECS_BC_PERIODIC;
@@ -1219,11 +1320,8 @@ int cycle_pre(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
   KrylovDev *kd = (KrylovDev *)ctx->kdev;
   Multigrid<T> &mg = mg_of<T>(ctx);
   const T *b = cycle_b<T>(ctx);
-  const unsigned nb = dot_blocks(ctx, n);
-  k_sq_partial<T><<<nb, kB, 0, ctx->stream>>>(n, b, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_cycle_init<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red, cond, use_graph);
-  ECS_LAUNCHED(ctx);
+  int rc = launch_reduce<T, kRedBeta>(ctx, n, b, 1.0, nullptr, cond, use_graph);
+  if (rc) return rc;
   k_cycle_start<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, b, basis_v<T>(ctx), mg.lv[0].b, cycle_x<T>(ctx), kd);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
@@ -1241,29 +1339,33 @@ int cycle_step(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
   int rc;
   // z = M v_j  (vin = L0.b holds v_j, the V-cycle writes L0.x)
   if ((rc = vcycle<T>(ctx, 0, L0.b, L0.x))) return rc;
-  const unsigned nb = dot_blocks(ctx, n);
   const double *mean = nullptr;
   if (fully_periodic(ctx)) {  // the operator's null space: project out the mean
-    k_sum_partial<T><<<nb, kB, 0, ctx->stream>>>(n, L0.x, ctx->red);
-    ECS_LAUNCHED(ctx);
-    k_final_sum<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, (double)n, &kd->mean);
-    ECS_LAUNCHED(ctx);
+    if ((rc = launch_reduce<T, kRedMean>(ctx, n, L0.x, (double)n, &kd->mean, cond, use_graph))) return rc;
     mean = &kd->mean;
   }
-  k_store_z<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, L0.x, Z, kd, mean);
+  k_apply_dyn<T><<<blocks3(o0.g), threads3(), 0, ctx->stream>>>(o0, L0.dens, L0.x, mean, Z, V, kd);
   ECS_LAUNCHED(ctx);
-  k_apply_dyn<T><<<blocks3(o0.g), threads3(), 0, ctx->stream>>>(o0, L0.dens, Z, V, kd);
-  ECS_LAUNCHED(ctx);
-  // classical Gram-Schmidt, two passes
-  k_dots1<T><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_dots1_final<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_orth1_dots2<T><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_arnoldi<<<1, 1024, 0, ctx->stream>>>(kd, (int)nb, ctx->red, cond, use_graph);
-  ECS_LAUNCHED(ctx);
-  k_orth2_scale<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
+  // classical Gram-Schmidt, two passes (the second ends with the Arnoldi
+  // bookkeeping)
+  constexpr int W = kPack<T>;
+  if (packed4(n)) {
+    const unsigned nb = dot_blocks(ctx, n / W);
+    k_dots1<T, W><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+    ECS_LAUNCHED(ctx);
+    k_orth1_dots2<T, W><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red, cond, use_graph);
+    ECS_LAUNCHED(ctx);
+  } else {
+    const unsigned nb = dot_blocks(ctx, n);
+    k_dots1<T, 1><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+    ECS_LAUNCHED(ctx);
+    k_orth1_dots2<T, 1><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red, cond, use_graph);
+    ECS_LAUNCHED(ctx);
+  }
+  if (packed4(n))
+    k_orth2_scale<T, W><<<blocks_for(ctx, n / W), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
+  else
+    k_orth2_scale<T, 1><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1304,39 +1406,17 @@ int fgmres_cycle(EcsCtx *ctx, double tol, int maxit) {
   return cycle_post<T>(ctx);
 }
 
-// ||v||_2 of an FP64 vector into dst[0] on the device.
-__global__ void __launch_bounds__(1024) k_final_norm(int nb, const double *__restrict__ partial, double *__restrict__ out) {
-  __shared__ double sh[32];
-  double t = 0.0;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) t += partial[q];
-  for (int s = 16; s >= 1; s >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double u = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) u += sh[q];
-    out[0] = sqrt(u);
-    out[1] = u > 0.0 ? 1.0 / sqrt(u) : 0.0;
-  }
-}
+// ||v||_2 of an FP64 vector into out2[0], its inverse into out2[1], on the device.
 int norm64_dev(EcsCtx *ctx, const double *v, double *out2) {
-  const unsigned nb = dot_blocks(ctx, ctx->ncell);
-  k_sq_partial<double><<<nb, kB, 0, ctx->stream>>>(ctx->ncell, v, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_final_norm<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, out2);
-  ECS_LAUNCHED(ctx);
-  return ECS_OK;
+  return launch_reduce<double, kRedNorm>(ctx, ctx->ncell, v, 1.0, out2, 0, 0);
 }
 
 template <typename T>
 int project_mean(EcsCtx *ctx, T *v) {
   if (!fully_periodic(ctx)) return ECS_OK;
   size_t n = ctx->ncell;
-  unsigned int nb = dot_blocks(ctx, n);
-  k_sum_partial<T><<<nb, kB, 0, ctx->stream>>>(n, v, ctx->red);
-  ECS_LAUNCHED(ctx);
-  k_final_sum<<<1, 1024, 0, ctx->stream>>>((int)nb, ctx->red, (double)n, ctx->dots + 2);
-  ECS_LAUNCHED(ctx);
+  int rc = launch_reduce<T, kRedMean>(ctx, n, v, (double)n, ctx->dots + 2, 0, 0);
+  if (rc) return rc;
   k_sub_value<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, v, ctx->dots + 2);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
