@@ -331,6 +331,30 @@ def test_tile_deposit_matches_warp_deposit(built, grid, zbc):
         assert m_tile[..., 0].sum() == pytest.approx(npart, rel=1e-9)
 
 
+@pytest.mark.parametrize("nui", [0.05, 3.0])
+def test_tile_step_matches_warp_step_with_collisions(built, nui):
+    """A full step with collisions: the tile kernel and the order-free kernel
+    give the same ions (as a set), collision count and moments, bit for bit,
+    at a low rate and at a rate of about one collision per ion."""
+    opts, _, pos, vel = c1_like(n=12, ppc=16, mn=True)
+    p = E.params_from_options(opts.replace("-nui 0.05", f"-nui {nui}"))
+    out = []
+    for every in (1, 0):
+        with E.Context(p, E.ECS_PREC_MIXED, np_capacity=pos.shape[0]) as ctx:
+            ctx.set_sort_every(every)
+            ctx.upload_particles(pos, vel)
+            ctx.collect()
+            ctx.compute_potential(rtol=1e-8, max_it=400)
+            st = ctx.step(0.1, rtol=1e-8, max_it=400)
+            gp, gv = ctx.download_particles()
+            rows = np.hstack([gp, gv])
+            out.append((st.collisions, ctx.moments, rows[np.lexsort(rows.T[::-1])]))
+    print(f"nui {nui}: {out[0][0]} collisions of {pos.shape[0]} ions")
+    assert out[0][0] == out[1][0] and out[0][0] > 0
+    bit_equal(out[0][1], out[1][1])
+    bit_equal(out[0][2], out[1][2])
+
+
 def test_sorting_preserves_particles(built):
     opts, p, pos, vel = c1_like(n=16, ppc=8, mn=False)
     got = []
