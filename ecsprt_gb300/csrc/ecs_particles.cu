@@ -783,6 +783,12 @@ __device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, 
 
 constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
 constexpr int kWNodes = kWX * kWY * kWZ;
+// Padded strides of the field window (float4 a node).  A 16-byte shared load
+// is served 8 lanes at a time; with the ions sorted, those 8 lanes sit in a
+// 4 x 2 block of cells of one z plane, and lx + 12 ly takes 8 different
+// values mod 8 there, so the eight corner loads are free of bank conflicts.
+constexpr int kEX = 12, kEXY = kEX * kWY;
+static_assert(kWX <= kEX, "field window stride");
 // Padded strides of the deposit window: the 32 cells of a tile (one lane
 // each when the ions are sorted) map to 32 different shared-memory banks,
 // lx + 12 ly + 112 lz taking every value mod 32 once for lx, ly < 4, lz < 2.
@@ -803,7 +809,7 @@ struct IonState {
   float ox, oy, oz, vx, vy, vz;
 };
 // Ew (nullptr: none) is a window of the difference numerators in shared
-// memory, kWX x kWY x kWZ nodes from node (wx0, wy0, wz0).
+// memory, kWX x kWY x kWZ nodes from node (wx0, wy0, wz0) at strides kEX, kEXY.
 __device__ __forceinline__ void ion_update(const PartK &k, int mode, const float4 *__restrict__ E, EcsDevStatus *st,
                                            IonState &q, unsigned int &nacc, unsigned int &nref,
                                            const float4 *Ew = nullptr, int wx0 = 0, int wy0 = 0, int wz0 = 0) {
@@ -811,10 +817,10 @@ __device__ __forceinline__ void ion_update(const PartK &k, int mode, const float
     float f[3];
     const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
     if (Ew && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
-      const int base = (lk * kWY + lj) * kWX + li;
+      const int base = lk * kEXY + lj * kEX + li;
       float4 D[8];
 #pragma unroll
-      for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kWX, kWX * kWY, b)];
+      for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kEX, kEXY, b)];
       interp8(D, q.ox, q.oy, q.oz, f);
     } else {
       gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
@@ -907,7 +913,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
                                                      int32_t *__restrict__ count, EcsDevStatus *st) {
   __shared__ int win[5][kWPad];  // [density H, density rint(r), flux x, y, z][node, padded strides]
   __shared__ int wcnt[kWCells];
-  __shared__ float4 ewin[kWNodes];    // difference numerators of the window's nodes
+  __shared__ float4 ewin[kEXY * kWZ];  // difference numerators of the window's nodes (padded strides)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = k.tg.ntx * k.tg.nty * k.tg.ntz;
   unsigned int nacc = 0, nref = 0;  // collision counters of this thread, flushed at the end
@@ -922,7 +928,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
       for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
         const int gx = wx0 + e % kWX, gy = wy0 + (e / kWX) % kWY, gz = wz0 + e / (kWX * kWY);
         const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
-        ewin[e] = in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        ewin[(gz - wz0) * kEXY + (gy - wy0) * kEX + (gx - wx0)] =
+            in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
     for (int ca = a; ca < b; ca += kWindowMax) {
