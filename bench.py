@@ -47,7 +47,11 @@ WORKLOAD = {
     "n": 128, "ppc": 64, "dt": 0.1, "drift": 1.0, "nu": 0.02, "seed": 20261205,
 }
 SORT_EVERY = 2          # cell sort cadence of the mixed path
-ALGO_BYTES_MIXED = 64   # per particle-step: one 32-byte ion record read + written
+# per particle-step: one 32-byte ion record read + written, and 4 bytes of the
+# index sort (the permutation read by the pass after a sort, or the cell key
+# written by the counting pass before one; with a sort every 2 steps each pass
+# moves one of the two)
+ALGO_BYTES_MIXED = 68
 ALGO_BYTES_FP64 = 96    # per particle-step: 6 FP64 read + written
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ion of one
 # k_tiles32 step launch, measured by ncu on the 64^3 x 64 ppc case of this

@@ -123,7 +123,7 @@ int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
     b += cap * 48 + ne * 32;   // ions (6 FP64), E numerators
   } else {
     b += (2 * m + 3) * n * 4;  // Krylov bases V, Z, two FP32 work vectors
-    b += cap * 64 + ne * 16;   // ions (two 32-byte record buffers), E numerators
+    b += cap * 72 + ne * 16;   // ions (two 32-byte record buffers, sort keys, permutation), E numerators
     const int64_t keys = (int64_t)((p->Nx + ECS_TILE_X - 1) / ECS_TILE_X) * ((p->Ny + ECS_TILE_Y - 1) / ECS_TILE_Y) *
                          ((p->Nz + ECS_TILE_Z - 1) / ECS_TILE_Z) * ECS_TILE_CELLS;
     b += keys * 4 * 2 + keys / 1024 * 4;  // sort counts and offsets

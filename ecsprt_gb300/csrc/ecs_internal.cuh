@@ -129,6 +129,11 @@ struct EcsCtx {
   int32_t *sort_offset = nullptr;  // [nkeys+1]: ions of key q at [offset[q], offset[q+1])
   int32_t *scan_blocks = nullptr;  // block sums of the scan
   bool tiles_valid = false;        // the buffer is ordered by the keys of sort_offset
+  // Index sort: the counting sort writes the permutation only, and the next
+  // particle pass reads ions[cur][perm[i]] and writes ions[1 - cur][i].
+  int32_t *sort_keys = nullptr;    // [cap] key of each ion's cell, by buffer position (counting passes)
+  int32_t *perm = nullptr;         // [cap] buffer position of the i-th ion in key order
+  bool perm_pending = false;       // ions[cur] is in key order only through perm
   int sort_every = 2;
   int steps_since_sort = 0;
 

@@ -872,7 +872,8 @@ __device__ __forceinline__ Ion ion_record(const IonState &q) {
 __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, int64_t np, float4 *ions,
                                                          const float4 *__restrict__ E,
                                                          long long *__restrict__ acc,
-                                                         int32_t *__restrict__ count, EcsDevStatus *st) {
+                                                         int32_t *__restrict__ count, int32_t *__restrict__ keys,
+                                                         EcsDevStatus *st) {
   extern __shared__ long long shm_tiles[];
   long long *tile = shm_tiles + (threadIdx.x >> 5) * 32 * kTileStride;
   const int64_t lane = threadIdx.x & 31;
@@ -885,7 +886,11 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
     unsigned int nacc = 0, nref = 0;
     if (active) ion_update(k, mode, E, st, q, nacc, nref);
     if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
-    if (count) count_cells(count, active ? tile_key(q.i, q.j, q.kk, k.tg) : -1);
+    if (count) {
+      const int key = active ? tile_key(q.i, q.j, q.kk, k.tg) : -1;
+      if (active) keys[ip] = key;
+      count_cells(count, key);
+    }
     if (mode & 8)
       deposit_warp<float>(acc, tile, k, active, q.i, q.j, q.kk, q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, k.fixn32,
                           k.fixf32);
@@ -908,9 +913,11 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
 // sort follows.  All sums are exact integers, so the moments equal those of
 // k_particles32 bit for bit.
 
-__global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4 *ions, const float4 *__restrict__ E,
+__global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const float4 *src, float4 *dst,
+                                                     const int32_t *__restrict__ perm, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
-                                                     int32_t *__restrict__ count, EcsDevStatus *st) {
+                                                     int32_t *__restrict__ count, int32_t *__restrict__ keys,
+                                                     EcsDevStatus *st) {
   __shared__ int win[5][kWPad];  // [density H, density rint(r), flux x, y, z][node, padded strides]
   __shared__ int wcnt[kWCells];
   __shared__ float4 ewin[kEXY * kWZ];  // difference numerators of the window's nodes (padded strides)
@@ -945,15 +952,18 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
         const int si = warp * sub + m, qi = lane * seg + si;
         const bool active = si < seg && qi < L;
         const int64_t ip = (int64_t)ca + qi;
-        IonState q = ion_state(active ? load_ion_ro(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
+        const int64_t sp = (perm && active) ? (int64_t)__ldg(perm + ip) : ip;
+        IonState q = ion_state(active ? load_ion_ro(src, sp) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
         if (active) ion_update(k, mode, E, st, q, nacc, nref, ewin, wx0, wy0, wz0);
         if (active) {
           const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
           if (count) {
+            const int key = tile_key(q.i, q.j, q.kk, k.tg);
+            keys[ip] = key;
             if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ)
               atomicAdd(&wcnt[(lk * kCY + lj) * kCX + li], 1);
             else
-              atomicAdd(&count[tile_key(q.i, q.j, q.kk, k.tg)], 1);
+              atomicAdd(&count[key], 1);
           }
           if (mode & 8) {
             const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
@@ -990,7 +1000,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, float4
               }
             }
           }
-          if (mode & 7) store_ion(ions, ip, ion_record(q));
+          if (mode & 7) store_ion(dst, ip, ion_record(q));
         }
       }
       __syncthreads();
@@ -1096,12 +1106,15 @@ __global__ void k_mixed_to_aos(int64_t n, int nd, PartK k, double *__restrict__ 
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
-__global__ void k_sort_count(int64_t np, TileG tg, const float4 *__restrict__ ions, int32_t *__restrict__ count) {
+__global__ void k_sort_count(int64_t np, TileG tg, const float4 *__restrict__ ions, int32_t *__restrict__ count,
+                             int32_t *__restrict__ keys) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ip = base + lane;
-    count_cells(count, ip < np ? cell_key(ion_cell(ions, ip), tg) : -1);
+    const int key = ip < np ? cell_key(ion_cell(ions, ip), tg) : -1;
+    if (ip < np) keys[ip] = key;
+    count_cells(count, key);
   }
 }
 
@@ -1181,29 +1194,35 @@ __global__ void k_scan_add(int n, int32_t *__restrict__ out, const int32_t *__re
 // Every ion record moves whole (32 bytes, one sector) to slot
 // off[key] + (its rank among the ions of its cell), ranks handed out by a
 // warp-aggregated atomic cursor per cell.
-__global__ void k_sort_scatter(int64_t np, TileG tg, const int32_t *__restrict__ off,
-                               int32_t *__restrict__ cursor, const float4 *__restrict__ src,
-                               float4 *__restrict__ dst) {
+// The counting sort's permutation: perm[d] = the buffer position of the ion
+// that goes to position d in key order (keys[ip] from the counting pass).
+// Within a key the order follows the atomics; nothing depends on it (the
+// moments are exact sums and each ion's random numbers come from its state).
+// Only 4-byte indices move: the next particle pass reads the 32-byte records
+// through perm and writes them in key order into the other buffer.
+__global__ void k_sort_index(int64_t np, const int32_t *__restrict__ keys, const int32_t *__restrict__ off,
+                             int32_t *__restrict__ cursor, int32_t *__restrict__ perm) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < np;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ip = base + lane;
-    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-    if (ip < np) {
-      a = __ldcs(src + 2 * ip);
-      b = __ldcs(src + 2 * ip + 1);
-    }
-    const int key = ip < np ? cell_key(__float_as_int(a.x), tg) : -1;
+    const int key = ip < np ? __ldcs(keys + ip) : -1;
     const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
     const int leader = __ffs(peers) - 1;
     int slot = 0;
     if (key >= 0 && lane == leader) slot = atomicAdd(&cursor[key], __popc(peers));
     slot = __shfl_sync(ECS_FULL_MASK, slot, leader);
-    if (key >= 0) {
-      const int64_t d = (int64_t)off[key] + slot + __popc(peers & ((1u << lane) - 1u));
-      __stcs(dst + 2 * d, a);
-      __stcs(dst + 2 * d + 1, b);
-    }
+    if (key >= 0) perm[(int64_t)off[key] + slot + __popc(peers & ((1u << lane) - 1u))] = (int32_t)ip;
+  }
+}
+
+// dst[i] = src[perm[i]]: the records of a pending sort put in key order.
+__global__ void k_gather_ions(int64_t np, const int32_t *__restrict__ perm, const float4 *__restrict__ src,
+                              float4 *__restrict__ dst) {
+  for (int64_t ip = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ip < np; ip += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sp = perm[ip];
+    __stcs(dst + 2 * ip, __ldcs(src + 2 * sp));
+    __stcs(dst + 2 * ip + 1, __ldcs(src + 2 * sp + 1));
   }
 }
 
@@ -1463,6 +1482,8 @@ int ecs_particles_alloc(EcsCtx *ctx) {
     for (auto a : arr) ECS_CUDA(ctx, cudaMalloc((void **)a, n * sizeof(double)));
   } else {
     for (int b = 0; b < 2; b++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->ions[b], n * 2 * sizeof(float4)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->sort_keys, n * sizeof(int32_t)));
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->perm, n * sizeof(int32_t)));
     ctx->ntile[0] = (ctx->p.Nx + ECS_TILE_X - 1) / ECS_TILE_X;
     ctx->ntile[1] = (ctx->p.Ny + ECS_TILE_Y - 1) / ECS_TILE_Y;
     ctx->ntile[2] = (ctx->p.Nz + ECS_TILE_Z - 1) / ECS_TILE_Z;
@@ -1479,7 +1500,7 @@ void ecs_part_xfer_free(EcsCtx *ctx);
 int ecs_particles_free(EcsCtx *ctx) {
   ecs_part_xfer_free(ctx);
   void *ptrs[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ions[0], ctx->ions[1],
-                  ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
+                  ctx->sort_keys, ctx->perm, ctx->sort_count, ctx->sort_offset, ctx->scan_blocks};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   return ECS_OK;
@@ -1549,6 +1570,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
   ctx->np = np;
   ctx->attempt_rate = -1.0;
   ctx->tiles_valid = false;
+  ctx->perm_pending = false;
   if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
     rc = ecs_part_sort(ctx);
     if (rc) return rc;
@@ -1619,10 +1641,26 @@ int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDen
   ctx->np = np;
   ctx->attempt_rate = -1.0;
   ctx->tiles_valid = false;
+  ctx->perm_pending = false;
   if (ctx->prec == ECS_PREC_MIXED && ctx->sort_every > 0 && np > 0) {
     int rc = ecs_part_sort(ctx);
     if (rc) return rc;
   }
+  return ECS_OK;
+}
+
+// Puts the records of a pending index sort into key order in the other
+// buffer (the particle passes read through the permutation instead; the
+// host transfers and the order-free kernel need the records themselves).
+static int settle_order(EcsCtx *ctx) {
+  if (!ctx->perm_pending) return ECS_OK;
+  if (ctx->np > 0) {
+    k_gather_ions<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, ctx->perm, ctx->ions[ctx->cur],
+                                                                          ctx->ions[1 - ctx->cur]);
+    ECS_LAUNCHED(ctx);
+    ctx->cur = 1 - ctx->cur;
+  }
+  ctx->perm_pending = false;
   return ECS_OK;
 }
 
@@ -1631,6 +1669,7 @@ int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDen
 int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
   int rc = ensure_xfer(ctx);
   if (rc) return rc;
+  if ((rc = settle_order(ctx))) return rc;
   const int64_t chunk = ctx->stage_n;
   const int nd = ctx->p.ndim == 2 ? 2 : 3;
   const int64_t np = ctx->np;
@@ -1707,12 +1746,23 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
     k_particles64<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                                 ctx->vy, ctx->vz, ctx->eext64, ctx->acc, ctx->dstat);
   } else if (ctx->tiles_valid) {
+    // after an index sort the pass reads the records through the permutation
+    // and, if it writes them, leaves them in key order in the other buffer
     const int ntiles = ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2];
-    k_tiles32<<<ntiles, kBlock, 0, ctx->stream>>>(k, mode, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
-                                                  ctx->sort_offset, count, ctx->dstat);
+    const bool gather = ctx->perm_pending, writes = (mode & 7) != 0;
+    float4 *src = ctx->ions[ctx->cur];
+    float4 *dst = gather ? ctx->ions[1 - ctx->cur] : src;
+    k_tiles32<<<ntiles, kBlock, 0, ctx->stream>>>(k, mode, src, dst, gather ? ctx->perm : nullptr, ctx->eext32,
+                                                  ctx->acc, ctx->sort_offset, count, ctx->sort_keys, ctx->dstat);
+    if (gather && writes) {
+      ctx->cur = 1 - ctx->cur;
+      ctx->perm_pending = false;
+    }
   } else {
+    int rc = settle_order(ctx);
+    if (rc) return rc;
     k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
-                                                count, ctx->dstat);
+                                                count, ctx->sort_keys, ctx->dstat);
   }
   ECS_LAUNCHED(ctx);
   if (ctx->ev[1]) {
@@ -1781,11 +1831,11 @@ static bool sort_due(const EcsCtx *ctx) {
          ctx->steps_since_sort + 1 >= ctx->sort_every;
 }
 
-// Scan of the cell counts and the scatter into the other buffer.
+// Scan of the cell counts and the permutation into key order (the next
+// particle pass moves the records).
 static int sort_counted(EcsCtx *ctx) {
   const int n = (int)ctx->nkeys;
   const int nb = (int)ecs_div_up(ctx->nkeys, (size_t)kScanBlock * kScanItems);
-  const int a = ctx->cur, b = 1 - ctx->cur;
   k_scan_local<<<nb, kScanBlock, 0, ctx->stream>>>(n, ctx->sort_count, ctx->sort_offset, ctx->scan_blocks);
   ECS_LAUNCHED(ctx);
   k_scan_sums<<<1, 1024, 0, ctx->stream>>>(nb, ctx->scan_blocks);
@@ -1794,11 +1844,10 @@ static int sort_counted(EcsCtx *ctx) {
                                                                   (int)ctx->np);
   ECS_LAUNCHED(ctx);
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
-  const PartK k = make_k(ctx, 0.0);
-  k_sort_scatter<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(
-      ctx->np, k.tg, ctx->sort_offset, ctx->sort_count, ctx->ions[a], ctx->ions[b]);
+  k_sort_index<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, ctx->sort_keys, ctx->sort_offset,
+                                                                        ctx->sort_count, ctx->perm);
   ECS_LAUNCHED(ctx);
-  ctx->cur = b;
+  ctx->perm_pending = true;
   ctx->steps_since_sort = 0;
   ctx->tiles_valid = true;
   return ECS_OK;
@@ -1851,10 +1900,12 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
 // Full counting sort (count pass included), used after an upload.
 int ecs_part_sort(EcsCtx *ctx) {
   if (ctx->prec != ECS_PREC_MIXED || ctx->np == 0 || ctx->p.ndim != 3) return ECS_OK;
+  int rc = settle_order(ctx);
+  if (rc) return rc;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
   const PartK k = make_k(ctx, 0.0);
   k_sort_count<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, k.tg, ctx->ions[ctx->cur],
-                                                                        ctx->sort_count);
+                                                                        ctx->sort_count, ctx->sort_keys);
   ECS_LAUNCHED(ctx);
   return sort_counted(ctx);
 }

@@ -26,8 +26,9 @@ def test_request_bytes(built):
     ions = 32 ** 3 * 16
     sim = E.serve_request_bytes(p, E.ECS_PREC_MIXED, E.ECS_SERVE_SIM, ions)
     solve = E.serve_request_bytes(p, E.ECS_PREC_MIXED, E.ECS_SERVE_SOLVE, ions)
-    # two 32-byte records an ion, plus two staging chunks of 48 bytes an ion
-    assert sim - solve == 64 * ions + 2 * max(ions // 8, 1 << 16) * 48
+    # two 32-byte records, a sort key and a permutation entry an ion, plus two
+    # staging chunks of 48 bytes an ion
+    assert sim - solve == 72 * ions + 2 * max(ions // 8, 1 << 16) * 48
     assert E.serve_request_bytes(params(16)) > 8 << 20  # fixed allowance: rounding, graphs
 
 
