@@ -419,12 +419,10 @@ static int step_particles(EcsCtx *ctx, double dt, EcsDevStatus *coll, int *sorte
 }
 
 // Field phase (src/pic.c:253-258): RHS, operator, potential solve.
+// The RHS, the operator set-up and the solve are one graph launch.
 static int step_field(EcsCtx *ctx, double rtol, int max_it, EcsSolveStats *st) {
-  int rc = ecs_grid_rhs(ctx);
-  if (rc) return rc;
-  if ((rc = ecs_solver_setup(ctx))) return rc;
   memset(st, 0, sizeof *st);
-  rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, st);
+  int rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, st, 1);
   ctx->eext_ready = false;
   return rc;
 }

@@ -78,9 +78,10 @@ struct SolverGraph {
   cudaGraphExec_t exec = nullptr;
   double rtol = 0.0;
   int max_it = 0, warm = -1;
-  // kernels of: the head (up to the first check), one sweep outside its
-  // Arnoldi steps, one Arnoldi step
-  int64_t k_head = 0, k_sweep = 0, k_step = 0;
+  int setup = -1;  // 1: the graph starts with the RHS and the operator set-up
+  // kernels of: the set-up prefix, the head (up to the first check), one
+  // sweep outside its Arnoldi steps, one Arnoldi step
+  int64_t k_pre = 0, k_head = 0, k_sweep = 0, k_step = 0;
 };
 
 // Instantiated graph of one stand-alone solve request (src/solver.c:107-170):
@@ -168,6 +169,10 @@ struct EcsCtx {
   void *rdev = nullptr;             // device state of the refinement loop
   void *rdev_host = nullptr;        // pinned copy
   cudaStream_t capst[3] = {nullptr, nullptr, nullptr};  // capture streams (graph nesting levels)
+  // side streams and events of the multigrid set-up, which forks off the
+  // context's stream and joins it again
+  cudaStream_t sst[2] = {nullptr, nullptr};
+  cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_solve[2] = {nullptr, nullptr};
   bool lhs_ready = false;
   bool moments_ready = false;
@@ -269,7 +274,9 @@ int ecs_grid_rhs(EcsCtx *ctx);           // RHS (+ mean removal) from moments
 int ecs_grid_clear_acc(EcsCtx *ctx);
 int ecs_solver_alloc(EcsCtx *ctx);       // reductions, Krylov bases, control block
 int ecs_solver_setup(EcsCtx *ctx);       // multigrid hierarchy from the density
-int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st);
+// setup = 1: compute the RHS and set up the operator first (the step's field
+// phase), in the same graph launch as the solve.
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup = 0);
 int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y);
 int ecs_solver_free(EcsCtx *ctx);
 // Stand-alone solve request: launch (asynchronous, on ctx->stream) and, once

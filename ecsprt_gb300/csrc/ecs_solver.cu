@@ -124,42 +124,70 @@ __global__ void k_zline_setup(GridG g, const T *__restrict__ lo, const T *__rest
   const T lo0 = cyc ? __ldg(&lo[col]) : T(0), d0 = __ldg(&dg[col]);
   const T gamma = -d0;
   T cp_prev = T(0), dq_prev = T(0), fprod = T(1);
-  // forward: factor T' and forward-substitute u = (gamma, 0, .., up_{N-1})
-#pragma unroll 4
-  for (int k = 0; k < N; k++) {
-    const size_t c = (size_t)k * plane + col;
-    const T lk = __ldg(&lo[c]), uk = __ldg(&up[c]), dk = __ldg(&dg[c]);
-    T a = (k == 0) ? T(0) : lk;
-    T upk = (k == N - 1) ? T(0) : uk;
-    T bb = dk;
-    if (cyc && k == 0) bb = d0 - gamma;
-    if (cyc && k == N - 1) bb = dk - uk * lo0 / gamma;
-    T m = bb - a * cp_prev;
-    T minv = T(1) / m;
-    T cp = upk * minv;
-    T u = cyc ? ((k == 0) ? gamma : ((k == N - 1) ? uk : T(0))) : T(0);
-    T dq = (u - a * dq_prev) * minv;
-    z.a[c] = a;
-    z.cp[c] = cp;
-    z.minv[c] = minv;
-    z.q[c] = dq;
-    if (k % S == 0) fprod = T(1);
-    fprod *= -(a * minv);
-    z.fb[c] = fprod;
-    cp_prev = cp;
-    dq_prev = dq;
+  // forward: factor T' and forward-substitute u = (gamma, 0, .., up_{N-1});
+  // the rows are read kBatch at a time, all loads first, so the recurrence
+  // waits on one memory latency a batch rather than one a cell
+  constexpr int kBatch = 8;
+  for (int k0 = 0; k0 < N; k0 += kBatch) {
+    T lv[kBatch], uv[kBatch], dv[kBatch];
+#pragma unroll
+    for (int e = 0; e < kBatch; e++) {
+      const size_t c = (size_t)min(k0 + e, N - 1) * plane + col;
+      lv[e] = __ldg(&lo[c]);
+      uv[e] = __ldg(&up[c]);
+      dv[e] = __ldg(&dg[c]);
+    }
+#pragma unroll
+    for (int e = 0; e < kBatch; e++) {
+      const int k = k0 + e;
+      if (k >= N) break;
+      const size_t c = (size_t)k * plane + col;
+      const T lk = lv[e], uk = uv[e], dk = dv[e];
+      T a = (k == 0) ? T(0) : lk;
+      T upk = (k == N - 1) ? T(0) : uk;
+      T bb = dk;
+      if (cyc && k == 0) bb = d0 - gamma;
+      if (cyc && k == N - 1) bb = dk - uk * lo0 / gamma;
+      T m = bb - a * cp_prev;
+      T minv = T(1) / m;
+      T cp = upk * minv;
+      T u = cyc ? ((k == 0) ? gamma : ((k == N - 1) ? uk : T(0))) : T(0);
+      T dq = (u - a * dq_prev) * minv;
+      z.a[c] = a;
+      z.cp[c] = cp;
+      z.minv[c] = minv;
+      z.q[c] = dq;
+      if (k % S == 0) fprod = T(1);
+      fprod *= -(a * minv);
+      z.fb[c] = fprod;
+      cp_prev = cp;
+      dq_prev = dq;
+    }
   }
-  // backward substitution for q, in-segment products of -cp
+  // backward substitution for q, in-segment products of -cp (this thread's
+  // own values from above, read back a batch at a time)
   T qn = z.q[(size_t)(N - 1) * plane + col];
   T bprod = -z.cp[(size_t)(N - 1) * plane + col];
   z.bb[(size_t)(N - 1) * plane + col] = bprod;
-  for (int k = N - 2; k >= 0; k--) {
-    size_t c = (size_t)k * plane + col;
-    qn = z.q[c] - z.cp[c] * qn;
-    z.q[c] = qn;
-    if ((k + 1) % S == 0) bprod = T(1);
-    bprod *= -z.cp[c];
-    z.bb[c] = bprod;
+  for (int k0 = N - 2; k0 >= 0; k0 -= kBatch) {
+    T qv[kBatch], cv[kBatch];
+#pragma unroll
+    for (int e = 0; e < kBatch; e++) {
+      const size_t c = (size_t)max(k0 - e, 0) * plane + col;
+      qv[e] = z.q[c];
+      cv[e] = z.cp[c];
+    }
+#pragma unroll
+    for (int e = 0; e < kBatch; e++) {
+      const int k = k0 - e;
+      if (k < 0) break;
+      const size_t c = (size_t)k * plane + col;
+      qn = qv[e] - cv[e] * qn;
+      z.q[c] = qn;
+      if ((k + 1) % S == 0) bprod = T(1);
+      bprod *= -cv[e];
+      z.bb[c] = bprod;
+    }
   }
   if (cyc) {
     T a0g = lo0 / gamma;
@@ -624,6 +652,148 @@ __global__ void __launch_bounds__(kInvThreads) k_coarse_inverse(OpK o, const T *
   for (int e = tid; e < n * n; e += bs) {
     const int r = e / n, k = e - r * n;
     invT[(size_t)k * n + r] = M[(size_t)r * w + n + k];
+  }
+}
+
+// The same inverse for n <= kRegInvMax with the work matrix in registers:
+// row r of M = [A | I] belongs to the tpr threads tid / tpr == r, thread jr
+// holding columns jr + tpr u.  Pivoting is implicit: the pivot of column c
+// is the largest |M[r][c]| among rows not yet used (lowest row on ties),
+// and the row used at step c ends up holding row c of the inverse.  Each
+// step needs two barriers: column c and the scaled pivot row pass through
+// shared memory (double-buffered by the parity of c).
+constexpr int kRegInvMax = 64;
+constexpr int kRegCols = 2 * kRegInvMax * kRegInvMax / kInvThreads;  // 8 columns a thread
+template <typename T>
+__global__ void __launch_bounds__(kInvThreads) k_coarse_inverse_reg(OpK o, const T *__restrict__ dens,
+                                                                    int regularize, T *__restrict__ invT) {
+  __shared__ T colbuf[2][kRegInvMax];
+  __shared__ T prow[2][2 * kRegInvMax];
+  __shared__ int rowpos[kRegInvMax];
+  __shared__ T wsum[32];
+  __shared__ T sigma;
+  const GridG &g = o.g;
+  const int n = (int)g.n, w = 2 * n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tpr = n <= 32 ? 32 : 16;  // threads a row
+  const int r = tid / tpr, jr = tid % tpr;
+  const bool live = r < n;
+  // Every access to M below has a compile-time index (u), so M stays in
+  // registers.
+  T M[kRegCols];
+#pragma unroll
+  for (int u = 0; u < kRegCols; u++) M[u] = T(0);
+  if (live) {  // row r: the operator's entries in the reference's order, then the identity
+    int i, j, k;
+    cell_ijk((unsigned)r, g, i, j, k);
+    T v[11];
+    int tc[11];
+    row11(dens, o, i, j, k, v);
+#pragma unroll
+    for (int e = 0; e < 11; e++) {
+      int ii = i + off_i(e), jj = j + off_j(e), kk = k + off_k(e);
+      bool out = false;
+      if (ii < 0 || ii >= g.nx) { if (g.bc[0]) out = true; else ii = ii < 0 ? ii + g.nx : ii - g.nx; }
+      if (jj < 0 || jj >= g.ny) { if (g.bc[1]) out = true; else jj = jj < 0 ? jj + g.ny : jj - g.ny; }
+      if (kk < 0 || kk >= g.nz) { if (g.bc[2]) out = true; else kk = kk < 0 ? kk + g.nz : kk - g.nz; }
+      tc[e] = out ? -1 : (kk * g.ny + jj) * g.nx + ii;
+    }
+#pragma unroll
+    for (int u = 0; u < kRegCols; u++) {
+      const int q = jr + tpr * u;
+#pragma unroll
+      for (int e = 0; e < 11; e++)
+        if (tc[e] == q) M[u] += v[e];
+      if (q == n + r) M[u] = T(1);
+    }
+  }
+  if (regularize) {  // sigma = sum |A_rr| / n^2 over the diagonal, added to every entry of A
+#pragma unroll
+    for (int u = 0; u < kRegCols; u++)
+      if (live && jr + tpr * u == r) colbuf[0][r] = fabs(M[u]);
+    __syncthreads();
+    T t = tid < n ? colbuf[0][tid] : T(0);
+    for (int s2 = 16; s2 >= 1; s2 >>= 1) t += __shfl_xor_sync(ECS_FULL_MASK, t, s2);
+    if (lane == 0) wsum[warp] = t;
+    __syncthreads();
+    if (tid == 0) {
+      T u2 = T(0);
+      for (int q = 0; q < (kInvThreads >> 5); q++) u2 += wsum[q];
+      sigma = u2 / (T(n) * T(n));
+    }
+    __syncthreads();
+    const T sg = sigma;
+#pragma unroll
+    for (int u = 0; u < kRegCols; u++)
+      if (live && jr + tpr * u < n) M[u] += sg;
+  }
+  __syncthreads();  // colbuf[0] is free again
+  if (live && jr == 0) colbuf[0][r] = M[0];  // column 0
+  unsigned long long used = 0ull;
+  // step c = j0 + tpr u0: column c is column u0 of the threads jr == j0
+#pragma unroll
+  for (int u0 = 0; u0 < kRegCols; u0++) {
+    for (int j0 = 0; j0 < tpr; j0++) {
+      const int c = j0 + tpr * u0;
+      if (c >= n) break;
+      const int b = c & 1;
+      __syncthreads();  // column c complete
+      T best = T(-1);
+      int bi = n;
+      for (int rr = lane; rr < n; rr += 32) {
+        if ((used >> rr) & 1ull) continue;
+        const T a = fabs(colbuf[b][rr]);
+        if (a > best) { best = a; bi = rr; }
+      }
+      for (int s2 = 16; s2 >= 1; s2 >>= 1) {
+        const T ob = __shfl_xor_sync(ECS_FULL_MASK, best, s2);
+        const int oi = __shfl_xor_sync(ECS_FULL_MASK, bi, s2);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      const int pr = bi < n ? bi : __ffsll((long long)~used) - 1;
+      used |= 1ull << pr;
+      const T pv = colbuf[b][pr];
+      const T ip = pv != T(0) ? T(1) / pv : T(0);
+      if (tid == 0) rowpos[pr] = c;
+      if (r == pr) {
+#pragma unroll
+        for (int u = 0; u < kRegCols; u++) {
+          const int q = jr + tpr * u;
+          if (q < w) {
+            M[u] *= ip;
+            prow[b][q] = M[u];
+          }
+        }
+      }
+      __syncthreads();  // scaled pivot row complete
+      if (live && r != pr) {
+        const T f = colbuf[b][r];
+        if (f != T(0)) {
+#pragma unroll
+          for (int u = 0; u < kRegCols; u++) {
+            const int q = jr + tpr * u;
+            if (q < w) M[u] -= f * prow[b][q];
+          }
+        }
+      }
+      // column c + 1 for the next step: column u0 of j0 + 1, or column
+      // u0 + 1 of thread 0 of the row
+      if (live && c + 1 < n) {
+        if (j0 + 1 < tpr) {
+          if (jr == j0 + 1) colbuf[b ^ 1][r] = M[u0];
+        } else if (u0 + 1 < kRegCols) {
+          if (jr == 0) colbuf[b ^ 1][r] = M[u0 + 1 < kRegCols ? u0 + 1 : u0];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (live) {
+    const int row = rowpos[r];
+#pragma unroll
+    for (int u = 0; u < kRegCols; u++) {
+      const int q = jr + tpr * u;
+      if (q >= n && q < w) invT[(size_t)(q - n) * n + row] = M[u];
+    }
   }
 }
 
@@ -1152,29 +1322,57 @@ __global__ void k_density_in(size_t n, const double *__restrict__ mom, T *__rest
     d[e] = (T)mom[e];
 }
 
+int ensure_setup_streams(EcsCtx *ctx) {
+  for (auto &c : ctx->sst)
+    if (!c) ECS_CUDA(ctx, cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+  for (auto &e : ctx->sev)
+    if (!e) ECS_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return ECS_OK;
+}
+
+// z-line rows and factors of level L on stream s.
+template <typename T>
+int zline_factor(EcsCtx *ctx, MgLevel<T> &L, cudaStream_t s) {
+  const int ncol = L.nx * L.ny;
+  const OpK o = op_level(ctx, L);
+  k_zline_rows<T><<<blocks3(o.g), threads3(), 0, s>>>(o, L.dens, L.x, L.b, L.r);  // x, b, r are free here
+  ECS_LAUNCHED(ctx);
+  k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, s>>>(o.g, L.x, L.b, L.r, zl_of(L), seg_len<T>(L.nz));
+  ECS_LAUNCHED(ctx);
+  return ECS_OK;
+}
+
+// Operator set-up of the multigrid levels: level densities, z-line factors,
+// coarsest inverse.  The pieces are latency-bound small launches with few
+// dependencies, so they run on three streams (also inside a graph capture,
+// where the fork and join become graph edges):
+//   context stream: fine density, fine z-line factors
+//   sst[0]:         restriction chain of the densities, then the coarse inverse
+//   sst[1]:         z-line factors of the coarse levels (after the chain)
+// and the context stream waits for both side streams at the end.
 template <typename T>
 int mg_setup(EcsCtx *ctx) {
   int rc = mg_alloc<T>(ctx);
   if (rc) return rc;
+  if ((rc = ensure_setup_streams(ctx))) return rc;
   Multigrid<T> &mg = mg_of<T>(ctx);
+  cudaStream_t s0 = ctx->stream, sa = ctx->sst[0], sb = ctx->sst[1];
   MgLevel<T> &L0 = mg.lv[0];
-  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, ctx->stream>>>(L0.n, op_density(ctx), L0.dens);
+  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, s0>>>(L0.n, op_density(ctx), L0.dens);
   ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[0], s0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(sa, ctx->sev[0], 0));
   for (size_t l = 1; l < mg.lv.size(); l++) {
     MgLevel<T> &F = mg.lv[l - 1], &C = mg.lv[l];
-    k_restrict<T><<<blocks3(C.nx, C.ny, C.nz), threads3(), 0, ctx->stream>>>(
+    k_restrict<T><<<blocks3(C.nx, C.ny, C.nz), threads3(), 0, sa>>>(
         grid_level(ctx, F.nx, F.ny, F.nz), grid_level(ctx, C.nx, C.ny, C.nz), F.dens, C.dens);
     ECS_LAUNCHED(ctx);
   }
-  for (auto &L : mg.lv) {  // the level's x, b and r are free here: they hold the rows
-    const int ncol = L.nx * L.ny;
-    const OpK o = op_level(ctx, L);
-    k_zline_rows<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, L.x, L.b, L.r);
-    ECS_LAUNCHED(ctx);
-    k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, ctx->stream>>>(o.g, L.x, L.b, L.r, zl_of(L),
-                                                                               seg_len<T>(L.nz));
-    ECS_LAUNCHED(ctx);
-  }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[1], sa));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(sb, ctx->sev[1], 0));
+  for (size_t l = 1; l < mg.lv.size(); l++)
+    if ((rc = zline_factor<T>(ctx, mg.lv[l], sb))) return rc;
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[2], sb));
   if (mg.cinv) {
     MgLevel<T> &C = mg.lv.back();
     const size_t bytes = C.n * 2 * C.n * sizeof(T);
@@ -1184,10 +1382,18 @@ int mg_setup(EcsCtx *ctx) {
       ECS_CUDA(ctx, cudaFuncSetAttribute(k_coarse_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInverseSmem));
       attr_set[sizeof(T) == 8] = true;
     }
-    k_coarse_inverse<T><<<1, kInvThreads, in_smem ? bytes : 0, ctx->stream>>>(
-        op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, in_smem ? nullptr : mg.cwork, mg.cinv);
+    if (C.n <= (size_t)kRegInvMax)
+      k_coarse_inverse_reg<T><<<1, kInvThreads, 0, sa>>>(op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0,
+                                                          mg.cinv);
+    else
+      k_coarse_inverse<T><<<1, kInvThreads, in_smem ? bytes : 0, sa>>>(
+          op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, in_smem ? nullptr : mg.cwork, mg.cinv);
     ECS_LAUNCHED(ctx);
   }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[3], sa));
+  if ((rc = zline_factor<T>(ctx, L0, s0))) return rc;
+  ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[2], 0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[3], 0));
   return ECS_OK;
 }
 
@@ -1665,12 +1871,17 @@ int ensure_capture_streams(EcsCtx *ctx) {
 
 // One solve as one graph (see capture_solve), built for (rtol, max_it, warm).
 template <typename T>
-int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm) {
+int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm, int setup) {
   SolverGraph &sg = ctx->sgraph;
-  if (sg.exec && sg.rtol == rtol && sg.max_it == max_it && sg.warm == warm) return ECS_OK;
+  if (sg.exec && sg.rtol == rtol && sg.max_it == max_it && sg.warm == warm && sg.setup == setup) return ECS_OK;
   free_graph(sg);
   int rc = ensure_capture_streams(ctx);
   if (rc) return rc;
+  if (setup) {  // allocations happen before the capture
+    if ((rc = ecs_solver_alloc(ctx))) return rc;
+    if (!identity_lhs(ctx) && (rc = mg_alloc<T>(ctx))) return rc;
+    if ((rc = ensure_setup_streams(ctx))) return rc;
+  }
   const int64_t launches0 = ctx->launches;
   cudaStream_t user = ctx->stream;
   ctx->stream = ctx->capst[0];
@@ -1680,7 +1891,14 @@ int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm) {
     ctx->stream = user;
     return ecs_cuda_check(ctx, ce, "solve graph capture");
   }
-  rc = capture_solve<T>(ctx, rtol, max_it, warm);
+  rc = ECS_OK;
+  sg.k_pre = 0;
+  if (setup) {
+    rc = ecs_grid_rhs(ctx);
+    if (!rc && !identity_lhs(ctx)) rc = mg_setup<T>(ctx);
+    sg.k_pre = ctx->launches - launches0;
+  }
+  if (!rc) rc = capture_solve<T>(ctx, rtol, max_it, warm);
   ce = cudaStreamEndCapture(ctx->stream, &g);
   ctx->stream = user;
   ctx->launches = launches0;
@@ -1694,13 +1912,14 @@ int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm) {
   sg.rtol = rtol;
   sg.max_it = max_it;
   sg.warm = warm;
+  sg.setup = setup;
   return ECS_OK;
 }
 
 // Launch the solve graph (asynchronous).
-int solve_graph_launch(EcsCtx *ctx, double rtol, int max_it, int warm) {
-  int rc = ctx->prec == ECS_PREC_FP64 ? build_solve_graph<double>(ctx, rtol, max_it, warm)
-                                      : build_solve_graph<float>(ctx, rtol, max_it, warm);
+int solve_graph_launch(EcsCtx *ctx, double rtol, int max_it, int warm, int setup) {
+  int rc = ctx->prec == ECS_PREC_FP64 ? build_solve_graph<double>(ctx, rtol, max_it, warm, setup)
+                                      : build_solve_graph<float>(ctx, rtol, max_it, warm, setup);
   if (rc) return rc;
   ECS_CUDA(ctx, cudaGraphLaunch(ctx->sgraph.exec, ctx->stream));
   return ECS_OK;
@@ -1868,7 +2087,15 @@ int ecs_solver_setup(EcsCtx *ctx) {
 
 // Iterative refinement around FGMRES cycles.  Per refinement the host waits
 // once, for the FP64 residual norm and the finished cycle's control block.
-int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st) {
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup) {
+  const bool graphs = ctx->use_graphs || identity_lhs(ctx);
+  if (setup && !graphs) {  // the host-driven loop: RHS and set-up launched one by one
+    int rc0 = ecs_grid_rhs(ctx);
+    if (!rc0) rc0 = ecs_solver_setup(ctx);
+    if (rc0) return rc0;
+    setup = 0;
+  }
+  if (setup) ctx->lhs_ready = true;  // the graph sets the operator up before it solves
   if (!ctx->lhs_ready) return ecs_fail(ctx, ECS_ERR_STATE, "solve called before lhs");
   const size_t n = ctx->ncell;
   const EcsParams &p = ctx->p;
@@ -1880,14 +2107,14 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
   }
   ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[0], ctx->stream));
   int rc;
-  if (ctx->use_graphs || identity_lhs(ctx)) {  // the whole solve as one graph launch, one wait
-    if ((rc = solve_graph_launch(ctx, rtol, max_it, warm))) return rc;
+  if (graphs) {  // the whole solve as one graph launch, one wait
+    if ((rc = solve_graph_launch(ctx, rtol, max_it, warm, setup))) return rc;
     RefineDev *hr = (RefineDev *)ctx->rdev_host;
     ECS_CUDA(ctx, cudaMemcpyAsync(hr, ctx->rdev, sizeof(RefineDev), cudaMemcpyDeviceToHost, ctx->stream));
     ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[1], ctx->stream));
     ECS_CUDA(ctx, cudaEventSynchronize(ctx->ev_solve[1]));
     const SolverGraph &sg = ctx->sgraph;
-    ctx->launches += sg.k_head + hr->sweeps * sg.k_sweep + (int64_t)hr->its * sg.k_step;
+    ctx->launches += sg.k_pre + sg.k_head + hr->sweeps * sg.k_sweep + (int64_t)hr->its * sg.k_step;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev_solve[0], ctx->ev_solve[1]);
     if (st) {
@@ -1990,6 +2217,10 @@ int ecs_solver_free(EcsCtx *ctx) {
   if (ctx->rgraph.h_out) cudaFreeHost(ctx->rgraph.h_out);
   for (auto &c : ctx->capst)
     if (c) cudaStreamDestroy(c);
+  for (auto &c : ctx->sst)
+    if (c) cudaStreamDestroy(c);
+  for (auto &e : ctx->sev)
+    if (e) cudaEventDestroy(e);
   free_mg(ctx->mg64);
   free_mg(ctx->mg32);
   void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->dots, ctx->red, ctx->kdev,

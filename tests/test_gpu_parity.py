@@ -170,6 +170,46 @@ def test_solver_graph_matches_host_loop(built, golden, prec):
     assert np.array_equal(out[True][0], out[False][0])
 
 
+# The FGMRES iteration counts of the multigrid-preconditioned solve on grids
+# whose coarsest level (4^3, 4x4x1) is solved directly by its explicit
+# inverse.  A wrong coarsest inverse still converges, only more slowly, so
+# the counts are pinned here (measured on GB300; both precisions reach the
+# tolerance in the listed number of iterations or fewer).
+ITERATION_BOUNDS = {  # (grid, prec) -> most FGMRES iterations (mixed: rtol 1e-8, FP64: 1e-10)
+    ((32, 32, 32), E.ECS_PREC_MIXED): 9,
+    ((32, 32, 32), E.ECS_PREC_FP64): 11,
+    ((64, 64, 64), E.ECS_PREC_MIXED): 9,
+    ((64, 64, 64), E.ECS_PREC_FP64): 11,
+    ((128, 128, 1), E.ECS_PREC_MIXED): 10,
+    ((128, 128, 1), E.ECS_PREC_FP64): 12,
+}
+
+
+@pytest.mark.parametrize("key", list(ITERATION_BOUNDS), ids=lambda k: f"{'x'.join(map(str, k[0]))}-{k[1]}")
+def test_multigrid_iteration_counts(built, key):
+    (nx, ny, nz), prec = key
+    nd = 2 if nz == 1 else 3
+    opts = (f"-ndim {nd} -Nx {nx} -Ny {ny} " + (f"-Nz {nz} -dz 1 " if nd == 3 else "") +
+            "-dx 1 -dy 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 1.0 -nue 8.79e9 -Te 11604.5 -E0 0 -mn 0")
+    p = E.params_from_options(opts)
+    rng = np.random.default_rng(20261203 + nx + nz)
+    x = np.arange(nx) / nx
+    n = 16.0 * (1.0 + 0.05 * np.sin(2 * np.pi * x))[None, None, :] * (1.0 + 0.25 * rng.standard_normal((nz, ny, nx)))
+    mom = np.zeros((nz, ny, nx, 4))
+    mom[..., 0] = n
+    mom[..., 1] = n * (1.0 + 0.25 * rng.standard_normal((nz, ny, nx)))
+    mom[..., 2] = n * 0.25 * rng.standard_normal((nz, ny, nx))
+    if nd == 3:
+        mom[..., 3] = n * 0.25 * rng.standard_normal((nz, ny, nx))
+    rtol = 1e-10 if prec == E.ECS_PREC_FP64 else 1e-8
+    with E.Context(p, prec, np_capacity=1) as ctx:
+        ctx.moments = mom
+        st = ctx.compute_potential(rtol=rtol, max_it=200)
+    print(f"{key}: {st.iterations} iterations, {st.refinements} refinements, relres {st.relres:.2e}")
+    assert st.relres <= rtol
+    assert st.iterations <= ITERATION_BOUNDS[key]
+
+
 # ---------------------------------------------------------------- mixed path
 @pytest.mark.parametrize("case", CASES)
 def test_mixed_push(built, golden, case):

@@ -118,13 +118,15 @@ def test_serve_solves_alone_vs_mix(built):
 
 
 def test_serve_budget_admission(built):
-    """A budget that holds two 32^3 slots: requests wait for room, idle
-    slots of the other size are evicted, the budget is never exceeded, and
-    a request larger than the budget is refused at submit."""
+    """A budget one byte short of a 32^3 slot beside a 24^3 slot: the two
+    sizes alternate, so every change of size waits for the other slot to go
+    idle and evicts it (whatever the timing of the solves), the budget is
+    never exceeded, and a request larger than the budget is refused at
+    submit."""
     p32, p24, p64 = solve_params(32), solve_params(24), solve_params(64)
     b32 = E.serve_request_bytes(p32)
     b24 = E.serve_request_bytes(p24)
-    budget = 2 * b32
+    budget = b32 + b24 - 1
     rng = np.random.default_rng(14)
     sizes = [32, 24, 32, 24, 32, 32, 24, 32]
     dens = [W.solve_density(n, rng) for n in sizes]
