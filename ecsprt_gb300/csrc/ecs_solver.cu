@@ -340,6 +340,27 @@ __global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__res
   c[lin3(gc, I, J, K)] = restrict_at(gf, f, I, J, K);
 }
 
+// The same sum with the loops kept rolled (less code, for the single-block
+// cycle); the terms are added in the same order.
+template <typename T>
+__device__ __forceinline__ T restrict_at_rolled(const GridG &gf, const T *__restrict__ f, int I, int J, int K) {
+  T s = T(0);
+#pragma unroll 1
+  for (int dk = -1; dk <= 1; dk++) {
+    const T wk = dk == 0 ? T(0.5) : T(0.25);
+#pragma unroll 1
+    for (int dj = -1; dj <= 1; dj++) {
+      const T wj = dj == 0 ? T(0.5) : T(0.25);
+#pragma unroll 1
+      for (int di = -1; di <= 1; di++) {
+        const T wi = di == 0 ? T(0.5) : T(0.25);
+        s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
+      }
+    }
+  }
+  return s;
+}
+
 // Trilinear prolongation value at fine cell (i,j,k).
 template <typename T>
 __device__ __forceinline__ T prolong_at(const GridG &gc, const T *__restrict__ c, int i, int j, int k) {
@@ -427,8 +448,11 @@ __device__ __forceinline__ SmallView<T> staged(const SmallLevel<T> &L, T *sm) {
 }
 
 // One damped z-line Jacobi sweep of level L from xo (nullptr: zero) into xn.
+// The single-block cycle runs its code once per launch, so its time goes to
+// instruction fetch as much as to arithmetic: the sweep, called three times,
+// is kept out of line (one copy of its code).
 template <typename T>
-__device__ void blk_sweep(const SmallLevel<T> &L, T *sm, const T *b, const T *xo, T *xn, T omega) {
+__device__ __noinline__ void blk_sweep(const SmallLevel<T> &L, T *sm, const T *b, const T *xo, T *xn, T omega) {
   const GridG &g = L.o.g;
   const SmallView<T> v = staged(L, sm);
   T *r = sm + L.sr;
@@ -497,21 +521,23 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
     for (unsigned c = threadIdx.x; c < C.o.g.n; c += blockDim.x) {
       int I, J, K;
       cell_ijk(c, C.o.g, I, J, K);
-      cb[c] = restrict_at(g, (const T *)r, I, J, K);
+      cb[c] = restrict_at_rolled(g, (const T *)r, I, J, K);
     }
     __syncthreads();
   }
   // coarsest: direct solve with the precomputed inverse, else damped z-line
   // Jacobi sweeps; the result in its x
-  if (sc.cinv) {
+  if (sc.cinv) {  // x = inv b: each row's sum split over the 32 lanes of a warp
     const SmallLevel<T> &L = sc.lv[nl - 1];
     const int n = (int)L.o.g.n;
     const T *b = sm + L.sb;
     const T *ci = sm + sc.scinv;
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < n; r += blockDim.x >> 5) {
       T acc = T(0);
-      for (int k = 0; k < n; k++) acc += ci[k * n + r] * b[k];
-      sm[L.sx + r] = acc;
+      for (int k = lane; k < n; k += 32) acc += ci[k * n + r] * b[k];
+      for (int s2 = 16; s2 >= 1; s2 >>= 1) acc += __shfl_xor_sync(ECS_FULL_MASK, acc, s2);
+      if (lane == 0) sm[L.sx + r] = acc;
     }
     __syncthreads();
   } else {
