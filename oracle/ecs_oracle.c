@@ -1049,34 +1049,50 @@ int orc_num_threads(void) {
 #endif
 }
 
-/* Multi-threaded CIC deposit for timing the CPU baseline on all host cores:
-   each OpenMP thread accumulates its contiguous share of the particles into a
-   private ghosted grid (the reference's per-rank local array), then the
-   private grids are folded in thread order.  Same weights as orc_collect;
+/* Multi-threaded CIC deposit for timing the CPU baseline on all host cores.
+   The grid is split into z slabs, one per OpenMP thread, as the reference's
+   ranks split the domain (each rank deposits into its subdomain plus a ghost
+   layer and adds the ghosts to their owners, src/moments.c:108-226 with
+   DMLocalToGlobal(ADD)): thread t deposits the ions whose base cell lies in
+   its slab, into the slab's planes and a private copy of the plane above,
+   which is then added to the plane's owner.  Same weights as orc_collect;
    only the summation order differs. */
 int orc_collect_mt(const OrcParams *p, int np, const double *pos, const double *vel, double *out) {
   int nt = orc_num_threads();
-  int gx = p->Nx + 2, gy = p->Ny + 2, gz = p->Nz + 2;
-  size_t gsz = (size_t)gx * gy * gz * 4;
-  double *loc = calloc(gsz * (size_t)nt, sizeof(double));
-  if (!loc) return -1;
+  if (nt > p->Nz) nt = p->Nz;
+  if (nt < 1) nt = 1;
+  const size_t plane = (size_t)p->Nx * p->Ny * 4;
+  memset(out, 0, sizeof(double) * plane * (size_t)p->Nz);
+  double *top = calloc(plane * (size_t)nt, sizeof(double)); /* the plane above each slab */
+  if (!top) return -1;
 #pragma omp parallel num_threads(nt)
   {
 #ifdef _OPENMP
-    int t = omp_get_thread_num();
+    const int t = omp_get_thread_num();
 #else
-    int t = 0;
+    const int t = 0;
 #endif
-    double *L = loc + gsz * (size_t)t;
-    int lo = (int)((long long)np * t / nt), hi = (int)((long long)np * (t + 1) / nt);
-    for (int ip = lo; ip < hi; ip++) {
+    const int k0 = (int)((long long)p->Nz * t / nt), k1 = (int)((long long)p->Nz * (t + 1) / nt);
+    double *T = top + plane * (size_t)t;
+    for (int ip = 0; ip < np; ip++) {
+      const double z = pos[ip * 3 + 2] / p->dz;
+      const int izl = (int)z;
+      if (izl < k0 || izl >= k1) continue;
       int idx[3];
       double w[8];
-      cic_weights(pos[ip * 3 + 0] / p->dx, pos[ip * 3 + 1] / p->dy, pos[ip * 3 + 2] / p->dz, idx, w);
+      cic_weights(pos[ip * 3 + 0] / p->dx, pos[ip * 3 + 1] / p->dy, z, idx, w);
       for (int b = 0; b < 8; b++) {
-        int i = idx[0] + (b & 1) + 1, j = idx[1] + ((b >> 1) & 1) + 1, k = idx[2] + (b >> 2) + 1;
-        if (i < 0 || i >= gx || j < 0 || j >= gy || k < 0 || k >= gz) continue;
-        double *node = L + (((size_t)k * gy + j) * gx + i) * 4;
+        int i = idx[0] + (b & 1), j = idx[1] + ((b >> 1) & 1);
+        const int k = idx[2] + (b >> 2);
+        if (i < 0 || i >= p->Nx) { if (p->bc[0]) continue; i = wrapi(i, p->Nx); }
+        if (j < 0 || j >= p->Ny) { if (p->bc[1]) continue; j = wrapi(j, p->Ny); }
+        double *node;
+        if (k < k1) {
+          node = out + (((size_t)k * p->Ny + j) * p->Nx + i) * 4;
+        } else {
+          if (k >= p->Nz && p->bc[2]) continue; /* past a ghosted z edge: dropped */
+          node = T + ((size_t)j * p->Nx + i) * 4;
+        }
         node[0] += w[b];
         node[1] += vel[ip * 3 + 0] * w[b];
         node[2] += vel[ip * 3 + 1] * w[b];
@@ -1084,25 +1100,16 @@ int orc_collect_mt(const OrcParams *p, int np, const double *pos, const double *
       }
     }
   }
-  memset(out, 0, sizeof(double) * (size_t)p->Nx * p->Ny * p->Nz * 4);
-  for (int t = 0; t < nt; t++) {
-    const double *L = loc + gsz * (size_t)t;
-    for (int kk = 0; kk < gz; kk++) {
-      int k = kk - 1;
-      if (k < 0 || k >= p->Nz) { if (p->bc[2]) continue; k = wrapi(k, p->Nz); }
-      for (int jj = 0; jj < gy; jj++) {
-        int j = jj - 1;
-        if (j < 0 || j >= p->Ny) { if (p->bc[1]) continue; j = wrapi(j, p->Ny); }
-        for (int ii = 0; ii < gx; ii++) {
-          int i = ii - 1;
-          if (i < 0 || i >= p->Nx) { if (p->bc[0]) continue; i = wrapi(i, p->Nx); }
-          const double *src = L + (((size_t)kk * gy + jj) * gx + ii) * 4;
-          double *dst = out + (((size_t)k * p->Ny + j) * p->Nx + i) * 4;
-          for (int c = 0; c < 4; c++) dst[c] += src[c];
-        }
-      }
+  for (int t = 0; t < nt; t++) { /* each slab's upper plane to its owner */
+    int k = (int)((long long)p->Nz * (t + 1) / nt);
+    if (k >= p->Nz) {
+      if (p->bc[2]) continue;
+      k -= p->Nz;
     }
+    double *dst = out + plane * (size_t)k;
+    const double *src = top + plane * (size_t)t;
+    for (size_t e = 0; e < plane; e++) dst[e] += src[e];
   }
-  free(loc);
+  free(top);
   return 0;
 }
