@@ -53,10 +53,13 @@ SORT_EVERY = 2          # cell sort cadence of the mixed path
 # moves one of the two)
 ALGO_BYTES_MIXED = 68
 ALGO_BYTES_FP64 = 96    # per particle-step: 6 FP64 read + written
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ion of one
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ion of a
 # k_tiles32 step launch, measured by ncu on the 64^3 x 64 ppc case of this
-# workload; the traffic grows with the ion count, so a launch moves this x N.
-TRAFFIC_BYTES_PER_ION = 62.0
+# workload: 67.3 B for a pass that counts cells for the next sort, 68.5 B for
+# the pass after a sort (records read through the permutation); the steps
+# alternate, so a launch moves their mean x N (the traffic grows with the ion
+# count).
+TRAFFIC_BYTES_PER_ION = 67.9
 
 
 def options(w):
@@ -194,8 +197,9 @@ def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
     rate = S * steps / el
     return {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
             "sample": f"{S} ions of the workload x {steps} steps of push+collide+move+deposit (FP64, "
-                      f"{threads} OpenMP threads for push, move and deposit (per-thread grids as per-rank "
-                      f"local arrays); collide serial as in the reference); the potential solve is excluded"}
+                      f"{threads} OpenMP threads for push, move and deposit (the deposit split into one z slab "
+                      f"a thread, as the reference's ranks split the domain); collide serial as in the "
+                      f"reference); the potential solve is excluded"}
 
 
 def dist_setup():
