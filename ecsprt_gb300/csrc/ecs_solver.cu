@@ -64,9 +64,14 @@ __global__ void k_apply(OpK o, const T *__restrict__ n, const T *__restrict__ x,
                         T *__restrict__ y, int mode) {
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
-  const unsigned c = lin3(o.g, i, j, k);
-  const T s = apply_row(n, x, o, i, j, k);
-  y[c] = mode ? b[c] - s : s;
+  const Nbr q = nbr_of(o.g, i, j, k);
+  T v[11], xe[11];
+  row11_n(n, o, q, v);
+  row_x(x, q, xe);
+  T s = T(0);
+#pragma unroll
+  for (int e = 0; e < 11; e++) s += v[e] * xe[e];
+  y[q.c] = mode ? b[q.c] - s : s;
 }
 
 // ---- z-line smoother --------------------------------------------------------------
@@ -206,8 +211,17 @@ __global__ void k_zline_rhs(OpK o, const T *__restrict__ n, const T *__restrict_
                             T *__restrict__ r) {
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
-  const unsigned c = lin3(o.g, i, j, k);
-  r[c] = zline_rhs_at(n, b, xo, o, i, j, k, c);
+  const Nbr q = nbr_of(o.g, i, j, k);
+  T v[11], xe[11];
+  row11_n(n, o, q, v);
+  row_x(xo, q, xe);
+  T s = b[q.c];
+#pragma unroll
+  for (int e = 0; e < 10; e++) {
+    if (e == 4 || e == 5) continue;
+    s -= v[e] * xe[e];
+  }
+  r[q.c] = s;
 }
 
 // Damped z-line Jacobi update: T' y = r by segments, Sherman-Morrison
@@ -1149,12 +1163,14 @@ __global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict_
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const int jj = kd->j;
   const T m = mean ? (T)mean[0] : T(0);
-  const unsigned c = lin3(o.g, i, j, k);
-  T v[11];
-  row11(n, o, i, j, k, v);
+  const Nbr q = nbr_of(o.g, i, j, k);
+  const unsigned c = q.c;
+  T v[11], xe[11];
+  row11_n(n, o, q, v);
+  row_x(x, q, xe);
   T s = T(0);
 #pragma unroll
-  for (int e = 0; e < 11; e++) s += v[e] * (gval(x, o.g, k + off_k(e), j + off_j(e), i + off_i(e)) - m);
+  for (int e = 0; e < 11; e++) s += v[e] * (xe[e] - m);
   Z[(size_t)jj * o.g.n + c] = x[c] - m;
   V[(size_t)(jj + 1) * o.g.n + c] = s;
 }
@@ -1719,8 +1735,14 @@ __global__ void k_residual64(OpK o, const double *__restrict__ n, const double *
                              const double *__restrict__ b, double *__restrict__ r) {
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
-  const unsigned c = lin3(o.g, i, j, k);
-  r[c] = b[c] - apply_row(n, x, o, i, j, k);
+  const Nbr q = nbr_of(o.g, i, j, k);
+  double v[11], xe[11];
+  row11_n(n, o, q, v);
+  row_x(x, q, xe);
+  double s = 0.0;
+#pragma unroll
+  for (int e = 0; e < 11; e++) s += v[e] * xe[e];
+  r[q.c] = b[q.c] - s;
 }
 
 template <typename T>

@@ -83,14 +83,11 @@ __device__ __forceinline__ int off_i(int e) { return (e == 0 || e == 6 || e == 7
 __device__ __forceinline__ int off_j(int e) { return (e == 2 || e == 6 || e == 8) ? 1 : ((e == 3 || e == 7 || e == 9) ? -1 : 0); }
 __device__ __forceinline__ int off_k(int e) { return e == 4 ? 1 : (e == 5 ? -1 : 0); }
 
-// 11 coefficients of row (k,j,i) in the order above.
+// 11 coefficients of a row in the order above, from the density at the
+// centre and its six face neighbours.
 template <typename T>
-__device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int i, int j, int k, T v[11]) {
-  const GridG &g = o.g;
-  T nijk = gval(n, g, k, j, i);
-  T nmjk = gval(n, g, k, j, i - 1), npjk = gval(n, g, k, j, i + 1);
-  T nimk = gval(n, g, k, j - 1, i), nipk = gval(n, g, k, j + 1, i);
-  T nijm = gval(n, g, k - 1, j, i), nijp = gval(n, g, k + 1, j, i);
+__device__ __forceinline__ void row11_vals(const OpK &o, T nijk, T nmjk, T npjk, T nimk, T nipk, T nijm, T nijp,
+                                           T v[11]) {
   if (o.unit) nijk = nmjk = npjk = nimk = nipk = nijm = nijp = T(1);
   T sxx, syy, szz, sod;
   op_scales(o, sxx, syy, szz, sod);
@@ -106,6 +103,67 @@ __device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int
   v[5] = szz * (nijk + nijm);
   v[10] = -(sxx * (npjk + T(2) * nijk + nmjk) + syy * (nipk + T(2) * nijk + nimk) +
             szz * (nijp + T(2) * nijk + nijm));
+}
+
+// 11 coefficients of row (k,j,i) in the order above.
+template <typename T>
+__device__ __forceinline__ void row11(const T *__restrict__ n, const OpK &o, int i, int j, int k, T v[11]) {
+  const GridG &g = o.g;
+  row11_vals(o, gval(n, g, k, j, i), gval(n, g, k, j, i - 1), gval(n, g, k, j, i + 1), gval(n, g, k, j - 1, i),
+             gval(n, g, k, j + 1, i), gval(n, g, k - 1, j, i), gval(n, g, k + 1, j, i), v);
+}
+
+// The neighbours of cell (i,j,k) as offsets from its linear index, with the
+// ghost semantics of gval: a periodic axis wraps, a ghosted one reads 0 past
+// its edge (valid flag false).  Computed once per cell, so that the row's 18
+// loads need no wrap logic of their own.
+struct Nbr {
+  unsigned c;                   // linear index of the cell
+  int xm, xp, ym, yp, zm, zp;   // offsets of the six face neighbours
+  bool vxm, vxp, vym, vyp, vzm, vzp;
+};
+__device__ __forceinline__ Nbr nbr_of(const GridG &g, int i, int j, int k) {
+  Nbr q;
+  const int sy = g.nx, sz = g.nx * g.ny;
+  q.c = ((unsigned)k * g.ny + j) * g.nx + i;
+  q.xm = i > 0 ? -1 : g.nx - 1;
+  q.xp = i < g.nx - 1 ? 1 : 1 - g.nx;
+  q.ym = j > 0 ? -sy : (g.ny - 1) * sy;
+  q.yp = j < g.ny - 1 ? sy : (1 - g.ny) * sy;
+  q.zm = k > 0 ? -sz : (g.nz - 1) * sz;
+  q.zp = k < g.nz - 1 ? sz : (1 - g.nz) * sz;
+  q.vxm = i > 0 || !g.bc[0];
+  q.vxp = i < g.nx - 1 || !g.bc[0];
+  q.vym = j > 0 || !g.bc[1];
+  q.vyp = j < g.ny - 1 || !g.bc[1];
+  q.vzm = k > 0 || !g.bc[2];
+  q.vzp = k < g.nz - 1 || !g.bc[2];
+  return q;
+}
+template <typename T>
+__device__ __forceinline__ T nval(const T *__restrict__ F, const Nbr &q, int off, bool valid) {
+  return valid ? F[(unsigned)((int)q.c + off)] : T(0);
+}
+// The 11 coefficients of the row (the same operands as row11).
+template <typename T>
+__device__ __forceinline__ void row11_n(const T *__restrict__ n, const OpK &o, const Nbr &q, T v[11]) {
+  row11_vals(o, n[q.c], nval(n, q, q.xm, q.vxm), nval(n, q, q.xp, q.vxp), nval(n, q, q.ym, q.vym),
+             nval(n, q, q.yp, q.vyp), nval(n, q, q.zm, q.vzm), nval(n, q, q.zp, q.vzp), v);
+}
+// x at the row's 11 entries, in the order of off_i/off_j/off_k.
+template <typename T>
+__device__ __forceinline__ void row_x(const T *__restrict__ x, const Nbr &q, T xe[11]) {
+  xe[0] = nval(x, q, q.xp, q.vxp);
+  xe[1] = nval(x, q, q.xm, q.vxm);
+  xe[2] = nval(x, q, q.yp, q.vyp);
+  xe[3] = nval(x, q, q.ym, q.vym);
+  xe[4] = nval(x, q, q.zp, q.vzp);
+  xe[5] = nval(x, q, q.zm, q.vzm);
+  xe[6] = nval(x, q, q.xp + q.yp, q.vxp && q.vyp);
+  xe[7] = nval(x, q, q.xp + q.ym, q.vxp && q.vym);
+  xe[8] = nval(x, q, q.xm + q.yp, q.vxm && q.vyp);
+  xe[9] = nval(x, q, q.xm + q.ym, q.vxm && q.vym);
+  xe[10] = x[q.c];
 }
 
 // (A x)(k,j,i)
