@@ -106,9 +106,10 @@ __global__ void k_zline_rows(OpK o, const T *__restrict__ n, T *__restrict__ lo,
                              T *__restrict__ dg) {
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const Nbr q = nbr_of(o.g, i, j, k);
   T v[11];
-  row11(n, o, i, j, k, v);
-  const unsigned c = lin3(o.g, i, j, k);
+  row11_n(n, o, q, v);
+  const unsigned c = q.c;
   lo[c] = v[5];
   up[c] = v[4];
   dg[c] = v[10];
@@ -328,34 +329,34 @@ __global__ void __launch_bounds__(32 * kMaxSeg) k_zline_seg(GridG g, ZlP<T> z, c
 }
 
 // ---- inter-grid transfer ---------------------------------------------------------
-// Full weighting (1/4,1/2,1/4 per axis) from fine (2I+a) to coarse I.
-template <typename T>
-__device__ __forceinline__ T restrict_at(const GridG &gf, const T *__restrict__ f, int I, int J, int K) {
-  T s = T(0);
-#pragma unroll
-  for (int dk = -1; dk <= 1; dk++) {
-    T wk = dk == 0 ? T(0.5) : T(0.25);
-#pragma unroll
-    for (int dj = -1; dj <= 1; dj++) {
-      T wj = dj == 0 ? T(0.5) : T(0.25);
-#pragma unroll
-      for (int di = -1; di <= 1; di++) {
-        T wi = di == 0 ? T(0.5) : T(0.25);
-        s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
-      }
-    }
-  }
-  return s;
-}
+// Full weighting (1/4,1/2,1/4 per axis) from fine (2I+a) to coarse I: the
+// 27 fine cells through the neighbour offsets of the fine cell (2I, 2J, 2K).
 template <typename T>
 __global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
   int I, J, K;
   if (!at3(gc.nx, gc.ny, I, J, K)) return;
-  c[lin3(gc, I, J, K)] = restrict_at(gf, f, I, J, K);
+  const Nbr q = nbr_of(gf, 2 * I, 2 * J, 2 * K);
+  const int oz[3] = {q.zm, 0, q.zp}, oy[3] = {q.ym, 0, q.yp}, ox[3] = {q.xm, 0, q.xp};
+  const bool vz[3] = {q.vzm, true, q.vzp}, vy[3] = {q.vym, true, q.vyp}, vx[3] = {q.vxm, true, q.vxp};
+  T s = T(0);
+#pragma unroll
+  for (int dk = 0; dk < 3; dk++) {
+    const T wk = dk == 1 ? T(0.5) : T(0.25);
+#pragma unroll
+    for (int dj = 0; dj < 3; dj++) {
+      const T wj = dj == 1 ? T(0.5) : T(0.25);
+#pragma unroll
+      for (int di = 0; di < 3; di++) {
+        const T wi = di == 1 ? T(0.5) : T(0.25);
+        s += wk * wj * wi * nval(f, q, oz[dk] + oy[dj] + ox[di], vz[dk] && vy[dj] && vx[di]);
+      }
+    }
+  }
+  c[lin3(gc, I, J, K)] = s;
 }
 
-// The same sum with the loops kept rolled (less code, for the single-block
-// cycle); the terms are added in the same order.
+// The same full-weighting sum with the loops kept rolled (less code, for the
+// single-block cycle); the terms are added in the same order as k_restrict.
 template <typename T>
 __device__ __forceinline__ T restrict_at_rolled(const GridG &gf, const T *__restrict__ f, int I, int J, int K) {
   T s = T(0);
@@ -388,11 +389,35 @@ __device__ __forceinline__ T prolong_at(const GridG &gc, const T *__restrict__ c
   return wi * wj * wk * s;
 }
 // f += P c.
+// The kernel's form: the coarse cells through the neighbour offsets of the
+// coarse cell (i/2, j/2, k/2); a term of the second cell along an axis is
+// added only for an odd index, in the order of prolong_at.
 template <typename T>
 __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__restrict__ f) {
   int i, j, k;
   if (!at3(gf.nx, gf.ny, i, j, k)) return;
-  f[lin3(gf, i, j, k)] += prolong_at(gc, c, i, j, k);
+  const Nbr q = nbr_of(gc, i >> 1, j >> 1, k >> 1);
+  const bool ti = i & 1, tj = j & 1, tk = k & 1;
+  const T wi = ti ? T(0.5) : T(1), wj = tj ? T(0.5) : T(1), wk = tk ? T(0.5) : T(1);
+  T s = T(0);
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    if (a == 1 && !tk) break;
+    const int oz = a ? q.zp : 0;
+    const bool vz = a ? q.vzp : true;
+#pragma unroll
+    for (int bq = 0; bq < 2; bq++) {
+      if (bq == 1 && !tj) break;
+      const int oy = bq ? q.yp : 0;
+      const bool vy = bq ? q.vyp : true;
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        if (e == 1 && !ti) break;
+        s += nval(c, q, oz + oy + (e ? q.xp : 0), vz && vy && (e ? q.vxp : true));
+      }
+    }
+  }
+  f[lin3(gf, i, j, k)] += wi * wj * wk * s;
 }
 
 // ---- whole V-cycle of the small levels in one thread block -------------------
