@@ -75,24 +75,25 @@ __global__ void k_rhs(GridG g, RhsK r, const double *__restrict__ mom, double *_
   int i, j, k0;
   if (at3(g.nx, g.ny, i, j, k0)) {
     for (int k = k0; k < g.nz; k += gridDim.z) {
-      rd nijk{gval(n, g, k, j, i)};
-      rd npjk{gval(n, g, k, j, i + 1)}, nmjk{gval(n, g, k, j, i - 1)};
-      rd nipk{gval(n, g, k, j + 1, i)}, nimk{gval(n, g, k, j - 1, i)};
-      rd nijp{gval(n, g, k + 1, j, i)}, nijm{gval(n, g, k - 1, j, i)};
+      const Nbr q = nbr_of(g, i, j, k);  // the neighbours' offsets (gval's wrap and ghosts)
+      rd nijk{n[q.c]};
+      rd npjk{nval(n, q, q.xp, q.vxp)}, nmjk{nval(n, q, q.xm, q.vxm)};
+      rd nipk{nval(n, q, q.yp, q.vyp)}, nimk{nval(n, q, q.ym, q.vym)};
+      rd nijp{nval(n, q, q.zp, q.vzp)}, nijm{nval(n, q, q.zm, q.vzm)};
       rd two{2.0}, one{1.0}, kap{r.kappa};
       rd dndx = rd{r.hx} * (npjk - nmjk);
       rd dndy = rd{r.hy} * (nipk - nimk);
       rd d2ndxx = rd{r.hxx} * ((npjk - two * nijk) + nmjk);
       rd d2ndyy = rd{r.hyy} * ((nipk - two * nijk) + nimk);
       rd d2ndzz = rd{r.hzz} * ((nijp - two * nijk) + nijm);
-      rd dGxdx = rd{r.hx} * (rd{gval(Gx, g, k, j, i + 1)} - rd{gval(Gx, g, k, j, i - 1)});
-      rd dGydy = rd{r.hy} * (rd{gval(Gy, g, k, j + 1, i)} - rd{gval(Gy, g, k, j - 1, i)});
-      rd dGzdz = rd{r.hz} * (rd{gval(Gz, g, k + 1, j, i)} - rd{gval(Gz, g, k - 1, j, i)});
+      rd dGxdx = rd{r.hx} * (rd{nval(Gx, q, q.xp, q.vxp)} - rd{nval(Gx, q, q.xm, q.vxm)});
+      rd dGydy = rd{r.hy} * (rd{nval(Gy, q, q.yp, q.vyp)} - rd{nval(Gy, q, q.ym, q.vym)});
+      rd dGzdz = rd{r.hz} * (rd{nval(Gz, q, q.zp, q.vzp)} - rd{nval(Gz, q, q.zm, q.vzm)});
       rd Eterm = (dndy - kap * dndx) * rd{r.E0};
       rd Pterm = rd{r.cth} * ((d2ndxx + d2ndyy) + (one + kap * kap) * d2ndzz);
       rd Gterm = rd{r.cG} * ((dGxdx + dGydy) + dGzdz);
       double v = (rd{r.scale} * ((Eterm + Pterm) + Gterm)).v;
-      b[lin3(g, i, j, k)] = v;
+      b[q.c] = v;
       local += v;
     }
   }
