@@ -221,7 +221,8 @@ def max_over_ranks(x, world):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"  # gloo: host tensors
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -544,8 +545,9 @@ def main():
     ap.add_argument("--grid", type=int, default=None, help="profiling only: smaller cube edge")
     ap.add_argument("--ppc", type=int, default=None, help="profiling only: ions per cell")
     ap.add_argument("--no-solver-graphs", action="store_true",
-                    help="profiling only: launch the FGMRES steps from the host instead of as one CUDA graph "
-                         "per cycle (same kernels; ncu then lists each solver kernel)")
+                    help="profiling only: launch the field phase (RHS, set-up, refinement sweeps, FGMRES steps) "
+                         "kernel by kernel from the host instead of as one CUDA graph (same kernels; ncu then "
+                         "lists each one)")
     args = ap.parse_args()
     if args.grid:
         WORKLOAD["n"] = args.grid
