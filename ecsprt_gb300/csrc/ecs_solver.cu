@@ -2047,6 +2047,7 @@ int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it
   if ((rc = ecs_solver_alloc(ctx))) return rc;
   if (!identity_lhs(ctx) && (rc = mg_alloc<T>(ctx))) return rc;
   if ((rc = ensure_capture_streams(ctx))) return rc;
+  if ((rc = ensure_setup_streams(ctx))) return rc;  // the set-up forks onto them inside the capture
   const int64_t launches0 = ctx->launches;
   cudaStream_t user = ctx->stream;
   ctx->stream = ctx->capst[0];
