@@ -253,6 +253,24 @@ class Context:
         self._check(self._lib.ecs_particles_download(self._h, _ptr(pos), _ptr(vel)))
         return pos, vel
 
+    def particle_ids(self) -> np.ndarray:
+        """Identity of each ion in the order of :meth:`download_particles`:
+        its index in the arrays of the last upload (ecs_particles_ids)."""
+        n = int(self._lib.ecs_particles_count(self._h))
+        ids = np.empty(n, dtype=np.int32)
+        self._check(self._lib.ecs_particles_ids(self._h, _ptr(ids)))
+        return ids
+
+    def download_particles_in_upload_order(self):
+        """The ions in the order of the last upload (the mixed path's cell
+        sort reorders them on the device)."""
+        pos, vel = self.download_particles()
+        ids = self.particle_ids()
+        out_p, out_v = np.empty_like(pos), np.empty_like(vel)
+        out_p[ids] = pos
+        out_v[ids] = vel
+        return out_p, out_v
+
     @property
     def phi(self) -> np.ndarray:
         out = np.empty(self.shape)

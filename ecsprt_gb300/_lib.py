@@ -154,6 +154,7 @@ GPU_API = [
     ("ecs_particles_upload", C.c_int, [_vp, _vp, _vp, C.c_int64]),
     ("ecs_particles_download", C.c_int, [_vp, _vp, _vp]),
     ("ecs_particles_count", C.c_int64, [_vp]),
+    ("ecs_particles_ids", C.c_int, [_vp, _vp]),
     ("ecs_particles_init", C.c_int, [_vp, C.c_int, C.c_int64, C.c_uint64, C.POINTER(EcsDensityModes)]),
     ("ecs_phi_upload", C.c_int, [_vp, _vp]),
     ("ecs_phi_download", C.c_int, [_vp, _vp]),

@@ -83,6 +83,9 @@ int read_status(EcsCtx *ctx) {
 
 }  // namespace
 
+// The parameter checks of ecs_ctx_create, shared with ecs_rhs_noalloc.
+int ecs_validate_params(const EcsParams *p) { return validate(p); }
+
 extern "C" {
 
 const char *ecs_version(void) { return "ecsprt-gb300 0.1.0 (sm_103a)"; }
@@ -272,6 +275,11 @@ int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel) {
 }
 
 int64_t ecs_particles_count(const EcsCtx *ctx) { return ctx ? ctx->np : -1; }
+
+int ecs_particles_ids(EcsCtx *ctx, int32_t *ids) {
+  if (!ctx || (ctx->np > 0 && !ids)) return ECS_ERR_INVALID;
+  return ecs_part_ids(ctx, ids);
+}
 
 int ecs_particles_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes) {
   if (!ctx) return ECS_ERR_INVALID;

@@ -118,7 +118,7 @@ struct EcsCtx {
   double *vx = nullptr, *vy = nullptr, *vz = nullptr;
 
   // Mixed particles: one 32-byte record per ion (a DRAM sector), two float4:
-  //   (int32 cell bits, FP32 in-cell offsets ox, oy, oz), (FP32 vx, vy, vz, 0),
+  //   (int32 cell bits, FP32 in-cell offsets ox, oy, oz), (FP32 vx, vy, vz, int32 identity),
   // double-buffered for the counting sort.
   float4 *ions[2] = {nullptr, nullptr};
   int cur = 0;
@@ -204,6 +204,8 @@ struct EcsCtx {
 
 // ---- error helpers -------------------------------------------------------
 int ecs_fail(EcsCtx *ctx, int code, const char *fmt, ...);
+// The parameter checks of ecs_ctx_create (ECS_OK or the failing status).
+int ecs_validate_params(const EcsParams *p);
 // Ions per staging chunk of the host transfers (two chunks are held): an
 // eighth of the capacity, between 2^16 and 2^22 ions.
 inline int64_t ecs_stage_ions(int64_t cap) {
@@ -290,6 +292,7 @@ int ecs_particles_free(EcsCtx *ctx);
 int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
 int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes);
 int ecs_part_download(EcsCtx *ctx, double *pos, double *vel);
+int ecs_part_ids(EcsCtx *ctx, int32_t *ids);
 // Enqueue the download after ctx->stream's current work; ecs_part_xfer_wait
 // waits for it.
 int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel);

@@ -649,24 +649,29 @@ __device__ __forceinline__ void unpack_cell(int32_t c, int &i, int &j, int &kk) 
 }
 
 // Ion record ip: two float4 at ions[2 ip], ions[2 ip + 1].  The particle
-// arrays are far larger than L2, so they are streamed (evict-first).
+// arrays are far larger than L2, so they are streamed (evict-first).  The
+// last word carries the ion's identity: its index in the host arrays of the
+// last upload (or in the device initialisation), which the kernels pass
+// through unchanged, so that ions can be matched after the sort reorders
+// them (ecs_particles_ids).
 struct Ion {
   int32_t c;
   float ox, oy, oz, vx, vy, vz;
+  int32_t id;
 };
 __device__ __forceinline__ Ion load_ion(const float4 *ions, int64_t ip) {
   const float4 a = __ldcs(ions + 2 * ip), b = __ldcs(ions + 2 * ip + 1);
-  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z};
+  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z, __float_as_int(b.w)};
 }
 // The same through the read-only cache: consecutive ions of one lane share
 // cache lines (each record is read before it is written, by the same thread).
 __device__ __forceinline__ Ion load_ion_ro(const float4 *ions, int64_t ip) {
   const float4 a = __ldg(ions + 2 * ip), b = __ldg(ions + 2 * ip + 1);
-  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z};
+  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z, __float_as_int(b.w)};
 }
 __device__ __forceinline__ void store_ion(float4 *ions, int64_t ip, const Ion &q) {
   __stcs(ions + 2 * ip, make_float4(__int_as_float(q.c), q.ox, q.oy, q.oz));
-  __stcs(ions + 2 * ip + 1, make_float4(q.vx, q.vy, q.vz, 0.f));
+  __stcs(ions + 2 * ip + 1, make_float4(q.vx, q.vy, q.vz, __int_as_float(q.id)));
 }
 __device__ __forceinline__ int32_t ion_cell(const float4 *ions, int64_t ip) {
   return __ldcs(reinterpret_cast<const int32_t *>(ions) + 8 * ip);
@@ -807,6 +812,7 @@ constexpr int kWindowMax = 4000;  // ions between window flushes (flux words <= 
 struct IonState {
   int i, j, kk;
   float ox, oy, oz, vx, vy, vz;
+  int id;
 };
 // Ew (nullptr: none) is a window of the difference numerators in shared
 // memory, kWX x kWY x kWZ nodes from node (wx0, wy0, wz0) at strides kEX, kEXY.
@@ -861,10 +867,11 @@ __device__ __forceinline__ IonState ion_state(const Ion &r) {
   IonState q;
   unpack_cell(r.c, q.i, q.j, q.kk);
   q.ox = r.ox; q.oy = r.oy; q.oz = r.oz; q.vx = r.vx; q.vy = r.vy; q.vz = r.vz;
+  q.id = r.id;
   return q;
 }
 __device__ __forceinline__ Ion ion_record(const IonState &q) {
-  return {q.i | (q.j << 10) | (q.kk << 20), q.ox, q.oy, q.oz, q.vx, q.vy, q.vz};
+  return {q.i | (q.j << 10) | (q.kk << 20), q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, q.id};
 }
 
 // Any ion order: grid-stride over ions, deposit by warp-level cell groups
@@ -882,7 +889,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
        base += stride) {
     const int64_t ip = base + lane;
     const bool active = ip < np;
-    IonState q = ion_state(active ? load_ion(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
+    IonState q = ion_state(active ? load_ion(ions, ip) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0});
     unsigned int nacc = 0, nref = 0;
     if (active) ion_update(k, mode, E, st, q, nacc, nref);
     if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
@@ -953,7 +960,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
         const bool active = si < seg && qi < L;
         const int64_t ip = (int64_t)ca + qi;
         const int64_t sp = (perm && active) ? (int64_t)__ldg(perm + ip) : ip;
-        IonState q = ion_state(active ? load_ion_ro(src, sp) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
+        IonState q = ion_state(active ? load_ion_ro(src, sp) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0});
         if (active) ion_update(k, mode, E, st, q, nacc, nref, ewin, wx0, wy0, wz0);
         if (active) {
           const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
@@ -1076,7 +1083,7 @@ __device__ __forceinline__ int to_cell(double pos, double d, int N, float &o) {
 }
 
 __global__ void k_aos_to_mixed(int64_t n, int nd, PartK k, const double *__restrict__ pos,
-                               const double *__restrict__ vel, float4 *__restrict__ ions) {
+                               const double *__restrict__ vel, float4 *__restrict__ ions, int64_t id0) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float a, b, c = 0.0f;
@@ -1084,7 +1091,7 @@ __global__ void k_aos_to_mixed(int64_t n, int nd, PartK k, const double *__restr
     int cj = to_cell(pos[nd * i + 1], k.dy, k.Ny, b);
     int ck = nd == 3 ? to_cell(pos[3 * i + 2], k.dz, k.Nz, c) : 0;
     store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[nd * i], (float)vel[nd * i + 1],
-                        nd == 3 ? (float)vel[3 * i + 2] : 0.0f});
+                        nd == 3 ? (float)vel[3 * i + 2] : 0.0f, (int32_t)(id0 + i)});
   }
 }
 
@@ -1103,6 +1110,12 @@ __global__ void k_mixed_to_aos(int64_t n, int nd, PartK k, double *__restrict__ 
       vel[3 * i + 2] = q.vz;
     }
   }
+}
+
+// ids[i] = identity of the i-th ion record (the order of a download).
+__global__ void k_mixed_ids(int64_t n, const float4 *__restrict__ ions, int32_t *__restrict__ ids) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    ids[i] = __float_as_int(ions[2 * i + 1].w);
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
@@ -1464,7 +1477,8 @@ __global__ void k_init_ions(InitK ik, PartK k, int64_t n, int fp64, float4 *__re
       const int ci = to_cell(pos[0], k.dx, k.Nx, a);
       const int cj = to_cell(pos[1], k.dy, k.Ny, b);
       const int ck = to_cell(pos[2], k.dz, k.Nz, c);
-      store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[0], (float)vel[1], (float)vel[2]});
+      store_ion(ions, i, {ci | (cj << 10) | (ck << 20), a, b, c, (float)vel[0], (float)vel[1], (float)vel[2],
+                          (int32_t)i});
     }
   }
 }
@@ -1562,7 +1576,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
       k_aos_to_soa64<<<g, kBlock, 0, ctx->stream>>>(n, nd, st, st + nd * n, ctx->px + off, ctx->py + off,
                                                    ctx->pz + off, ctx->vx + off, ctx->vy + off, ctx->vz + off);
     } else {
-      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, nd, k, st, st + nd * n, ctx->ions[ctx->cur] + 2 * off);
+      k_aos_to_mixed<<<g, kBlock, 0, ctx->stream>>>(n, nd, k, st, st + nd * n, ctx->ions[ctx->cur] + 2 * off, off);
     }
     ECS_LAUNCHED(ctx);
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
@@ -1710,6 +1724,26 @@ int ecs_part_download(EcsCtx *ctx, double *pos, double *vel) {
   int rc = ecs_part_download_async(ctx, pos, vel);
   if (rc) return rc;
   return ecs_part_xfer_wait(ctx);
+}
+
+// The identity of every ion, in the order ecs_part_download returns them.
+int ecs_part_ids(EcsCtx *ctx, int32_t *ids) {
+  const int64_t np = ctx->np;
+  if (np == 0) return ECS_OK;
+  if (ctx->prec == ECS_PREC_FP64) {  // the FP64 path never reorders its ions
+    for (int64_t i = 0; i < np; i++) ids[i] = (int32_t)i;
+    return ECS_OK;
+  }
+  int rc = settle_order(ctx);
+  if (rc) return rc;
+  int32_t *d = nullptr;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&d, (size_t)np * sizeof(int32_t), ctx->stream));
+  k_mixed_ids<<<grid_blocks(ctx, np, 8), kBlock, 0, ctx->stream>>>(np, ctx->ions[ctx->cur], d);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaMemcpyAsync(ids, d, (size_t)np * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return ECS_OK;
 }
 
 // One pass of the particle kernel over all ions.  With `count_for_sort` the

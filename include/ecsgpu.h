@@ -136,8 +136,16 @@ int ecs_set_solver_graphs(EcsCtx *ctx, int on);
 /* pos/vel are AoS FP64: pos[ip*ndim+d], vel[ip*ndim+d] (src/velocities.c:342-356;
    ndim = 2 for -ndim 2, src/velocities.c:254-266). */
 int ecs_particles_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t np);
+/* The mixed path keeps its ions counting-sorted by cell, so a download
+   returns them in the device's order, not the order of the upload (as
+   DMSwarmMigrate reorders a swarm across ranks, src/boundaries.c:92). */
 int ecs_particles_download(EcsCtx *ctx, double *pos, double *vel);
 int64_t ecs_particles_count(const EcsCtx *ctx);
+/* ids[i] = the identity of the i-th ion of a download: its index in the
+   arrays of the last ecs_particles_upload (or in ecs_particles_init).  The
+   FP64 path never reorders, so there ids[i] = i.  No counterpart in the
+   reference (a single-rank DMSwarm keeps its order). */
+int ecs_particles_ids(EcsCtx *ctx, int32_t *ids);
 
 /* ---- initial ions generated on the device -------------------------------- */
 /* Position distributions: the PDistType values of src/positions.c:8-10 that
@@ -188,19 +196,24 @@ int ecs_solve(EcsCtx *ctx, double rtol, int max_it, int warm_start, EcsSolveStat
 int ecs_lhs_apply_host(EcsCtx *ctx, const double *x, double *y);
 
 /* RHS for callers that cannot allocate device memory (no counterpart in the
-   reference; it computes what ecs_rhs computes).  For code that owns all of
-   its device memory in its own pool and may not call cudaMalloc inside its
-   step loop, or cannot accept the device synchronisation an allocation may
-   cause: no allocation of any kind is made.  d_moments (device, FluidNode
-   {n,Gx,Gy,Gz} per node, [Nz][Ny][Nx][4]) and d_rhs (device, [Nz][Ny][Nx])
-   belong to the caller; the work is queued on `stream` (a cudaStream_t,
-   NULL for the default stream).  Its reduction scratch is a fixed 32 KiB
-   __device__ array held by every device that loads the library, so grids of
-   more than 8,388,608 nodes (256 x 256 x 128) are rejected with
-   ECS_ERR_INVALID.  The first call on a device looks up the array's device
-   address (cudaGetSymbolAddress); make that first call before any stream
-   capture.  Calls share the scratch: calls that overlap on the GPU race.
-   Errors are reported by ecs_last_error(NULL). */
+   reference; it computes what ecs_rhs computes for the same parameters:
+   -rhs full in 3-D or 2-D, -rhs sinusoidal, -rhs constant).  For code that
+   owns all of its device memory in its own pool and may not call cudaMalloc
+   inside its step loop, or cannot accept the device synchronisation an
+   allocation may cause: no allocation of any kind is made.  d_moments
+   (device, FluidNode {n,Gx,Gy,Gz} per node, [Nz][Ny][Nx][4]; unused, and
+   may be NULL, unless -rhs full) and d_rhs (device, [Nz][Ny][Nx]) belong to
+   the caller; the work is queued on `stream` (a cudaStream_t, NULL for the
+   default stream).  The parameters are checked as ecs_ctx_create checks
+   them.  Its reduction scratch is a fixed __device__ array of 32 KiB + 8 B
+   held by every device that loads the library, so grids of more than
+   8,388,608 nodes (256 x 256 x 128) are rejected with ECS_ERR_INVALID.  The
+   first call on a device looks up the array's device address
+   (cudaGetSymbolAddress) and keeps it for the life of the process; make
+   that first call before any stream capture, and do not call it on a device
+   after cudaDeviceReset.  Every call shares the one scratch array: calls
+   that overlap on the GPU (unordered streams) race.  Errors are reported by
+   ecs_last_error(NULL). */
 int ecs_rhs_noalloc(const EcsParams *params, const double *d_moments, double *d_rhs, void *stream);
 
 /* One time step of src/pic.c:244-258: push, collide (if mn > 0), move + BC,

@@ -201,6 +201,68 @@ class Oracle:
         its = self.L.orc_gmres(C.byref(self.p), _p(n), _p(b), _p(x), rtol, maxit, restart, C.byref(rel))
         return x, its, rel.value
 
+    def solve_fft(self, density, b, rtol=1e-13, maxit=400, restart=40):
+        """The same converged potential as :meth:`solve`, reached faster on a
+        fully periodic grid: restarted GMRES right-preconditioned by the
+        operator assembled from the mean density (constant coefficients, so
+        a periodic convolution that the FFT diagonalises; its stencil is the
+        oracle operator's response to a unit impulse).  The operator applied
+        is the oracle's variable-coefficient one throughout, the iterate is
+        kept mean-free as the reference's null-space projection does, and
+        the stop test is the true FP64 residual ||b - A x|| / ||b||.  Grids
+        with a non-periodic axis use :meth:`solve`."""
+        if any(int(c) for c in self.p.bc):
+            return self.solve(density, b, rtol=rtol)
+        n = np.ascontiguousarray(density, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        imp = np.zeros(self.shape)
+        imp[0, 0, 0] = 1.0
+        lam = np.fft.fftn(self.lhs_apply(np.full(self.shape, n.mean()), imp))
+        lam[0, 0, 0] = np.inf  # the constant null space: no mean in the correction
+
+        def prec(r):
+            return np.real(np.fft.ifftn(np.fft.fftn(r) / lam))
+
+        def mf(v):
+            return v - v.mean()
+
+        bnorm = np.linalg.norm(b)
+        x = np.zeros(self.shape)
+        if bnorm == 0.0:
+            return x, 0, 0.0
+        its = 0
+        while True:
+            r = b - self.lhs_apply(n, x)
+            rel = np.linalg.norm(r) / bnorm
+            if rel <= rtol or its >= maxit:
+                return mf(x), its, rel
+            beta = np.linalg.norm(r)
+            V = [r / beta]
+            Z = []
+            H = np.zeros((restart + 1, restart))
+            for j in range(restart):
+                z = prec(V[j])
+                Z.append(z)
+                w = self.lhs_apply(n, z)
+                for q in range(j + 1):  # modified Gram-Schmidt, twice
+                    h = np.vdot(V[q], w)
+                    H[q, j] += h
+                    w = w - h * V[q]
+                for q in range(j + 1):
+                    h = np.vdot(V[q], w)
+                    H[q, j] += h
+                    w = w - h * V[q]
+                H[j + 1, j] = np.linalg.norm(w)
+                its += 1
+                e1 = np.zeros(j + 2)
+                e1[0] = beta
+                y, *_ = np.linalg.lstsq(H[: j + 2, : j + 1], e1, rcond=None)
+                est = np.linalg.norm(H[: j + 2, : j + 1] @ y - e1) / bnorm
+                if H[j + 1, j] == 0.0 or est <= 0.1 * rtol or its >= maxit:
+                    break
+                V.append(w / H[j + 1, j])
+            x = mf(x + sum(yq * zq for yq, zq in zip(y, Z)))
+
     def collide(self, vel, dt):
         vel = np.array(vel, dtype=np.float64, order="C")
         stats = np.zeros(3, dtype=np.int64)

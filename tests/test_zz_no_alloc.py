@@ -6,17 +6,21 @@ device synchronisation an allocation can cause).  The caller passes device
 input and output buffers; the entry point's reduction scratch is a fixed
 __device__ array.  This test allocates the caller's buffers itself (as such a
 caller would, from its own pool), calls the entry point through the C ABI
-twice in a row with different grids, and checks each result against the
-context entry point ecs_rhs with the RHS tolerance used throughout the GPU
-tests (1e-14 relative).  It lives in a file collected last so that a run
-stopping at the first failure has already run every other test.
+on several grids in a row (3-D and 2-D, the full RHS and the -rhs
+sinusoidal and -rhs constant options), and checks each result against the
+context entry point ecs_rhs and the reference's golden RHS with the RHS
+tolerance used throughout the GPU tests (1e-14 relative).  It lives in a
+file collected last so that a run stopping at the first failure has already
+run every other test.
 """
 import ctypes
+import json
 
 import numpy as np
 import pytest
 
 import ecsprt_gb300 as E
+from conftest import GOLDEN, load_golden
 from ecsprt_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
@@ -62,15 +66,33 @@ def _rhs_noalloc(rt, p, moments):
     return out
 
 
-def test_rhs_noalloc_matches_context_entry_point(built, golden):
+def _cases():
+    """(name, params, moments, golden RHS) for the full RHS in 3-D (two
+    grids) and 2-D, and the -rhs sinusoidal and -rhs constant options."""
+    out = []
+    for name in ("fb", "c1", "twod"):
+        g = load_golden(name)
+        out.append((name, E.params_from_options(g["opts"]), g["moments"], g["rhs"]))
+    ops = np.load(GOLDEN / "ops.npz")
+    variants = json.loads(str(ops["variants"]))
+    for v in ("full_sin", "id_const"):
+        p = E.params_from_options(str(ops["opts_base"]) + variants[v])
+        dens = ops["full_sin_density"] if v == "full_sin" else np.zeros((p.Nz, p.Ny, p.Nx))
+        m = np.zeros(dens.shape + (4,))
+        m[..., 0] = dens
+        out.append((v, p, m, ops[f"{v}_rhs"]))
+    return out
+
+
+def test_rhs_noalloc_matches_context_entry_point(built):
     rt = _cudart()
-    cases = [golden["fb"], golden["c1"], golden["fb"]]
-    for g in cases:  # consecutive calls share the scratch array
-        p = E.params_from_options(g["opts"])
-        expect = _rhs_with_context(p, g["moments"])
-        got = _rhs_noalloc(rt, p, g["moments"])
-        assert _rel_inf(got, expect) <= 1e-14
-        assert _rel_inf(got, g["rhs"]) <= 1e-14
+    cases = _cases()
+    for name, p, moments, golden_rhs in cases + cases[:1]:  # consecutive calls share the scratch array
+        expect = _rhs_with_context(p, moments)
+        got = _rhs_noalloc(rt, p, moments)
+        assert np.isfinite(got).all(), name
+        assert _rel_inf(got, expect) <= 1e-14, name
+        assert _rel_inf(got, golden_rhs) <= 1e-14, name
 
 
 def test_rhs_noalloc_rejects_grids_beyond_its_scratch(built):
