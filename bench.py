@@ -68,6 +68,58 @@ RECORD_BYTES_MIXED = 68
 TRAFFIC_BYTES_PER_ION = 67.9
 
 
+def mg_levels(nx, ny, nz):
+    """Cells of the multigrid levels: full coarsening while every axis stays
+    even and at least 8 (the solver's rule)."""
+    out = []
+    while True:
+        out.append(nx * ny * nz)
+        flat = nz == 1
+        even = nx % 2 == 0 and ny % 2 == 0 and (flat or nz % 2 == 0)
+        if not even or min(nx, ny, nx if flat else nz) < 8 or len(out) >= 12:
+            return out
+        nx, ny = nx // 2, ny // 2
+        if not flat:
+            nz //= 2
+
+
+# Algorithmic bytes of the field phase (RHS, operator set-up, solve), by the
+# rule 12 B a cell for an FP32 operator or smoother application and 24 B for
+# an FP64 one (read the iterate and the density, write the result), 4 B (FP32)
+# or 8 B (FP64) a cell for every other vector read or written; each level at
+# its own cell count.
+B_OP32, B_OP64, B_V32, B_V64 = 12, 24, 4, 8
+
+
+def field_phase_bytes(levels, iterations, refinements):
+    """Bytes of one field phase of the mixed path with `iterations` FGMRES
+    steps in `refinements` FP64 refinement sweeps (the steps taken as evenly
+    spread over the sweeps' cycles)."""
+    n0 = levels[0]
+    rhs = 4 * B_V64 * n0 + B_V64 * n0 + 2 * B_V64 * n0  # moments in, b out; mean removal (read, write)
+    setup = (B_V64 + B_V32) * n0  # FP64 density -> FP32
+    for i, n in enumerate(levels):
+        if i:
+            setup += B_V32 * (levels[i - 1] + n)  # full-weighting restriction of the density
+        setup += B_V32 * n * (1 + 2 + 2 + 6)  # z-line rows (density in, 2 out), factors (2 in, 6 out)
+    vcycle = 0
+    for i, n in enumerate(levels[:-1]):
+        vcycle += 2 * B_OP32 * n + 2 * B_OP32 * n  # pre- and post-smoothing, residual, post-smoothing RHS
+        vcycle += B_V32 * (3 * n + 2 * levels[i + 1])  # restriction (read r, write b), prolongation (x in, t rw)
+    vcycle += B_V32 * levels[-1] * (levels[-1] + 2)  # coarsest: explicit inverse times b
+    k = iterations / max(refinements, 1)
+    steps = 0.0
+    j = 0.0
+    while j < k:  # Arnoldi step j: V-cycle, mean, operator, two Gram-Schmidt passes
+        frac = min(1.0, k - j)
+        steps += frac * (vcycle + B_V32 * n0 + B_OP32 * n0 + 2 * B_V32 * n0 + (3 * j + 9) * B_V32 * n0)
+        j += 1.0
+    cycle = B_V32 * n0 * 5 + B_V32 * n0 * (k + 1)  # ||b||, start vectors; x = Z y
+    sweep = (B_OP64 + 2 * B_V64) * n0 + B_V64 * n0 + (B_V64 + B_V32) * n0 + (B_V32 + 2 * B_V64) * n0 + \
+        3 * B_V64 * n0  # FP64 residual, norm, scale to FP32, phi += e, mean projection
+    return rhs + setup + refinements * (cycle + sweep) + refinements * steps
+
+
 def options(w):
     n = w["n"]
     return (f"-Nx {n} -Ny {n} -Nz {n} -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x {w['drift']} "
@@ -177,8 +229,8 @@ class ClockSampler:
 def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
     """The oracle port of the reference's particle phase (push, collide,
     move + BC, deposit in FP64), timed on the host cores on a bounded sample
-    of the same workload; the potential solve is not included, which only
-    raises the CPU rate."""
+    of the same workload; the potential solve is timed separately
+    (cpu_solve_baseline)."""
     from oracle import oracle as orc
     import ecsprt_gb300 as E
 
@@ -205,7 +257,46 @@ def cpu_baseline(w, pos, vel, phi, seconds_target=20.0):
             "sample": f"{S} ions of the workload x {steps} steps of push+collide+move+deposit (FP64, "
                       f"{threads} OpenMP threads for push, move and deposit (the deposit split into one z slab "
                       f"a thread, as the reference's ranks split the domain); collide serial as in the "
-                      f"reference); the potential solve is excluded"}
+                      f"reference); the potential solve is timed separately (solve)"}
+
+
+def cpu_solve_baseline(w, moments):
+    """The FP64 potential solve on the host cores, to the workload's 1e-8
+    relative residual: the oracle's RHS and variable-coefficient operator
+    (OpenMP) in restarted GMRES right-preconditioned by the FFT inverse of
+    the mean-density operator (numpy; a stand-in for the reference's PETSc
+    GMRES + hypre BoomerAMG, neither of which exists here).  Timed on the
+    workload's own moments (the system the GPU solved) and on one density of
+    each stand-alone solve size ({32,48,64,96,128}^3, lognormal x Fourier
+    modes, flux = density)."""
+    from oracle import oracle as orc
+    import ecsprt_gb300 as E
+    from ecsprt_gb300 import workloads as W
+
+    orc.build()
+
+    def one(p, m):
+        O = orc.Oracle(p)
+        t0 = time.perf_counter()
+        b = O.rhs(m)
+        _, its, rel = O.solve_fft(m[..., 0], b, rtol=1e-8)
+        return time.perf_counter() - t0, its, rel
+
+    t, its, rel = one(E.params_from_options(options(w)), moments)
+    sizes = {}
+    rng = np.random.default_rng(20261206)
+    for n in W.SOLVE_SIZES:
+        dens = W.solve_density(n, rng)
+        m = np.zeros(dens.shape + (4,))
+        m[..., 0] = dens
+        m[..., 1:] = dens[..., None]
+        tn, itn, _ = one(E.params_from_options(W.solver_options(n)), m)
+        sizes[str(n)] = {"ms": 1e3 * tn, "iterations": itn}
+    mix = len(sizes) / sum(v["ms"] * 1e-3 for v in sizes.values())
+    return {"kind": "port", "cores": orc.num_threads(),
+            "method": "oracle RHS + FP64 GMRES(40), FFT-preconditioned by the mean-density operator, to 1e-8",
+            "workload_solve_ms": 1e3 * t, "workload_iterations": its, "workload_relres": rel,
+            "solves_per_s": 1.0 / t, "by_size": sizes, "mixed_sizes_solves_per_s": mix}
 
 
 def dist_setup():
@@ -250,25 +341,54 @@ def workload_config(w, world):
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU path (the oracle port) for a whole step of the
+    workload on a bounded sample: a 32^3 box at the workload's 64 ions per
+    cell (2,097,152 ions) with the same physics, each step push + collide +
+    move/BC + deposit + RHS + the FP64 potential solve to 1e-8
+    (cpu_solve_baseline's method), the potential carried from step to step."""
     if rank != 0:
         return
-    w = WORKLOAD
-    pos, vel = make_particles(w, count=1 << 21)
-    phi = np.zeros((w["n"],) * 3)
-    per = []
+    from oracle import oracle as orc
+    import ecsprt_gb300 as E
+
+    orc.build()
+    w = dict(WORKLOAD, n=32, name=WORKLOAD["name"].replace("128^3", "32^3"))
+    pos, vel = make_particles(w)
+    S = pos.shape[0]
+    p = E.params_from_options(options(w))
+    O = orc.Oracle(p)
+    dt = w["dt"]
+    m = O.collect_mt(pos, vel)
+    phi, _, _ = O.solve_fft(m[..., 0], O.rhs(m), rtol=1e-8)
+
+    def step():
+        nonlocal pos, vel, phi
+        vel = O.push(pos, vel, phi, dt)
+        vel, _, _ = O.collide(vel, dt)
+        pos, vel = O.move(pos, vel, dt)
+        mm = O.collect_mt(pos, vel)
+        phi, _, rel = O.solve_fft(mm[..., 0], O.rhs(mm), rtol=1e-8)
+        assert rel <= 1e-8
+
     for _ in range(args.warmup):
-        cpu_baseline(w, pos, vel, phi, seconds_target=0.0)
+        step()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        per.append(cpu_baseline(w, pos, vel, phi, seconds_target=0.0))
-    value = float(np.mean([c["value"] for c in per]))
-    c = dict(per[0])
-    c["value"] = value
+        step()
+    el = time.perf_counter() - t0
+    value = S * args.steps / el
+    threads = orc.num_threads()
+    c = {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+         "sample": f"a 32^3 box of the workload at 64 ions/cell ({S} ions), {args.steps} whole steps: push, "
+                   f"collide (serial, as the reference), move/BC, deposit ({threads} OpenMP threads), RHS and "
+                   f"the FP64 potential solve to 1e-8 (oracle operator, FFT-preconditioned GMRES), the "
+                   f"potential carried between steps"}
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * (1 << 21) / value, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(workload_config(w, 1), sample_ions=1 << 21,
+        "config": dict(workload_config(WORKLOAD, 1), sample="32^3 x 64 ions/cell", sample_ions=S,
                        precision="FP64 (the reference's CPU path, restated by the oracle)"),
         "cpu_baseline": c,
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -405,6 +525,65 @@ def run_serve_sims(E, W, ninst, nsteps, seed=20261207):
             "hbm_budget_bytes": SERVE_BUDGET, "max_inflight": SERVE_INFLIGHT}
 
 
+def _timed_steps(ctx, stream, n_ions, steps, warmup, dt, rtol=1e-8):
+    import torch
+
+    for _ in range(warmup):
+        ctx.step(dt, rtol, 400)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = [ctx.step(dt, rtol, 400) for _ in range(steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el = e0.elapsed_time(e1) * 1e-3
+    return {"value": n_ions * steps / el, "unit": "particle-steps/s", "ms_per_step": 1e3 * el / steps,
+            "steps": steps, "warmup": warmup,
+            "particle_ms": 1e3 * float(np.mean([s.particle_seconds for s in st])),
+            "field_ms": 1e3 * float(np.mean([s.solve.seconds for s in st])),
+            "iterations": [s.solve.iterations for s in st], "max_relres": max(s.solve.relres for s in st),
+            "collisions_per_step": float(np.mean([s.collisions for s in st]))}
+
+
+def run_c1(E, stream, args):
+    """32^3 periodic, 16 ions/cell (524,288), drift 0.5, nu 0.05, dt 0.1, the
+    reference's Sobol positions and Maxwellian velocities (generated on the
+    device), solve to 1e-8: the plain FP64 path and the mixed path."""
+    n = 32
+    p = E.params_from_options(f"-Nx {n} -Ny {n} -Nz {n} -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 "
+                              f"-vi0x 0.5 -nui 0.05 -nue 8.79e9 -Te 11604.5 -E0 0")
+    N = 16 * n ** 3
+    out = {"workload": "32^3 periodic, 16 ions/cell (524,288 ions), drift 0.5, nu 0.05, Sobol positions, dt 0.1"}
+    for name, prec in (("fp64", E.ECS_PREC_FP64), ("mixed", E.ECS_PREC_MIXED)):
+        with E.Context(p, prec, np_capacity=N, stream=stream.cuda_stream) as ctx:
+            ctx.init_particles(E.ECS_INIT_SOBOL, N, seed=20261203)
+            ctx.collect()
+            ctx.compute_potential(rtol=1e-8, max_it=400)
+            out[name] = _timed_steps(ctx, stream, N, max(args.steps, 20), max(args.warmup, 3), 0.1)
+    return out
+
+
+def run_c3(E, stream, args):
+    """256 x 256 x 128, periodic x/y, reflecting z, 32 ions/cell
+    (268,435,456 ions), density 1 + 8 Fourier modes of amplitude 0.02,
+    drift 0.5, nu 0.02, mixed precision, cell sort every 4 steps, solve to
+    1e-8."""
+    from ecsprt_gb300 import workloads as W
+
+    p = E.params_from_options("-Nx 256 -Ny 256 -Nz 128 -dx 1 -dy 1 -dz 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 0.5 "
+                              "-nui 0.02 -nue 8.79e9 -Te 11604.5 -E0 0 -zBC inject-reflect")
+    N = 256 * 256 * 128 * 32
+    with E.Context(p, E.ECS_PREC_MIXED, np_capacity=N, stream=stream.cuda_stream) as ctx:
+        ctx.set_sort_every(4)
+        ctx.init_particles(E.ECS_INIT_MODES, N, seed=W.C3_SEED, modes=W.c3_modes())
+        ctx.collect()
+        ctx.compute_potential(rtol=1e-8, max_it=400)
+        r = _timed_steps(ctx, stream, N, max(args.steps, 8), max(args.warmup, 3), 0.1)
+    r["workload"] = ("256x256x128, periodic x/y, reflecting z, 32 ions/cell (268,435,456 ions), density 1 + 8 "
+                     "Fourier modes (0.02), drift 0.5, nu 0.02, sort every 4, mixed")
+    return r
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -457,6 +636,10 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peaks()
     achieved = ALGO_BYTES_MIXED * N / part_s.mean() / 1e9
     phi_now = ctx.phi
+    mom_now = ctx.moments if not args.skip_cpu else None
+    lv = mg_levels(p.Nx, p.Ny, p.Nz)
+    fbytes = np.array([field_phase_bytes(lv, s.solve.iterations, s.solve.refinements) for s in stats])
+    solve_gbs = float((fbytes / solve_s).mean()) / 1e9
 
     # ---------------- end to end through host buffers ------------------
     e2e = None
@@ -488,7 +671,7 @@ def run_ours(args, world, rank, local):
         ctx64.collect()
         ctx64.compute_potential(rtol=rtol, max_it=400)
         ctx64.step(dt, rtol, 400)
-        k64 = max(1, min(3, args.steps))
+        k64 = max(1, args.steps)
         torch.cuda.synchronize()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
@@ -501,6 +684,8 @@ def run_ours(args, world, rank, local):
                  "solve_ms": 1e3 * float(np.mean([s.solve.seconds for s in st64]))}
         ctx64.close()
 
+    configs = None if args.skip_configs else {"c1": run_c1(E, stream, args), "c3": run_c3(E, stream, args)}
+
     serving = None
     if not args.skip_serve:
         from ecsprt_gb300 import workloads as W
@@ -510,6 +695,8 @@ def run_ours(args, world, rank, local):
     if rank != 0:
         return
     cpu = cpu_baseline(w, pos, vel, phi_now) if not args.skip_cpu else None
+    if cpu is not None:
+        cpu["solve"] = cpu_solve_baseline(w, mom_now)
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -523,6 +710,13 @@ def run_ours(args, world, rank, local):
                                        "on the 64^3 case, per ion, times the ions here",
                      "algorithmic_bytes_per_launch": ALGO_BYTES_MIXED * N,
                      "design_bytes_per_launch": RECORD_BYTES_MIXED * N},
+        "roofline_solve": {"bound": "hbm", "phase": "field phase: RHS + operator set-up + solve (one graph)",
+                           "achieved": solve_gbs, "peak": peak, "unit": "GB/s", "frac": solve_gbs / peak,
+                           "peak_kind": peak_kind, "bytes_per_phase": float(fbytes.mean()),
+                           "bytes_rule": "12 B a cell an FP32 operator or smoother application, 24 B FP64, "
+                                         "4 / 8 B a cell every other FP32 / FP64 vector read or written, each "
+                                         "multigrid level at its own size (bench.field_phase_bytes)",
+                           "solves_per_s": float(1.0 / solve_s.mean())},
         "solve_latency_ms": {"p50": 1e3 * float(np.percentile(solve_s, 50)),
                              "p99": 1e3 * float(np.percentile(solve_s, 99)),
                              "iterations": its, "max_relres": relres},
@@ -530,6 +724,7 @@ def run_ours(args, world, rank, local):
                      "sort": 1e3 * float(sort_s.mean()) if sort_s.size else 0.0},
         "collisions_per_step": collisions,
         "plain_fp64": plain,
+        "configs": configs,
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "serving": serving,
@@ -547,6 +742,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--skip-serve", action="store_true", help="leave out the request-loop measurements")
+    ap.add_argument("--skip-configs", action="store_true",
+                    help="leave out the 32^3 FP64 and 256x256x128 reflecting-z workload lines")
     ap.add_argument("--serve-requests", type=int, default=10000, help="stand-alone solve requests (Poisson, 200/s)")
     ap.add_argument("--serve-steps", type=int, default=500, help="steps of each of the 48 served simulations")
     ap.add_argument("--grid", type=int, default=None, help="profiling only: smaller cube edge")

@@ -1,4 +1,5 @@
-"""Build libecsgpu.so (CUDA, sm_103a) and libecshost.so (host C) in-tree.
+"""Build libecsgpu.so (CUDA, sm_103a), libecshost.so (host C) and the
+re-hosted programs pic and solver in-tree.
 
 Translation units compile in parallel; a unit is rebuilt only when its
 source, a shared header or the flags change.  Run as a module
@@ -38,6 +39,9 @@ CC_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-Wextra", "-Wno-unused-param
 GPU_SOURCES = ["ecs_api.cu", "ecs_particles.cu", "ecs_grid.cu", "ecs_solver.cu", "ecs_noalloc.cu", "ecs_serve.cu"]
 HOST_SOURCES = ["ecs_options.c", "ecs_io.c"]
 GPU_HOST_SOURCES = ["ecs_ops.c"]  # host C linked into libecsgpu (operator slots)
+# the reference's programs re-hosted on the libraries: program -> main source
+PROGRAMS = {"pic": "ecs_pic_main.c", "solver": "ecs_solver_main.c"}
+DRIVER_SOURCES = ["ecs_driver.c"]
 
 LIBGPU = OUT / "libecsgpu.so"
 LIBHOST = OUT / "libecshost.so"
@@ -110,10 +114,24 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict:
         r = subprocess.run(link_host, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"host link failed: {r.stderr}")
+    programs = {}
+    for prog, main in PROGRAMS.items():
+        srcs = [HOST / main] + [HOST / d for d in DRIVER_SOURCES]
+        exe = OUT / prog
+        flags = CC_FLAGS + [f"-I{HOST}"] + [str(x) for x in srcs] + [
+            "-o", str(exe), f"-L{OUT}", "-lecsgpu", "-lecshost", "-lm", "-Wl,-rpath,$ORIGIN"]
+        stamp = OUT / (prog + ".stamp")
+        digest = _digest(srcs + headers + [LIBGPU, LIBHOST], flags)
+        if not (exe.exists() and stamp.exists() and stamp.read_text() == digest):
+            r = subprocess.run([cc] + flags, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link of {prog} failed: {r.stderr}")
+            stamp.write_text(digest)
+        programs[prog] = str(exe)
     if verbose:
         for w in warnings:
             sys.stderr.write(w)
-    return {"gpu": str(LIBGPU), "host": str(LIBHOST), "warnings": warnings}
+    return {"gpu": str(LIBGPU), "host": str(LIBHOST), "programs": programs, "warnings": warnings}
 
 
 if __name__ == "__main__":

@@ -461,20 +461,36 @@ int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stat
   return rc;
 }
 
-// The ions come from and go back to the host arrays; their download runs on
-// side streams while the potential is solved.
+// The ions come from and go back to the host arrays.  When the arrays hold
+// the ions as the previous call returned them, the upload, the particle pass
+// and the download are pipelined by ranges of tiles (ecs_part_host_pass);
+// otherwise the ions are uploaded and sorted first.  Either way the ions'
+// download overlaps the potential solve.
 int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, double rtol, int max_it,
                   double *moments_out, double *phi_out, EcsStepStats *stats) {
   if (!ctx || !pos || !vel || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
-  int rc = ecs_part_upload(ctx, pos, vel, np);
-  if (rc) return rc;
   EcsDevStatus coll;
   int sorted = 0;
-  if ((rc = step_particles(ctx, dt, &coll, &sorted))) return rc;
-  if ((rc = ecs_part_download_async(ctx, pos, vel))) return rc;
+  int rc = ensure_eext(ctx, ctx->eext_ready);
+  if (rc) return rc;
+  ctx->ev_particle = ctx->ev_sort = false;
+  ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
+  rc = ecs_part_host_pass(ctx, pos, vel, np, dt, &sorted);
+  if (rc == ECS_ERR_STATE) {  // no hand-off from a previous call: upload (and sort) first
+    if ((rc = ecs_part_upload(ctx, pos, vel, np))) return rc;
+    if ((rc = step_particles(ctx, dt, &coll, &sorted))) return rc;
+    if ((rc = ecs_part_download_async(ctx, pos, vel))) return rc;
+  } else {
+    if (rc) return rc;
+    coll = *ctx->hstat;
+    if (ctx->p.mn <= 0.0) memset(&coll, 0, sizeof coll);
+    if ((rc = ecs_grid_moments(ctx))) return rc;
+    if ((rc = read_status(ctx))) return rc;
+  }
   EcsSolveStats st;
   const int rc_field = step_field(ctx, rtol, max_it, &st);
   if ((rc = ecs_part_xfer_wait(ctx))) return rc;
+  ctx->host_gen = ctx->pgen;  // the host arrays now hold the device's ions, in the buffer's next order
   if (rc_field) return rc_field;
   step_stats(ctx, coll, sorted, st, stats);
   if (moments_out && (rc = moments_to_host(ctx, moments_out))) return rc;

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -200,6 +201,14 @@ struct EcsCtx {
   cudaEvent_t xev_ready = nullptr;  // the ions are ready for a download
   double *stage[2] = {nullptr, nullptr};
   int64_t stage_n = 0;              // ions per staging buffer
+  // Host hand-off of ecs_step_host: the ions' download runs beside the next
+  // chunk's upload, through its own staging buffers and events.
+  double *stage_dn[2] = {nullptr, nullptr};
+  cudaEvent_t xev_dn_conv[2] = {nullptr, nullptr}, xev_dn_copy[2] = {nullptr, nullptr};
+  uint64_t pgen = 0;                // bumped by every change of the device ions
+  uint64_t host_gen = ~0ull;        // pgen when ecs_step_host last returned the ions to the host
+  bool bounds_valid = false;        // tile_bounds holds the current sort's tile offsets
+  std::vector<int32_t> tile_bounds; // first ion of every tile, and np (ntiles + 1)
 };
 
 // ---- error helpers -------------------------------------------------------
@@ -229,6 +238,37 @@ int ecs_cuda_check(EcsCtx *ctx, cudaError_t e, const char *what);
   } while (0)
 
 static inline unsigned int ecs_div_up(size_t a, size_t b) { return (unsigned int)((a + b - 1) / b); }
+
+// Programmatic dependent launch: a kernel launched by ecs_launch_pdl may be
+// scheduled while the kernel before it on the stream (or before it in a
+// captured graph) is still finishing, and waits in ecs_pdl_wait until that
+// kernel has completed and its writes are visible.  Every kernel launched
+// this way calls ecs_pdl_wait before touching global memory, and then lets
+// its own successor be scheduled (ecs_pdl_trigger); for a kernel launched
+// the ordinary way both are no-ops.
+__device__ __forceinline__ void ecs_pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void ecs_pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+#define ECS_PDL_ENTRY() \
+  do {                  \
+    ecs_pdl_wait();     \
+    ecs_pdl_trigger();  \
+  } while (0)
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t ecs_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                  Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // ---- counter-based RNG: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) --
 struct EcsU4 {
@@ -293,6 +333,10 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
 int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDensityModes *modes);
 int ecs_part_download(EcsCtx *ctx, double *pos, double *vel);
 int ecs_part_ids(EcsCtx *ctx, int32_t *ids);
+// The particle pass of ecs_step_host when the host arrays hold the ions as
+// the previous ecs_step_host call returned them: upload, pass and download
+// pipelined by ranges of tiles.  ECS_ERR_STATE (nothing done) otherwise.
+int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, int *sorted);
 // Enqueue the download after ctx->stream's current work; ecs_part_xfer_wait
 // waits for it.
 int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel);

@@ -61,6 +61,8 @@ struct TileG {
 struct FixScale64 {
   double s;
   __device__ __forceinline__ long long put(double v) const { return __double2ll_rn(v * s); }
+  // flux contribution v w
+  __device__ __forceinline__ long long putvw(double v, double w) const { return put(v * w); }
 };
 
 // FP32: the same integer, rint(v 2^S) with |v 2^S| <= 2^38 (S = 38 on the
@@ -110,15 +112,17 @@ __device__ __forceinline__ long long fix_unbias(unsigned hi_sum, unsigned lo_sum
 // int32 only for ions whose velocity components are within 2^(e_v - 3)
 // (words <= 2^19: kWindowMax x 2^19 < 2^31); faster ions add theirs to the
 // int64 accumulators directly.
+// A flux contribution v w is rounded once: with vs = v 2^S (exact), the
+// fused multiply-add vs w + bias rounds the exact product to an integer.
 struct FixWord32 {
   float s;  // 2^S
-  __device__ __forceinline__ int word(float v) const {
-    return (int)(__float_as_uint(__fmaf_rn(v, s, kFixBias)) - kFixBiasBits);
+  // the biased word bits(bias) + rint(vs w)
+  __device__ __forceinline__ unsigned biased(float vs, float w) const {
+    return __float_as_uint(__fmaf_rn(vs, w, kFixBias));
   }
-  // the biased word bits(bias) + rint(v 2^S) in a 64-bit tile entry
-  __device__ __forceinline__ long long put(float v) const {
-    return (long long)__float_as_uint(__fmaf_rn(v, s, kFixBias));
-  }
+  __device__ __forceinline__ int word(float vs, float w) const { return (int)(biased(vs, w) - kFixBiasBits); }
+  // the biased word in a 64-bit tile entry
+  __device__ __forceinline__ long long putvw(float v, float w) const { return (long long)biased(v * s, w); }
 };
 
 // Exact sum of the tile entries q in `m` (bit mask of lanes).
@@ -242,15 +246,15 @@ __device__ __forceinline__ void deposit_warp(long long *__restrict__ acc, long l
   const int lane = threadIdx.x & 31;
   const T wxl = T(1) - wxh, wyl = T(1) - wyh, wzl = T(1) - wzh;
   // inactive lanes contribute the zero entry (bias included for FP32)
-  const long long zero_n = fn.put(T(0)), zero_f = ff.put(T(0));
+  const long long zero_n = fn.put(T(0)), zero_f = ff.putvw(T(0), T(0));
 #pragma unroll
   for (int b = 0; b < 8; b++) {
     const T wz = (b & 4) ? wzh : wzl, wy = (b & 2) ? wyh : wyl, wx = (b & 1) ? wxh : wxl;
     const T w = wz * wy * wx;
     tile[(b + 0) * kTileStride + lane] = active ? fn.put(w) : zero_n;
-    tile[(b + 8) * kTileStride + lane] = active ? ff.put(v0 * w) : zero_f;
-    tile[(b + 16) * kTileStride + lane] = active ? ff.put(v1 * w) : zero_f;
-    tile[(b + 24) * kTileStride + lane] = active ? ff.put(v2 * w) : zero_f;
+    tile[(b + 8) * kTileStride + lane] = active ? ff.putvw(v0, w) : zero_f;
+    tile[(b + 16) * kTileStride + lane] = active ? ff.putvw(v1, w) : zero_f;
+    tile[(b + 24) * kTileStride + lane] = active ? ff.putvw(v2, w) : zero_f;
   }
   const int key = active ? (i | (j << 10) | (kk << 20)) : -1;
   const unsigned peers = __match_any_sync(ECS_FULL_MASK, key);
@@ -359,18 +363,28 @@ __device__ __forceinline__ double coll_vc(const CollK<double> &c, double vi, dou
 __device__ __forceinline__ bool coll_refuse(const CollK<float> &c, float vf2) { return sqrtf(vf2) > c.vlim; }
 __device__ __forceinline__ bool coll_refuse(const CollK<double> &c, double vf2) { return sqrt(vf2) / c.viT > 10.0; }
 
-// One ion's collisions in one pass (src/collisions.c:70-157): a Poisson
-// number of attempts (rate k.rate) by inversion of a uniform drawn from the
-// state hash mixed with the step and seed; each attempt draws a Maxwellian
-// neutral, accepts with U1*U2 < |vr|^2/vrm^2, and scatters isotropically in
-// the centre-of-mass frame.
+// Gate uniform of one ion in one pass: a uniform from the hash `a` (the
+// FP64 path: its state hash; the mixed path: its identity) mixed with the
+// step and seed.  The ion makes at least one collision attempt when
+// u > exp(-rate) (gate_open), the common case being none.
+__device__ __forceinline__ float gate_uniform(const PartK &k, uint32_t a) {
+  return ecs_u01f(ecs_mix32(a ^ k.stepmix));
+}
+__device__ __forceinline__ bool gate_open(const PartK &k, float u) { return u > k.p0f; }
+
+// Counter words of the mixed path's collision streams: the ion's identity
+// and a tag (the FP64 path keys by its 64-bit state hash instead).
+constexpr uint32_t kIdTag = 0x49444B59u;
+
+// One ion's collisions in one pass (src/collisions.c:70-157) once its gate is
+// open: a Poisson number of attempts (rate k.rate) by inversion of the gate
+// uniform u; each attempt draws a Maxwellian neutral from Philox keyed by
+// (c0, c1, attempt, step), accepts with U1*U2 < |vr|^2/vrm^2, and scatters
+// isotropically in the centre-of-mass frame.
 template <typename T>
-__device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &vy, T &vz,
-                            unsigned int &nacc, unsigned int &nref) {
+__device__ void collide_attempts(const PartK &k, uint32_t h0, uint32_t h1, float u, T &vx, T &vy, T &vz,
+                                 unsigned int &nacc, unsigned int &nref) {
   typedef RMath<T> M;
-  const uint32_t hu = ecs_mix32(h1 ^ k.stepmix);
-  const float u = ecs_u01f(hu);
-  if (u <= k.p0f) return;  // no attempt (the common case)
   const CollK<T> ck(k);
   float p = k.p0f, cdf = p;
   const float rate = k.ratef;
@@ -446,6 +460,13 @@ __device__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, T &vx, T &
       nacc++;
     }
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void collide_ion(const PartK &k, uint32_t h0, uint32_t h1, uint32_t a, T &vx, T &vy,
+                                            T &vz, unsigned int &nacc, unsigned int &nref) {
+  const float u = gate_uniform(k, a);
+  if (gate_open(k, u)) collide_attempts<T>(k, h0, h1, u, vx, vy, vz, nacc, nref);
 }
 
 // Warp-aggregated status counters.
@@ -617,7 +638,7 @@ __global__ void __launch_bounds__(kBlock) k_particles64(PartK k, int mode, int64
       if (active) {
         uint32_t h0, h1;
         hash64(x, y, z, vx, vy, vz, h0, h1);
-        collide_ion<double>(k, h0, h1, vx, vy, vz, nacc, nref);
+        collide_ion<double>(k, h0, h1, h1, vx, vy, vz, nacc, nref);
       }
       flush_counts(st, nacc, nref);
     }
@@ -661,12 +682,6 @@ struct Ion {
 };
 __device__ __forceinline__ Ion load_ion(const float4 *ions, int64_t ip) {
   const float4 a = __ldcs(ions + 2 * ip), b = __ldcs(ions + 2 * ip + 1);
-  return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z, __float_as_int(b.w)};
-}
-// The same through the read-only cache: consecutive ions of one lane share
-// cache lines (each record is read before it is written, by the same thread).
-__device__ __forceinline__ Ion load_ion_ro(const float4 *ions, int64_t ip) {
-  const float4 a = __ldg(ions + 2 * ip), b = __ldg(ions + 2 * ip + 1);
   return {__float_as_int(a.x), a.y, a.z, a.w, b.x, b.y, b.z, __float_as_int(b.w)};
 }
 __device__ __forceinline__ void store_ion(float4 *ions, int64_t ip, const Ion &q) {
@@ -779,12 +794,6 @@ __device__ __forceinline__ bool bound_axis(int bc, int N, int &c, float &o, floa
   return c >= 0 && c < N;
 }
 
-__device__ __forceinline__ void hash32(int32_t c, float ox, float oy, float oz, float vx,
-                                       float vy, float vz, uint32_t &h0, uint32_t &h1) {
-  uint32_t w[7] = {(uint32_t)c, __float_as_uint(ox), __float_as_uint(oy), __float_as_uint(oz),
-                   __float_as_uint(vx), __float_as_uint(vy), __float_as_uint(vz)};
-  state_hash(w, 7, h0, h1);
-}
 
 constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
 constexpr int kWNodes = kWX * kWY * kWZ;
@@ -814,38 +823,36 @@ struct IonState {
   float ox, oy, oz, vx, vy, vz;
   int id;
 };
-// Ew (nullptr: none) is a window of the difference numerators in shared
-// memory, kWX x kWY x kWZ nodes from node (wx0, wy0, wz0) at strides kEX, kEXY.
-__device__ __forceinline__ void ion_update(const PartK &k, int mode, const float4 *__restrict__ E, EcsDevStatus *st,
-                                           IonState &q, unsigned int &nacc, unsigned int &nref,
-                                           const float4 *Ew = nullptr, int wx0 = 0, int wy0 = 0, int wz0 = 0) {
-  if (mode & 1) {
-    float f[3];
-    const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
-    if (Ew && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
-      const int base = lk * kEXY + lj * kEX + li;
-      float4 D[8];
+// Push (src/velocities.c:281-371) of one ion.  Ew (nullptr: none) is a
+// window of the difference numerators in shared memory, kWX x kWY x kWZ nodes
+// from node (wx0, wy0, wz0) at strides kEX, kEXY.
+__device__ __forceinline__ void ion_push(const PartK &k, const float4 *__restrict__ E, IonState &q,
+                                         const float4 *Ew = nullptr, int wx0 = 0, int wy0 = 0, int wz0 = 0) {
+  float f[3];
+  const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
+  if (Ew && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
+    const int base = lk * kEXY + lj * kEX + li;
+    float4 D[8];
 #pragma unroll
-      for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kEX, kEXY, b)];
-      interp8(D, q.ox, q.oy, q.oz, f);
-    } else {
-      gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
-    }
-    float vxm = q.vx + k.escf[0] * f[0];
-    float vym = q.vy + k.escf[1] * f[1];
-    float vzm = q.vz + k.escf[2] * f[2];
-    float vxt = vxm + vym * k.tf;
-    float vyp = vym - vxt * k.sf;
-    float vxp = vxt + vyp * k.tf;
-    q.vx = vxp;
-    q.vy = vyp;
-    q.vz = vzm;
+    for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kEX, kEXY, b)];
+    interp8(D, q.ox, q.oy, q.oz, f);
+  } else {
+    gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
   }
-  if ((mode & 2) && k.collide) {
-    uint32_t h0, h1;
-    hash32(q.i | (q.j << 10) | (q.kk << 20), q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, h0, h1);
-    collide_ion<float>(k, h0, h1, q.vx, q.vy, q.vz, nacc, nref);
-  }
+  float vxm = q.vx + k.escf[0] * f[0];
+  float vym = q.vy + k.escf[1] * f[1];
+  float vzm = q.vz + k.escf[2] * f[2];
+  float vxt = vxm + vym * k.tf;
+  float vyp = vym - vxt * k.sf;
+  float vxp = vxt + vyp * k.tf;
+  q.vx = vxp;
+  q.vy = vyp;
+  q.vz = vzm;
+}
+
+// Move + boundary conditions (src/positions.c:436-472, src/boundaries.c:6-34)
+// in the pass's mode, then the velocity checks.
+__device__ __forceinline__ void ion_move(const PartK &k, int mode, EcsDevStatus *st, IonState &q) {
   if (mode & 4) {
     q.i += advance(q.ox, q.vx * k.dtc[0]);
     q.j += advance(q.oy, q.vy * k.dtc[1]);
@@ -862,6 +869,16 @@ __device__ __forceinline__ void ion_update(const PartK &k, int mode, const float
   if (!(isfinite(q.vx) && isfinite(q.vy) && isfinite(q.vz))) atomicOr(&st->flags, ECS_FLAG_NONFINITE);
   if ((mode & 8) && !(fabsf(q.vx) <= k.vmaxf && fabsf(q.vy) <= k.vmaxf && fabsf(q.vz) <= k.vmaxf))
     atomicOr(&st->flags, ECS_FLAG_RANGE);
+}
+
+// Push, collisions (src/collisions.c:9-167; keyed by the ion's identity) and
+// move of one ion in the pass's mode bits.
+__device__ __forceinline__ void ion_update(const PartK &k, int mode, const float4 *__restrict__ E, EcsDevStatus *st,
+                                           IonState &q, unsigned int &nacc, unsigned int &nref) {
+  if (mode & 1) ion_push(k, E, q);
+  if ((mode & 2) && k.collide)
+    collide_ion<float>(k, (uint32_t)q.id, kIdTag, (uint32_t)q.id, q.vx, q.vy, q.vz, nacc, nref);
+  ion_move(k, mode, st, q);
 }
 __device__ __forceinline__ IonState ion_state(const Ion &r) {
   IonState q;
@@ -909,40 +926,120 @@ __global__ void __launch_bounds__(kBlock, 3) k_particles32(PartK k, int mode, in
 // One block per tile of cells processes the ions of the tile's key range
 // (the ions that were in the tile at the last sort) in chunks of at most
 // kWindowMax.  Each chunk deposits into a shared-memory window of the nodes
-// of the tile's cells widened by one cell on every side: the two int32 words
-// of each contribution's fixed-point value (H, rint(r)) are added with
-// shared-memory atomics, and the window is added to the global int64
-// accumulators once per chunk.  The chunk is split into 32 consecutive
-// segments, one per lane, so the lanes of a warp work on different cells and
-// rarely on the same node.  Ions outside the window (moved farther, or
-// wrapped around a periodic edge) deposit straight into the global
-// accumulators.  The cells of the moved ions are counted the same way when a
-// sort follows.  All sums are exact integers, so the moments equal those of
-// k_particles32 bit for bit.
+// of the tile's cells widened by one cell on every side: five int32 words a
+// contribution (the density's two fixed-point words H, rint(r) and one word
+// for each flux component), added with shared-memory atomics as biased
+// words (bits(bias) + value; the bias of every contribution is taken out at
+// the flush from per-cell counts of the window's ions), and the window is
+// added to the global int64 accumulators once per chunk.  The chunk is split
+// into 32 consecutive segments, one per lane, so the lanes of a warp work on
+// different cells and rarely on the same node.  Ions outside the window
+// (moved farther, or wrapped around a periodic edge) deposit straight into
+// the global accumulators.  The cells of the moved ions are counted the same
+// way when a sort follows.
+//
+// Loads: each thread's next ion record is copied into shared memory with
+// cp.async while it works on the current one (and the permutation entry of
+// the one after that is loaded into a register), so the memory latency of a
+// record overlaps the arithmetic of the previous ion.  All sums are exact
+// integers, so the moments equal those of k_particles32 bit for bit.
+// 16-byte global -> shared copy that bypasses L1 (cp.async.cg), and the group
+// bookkeeping of the issuing thread.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prior1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+struct TileCtx {
+  int wx0, wy0, wz0;  // window origin (node and cell index of its corner)
+};
+
+__device__ __forceinline__ bool in_cell_window(int li, int lj, int lk) {
+  return li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ;
+}
+
+// The rest of one ion's pass after its push and collisions: move + BC and
+// checks, the cell count for the next sort, the deposit, and the record.
+__device__ __forceinline__ void tile_finish(const PartK &k, int mode, EcsDevStatus *st, IonState &q, int64_t ip,
+                                            const TileCtx &tc, unsigned (*win)[kWPad], int *dcnt, int *wcnt,
+                                            long long *__restrict__ acc, int32_t *__restrict__ count,
+                                            int32_t *__restrict__ keys, float4 *dst) {
+  ion_move(k, mode, st, q);
+  const int li = q.i - tc.wx0, lj = q.j - tc.wy0, lk = q.kk - tc.wz0;
+  const bool inwin = in_cell_window(li, lj, lk);
+  if (count) {
+    const int key = tile_key(q.i, q.j, q.kk, k.tg);
+    keys[ip] = key;
+    if (inwin) atomicAdd(&wcnt[(lk * kCY + lj) * kCX + li], 1);
+    else atomicAdd(&count[key], 1);
+  }
+  if (mode & 8) {
+    const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
+    const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
+    // weights w = (wz wy) wx, the product order of deposit_warp
+    const float wzy[4] = {wzl * wyl, wzl * wyh, wzh * wyl, wzh * wyh};
+    const float s = k.fixf32.s;
+    const float vxs = q.vx * s, vys = q.vy * s, vzs = q.vz * s;  // exact: s is a power of two
+    if (inwin && fabsf(q.vx) <= k.vwinf && fabsf(q.vy) <= k.vwinf && fabsf(q.vz) <= k.vwinf) {
+      const int n0 = lk * kSZ + lj * kSY + li;
+      atomicAdd(&dcnt[(lk * kCY + lj) * kCX + li], 1);
+#pragma unroll
+      for (int bc = 0; bc < 8; bc++) {
+        const float w = wzy[bc >> 1] * ((bc & 1) ? wxh : wxl);
+        const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
+        const float h = __fmaf_rn(w, k.fixn32.s_hi, kFixBias);
+        const float r = __fmaf_rn(__fsub_rn(h, kFixBias), k.fixn32.s_back, w);
+        atomicAdd(&win[0][nb], __float_as_uint(h));
+        atomicAdd(&win[1][nb], __float_as_uint(__fmaf_rn(r, k.fixn32.s, kFixBias)));
+        atomicAdd(&win[2][nb], k.fixf32.biased(vxs, w));
+        atomicAdd(&win[3][nb], k.fixf32.biased(vys, w));
+        atomicAdd(&win[4][nb], k.fixf32.biased(vzs, w));
+      }
+    } else {  // outside the window, or fast: straight into the global accumulators
+#pragma unroll 1
+      for (int bc = 0; bc < 8; bc++) {
+        const long long gnode = corner_node(k, q.i, q.j, q.kk, bc);
+        if (gnode < 0) continue;
+        const float w = (((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl)) * ((bc & 1) ? wxh : wxl);
+        int hi, lo;
+        k.fixn32.split(w, hi, lo);
+        atomicAdd((unsigned long long *)&acc[gnode], (unsigned long long)fix_join(hi, lo));
+        atomicAdd((unsigned long long *)&acc[k.ncell + gnode], (unsigned long long)(long long)k.fixf32.word(vxs, w));
+        atomicAdd((unsigned long long *)&acc[2 * k.ncell + gnode], (unsigned long long)(long long)k.fixf32.word(vys, w));
+        atomicAdd((unsigned long long *)&acc[3 * k.ncell + gnode], (unsigned long long)(long long)k.fixf32.word(vzs, w));
+      }
+    }
+  }
+  if (mode & 7) store_ion(dst, ip, ion_record(q));
+}
 
 __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const float4 *src, float4 *dst,
                                                      const int32_t *__restrict__ perm, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
                                                      int32_t *__restrict__ count, int32_t *__restrict__ keys,
-                                                     EcsDevStatus *st) {
-  __shared__ int win[5][kWPad];  // [density H, density rint(r), flux x, y, z][node, padded strides]
-  __shared__ int wcnt[kWCells];
+                                                     EcsDevStatus *st, int t_begin, int t_end) {
+  __shared__ unsigned win[5][kWPad];  // biased words [H, rint(r), flux x, y, z][node, padded strides]
+  __shared__ int wcnt[kWCells];       // cells of the moved ions (next sort)
+  __shared__ int dcnt[kWCells];       // window deposits a cell (bias removal)
   __shared__ float4 ewin[kEXY * kWZ];  // difference numerators of the window's nodes (padded strides)
+  __shared__ float4 pre[2][2 * kBlock];  // each thread's prefetched records, two iterations
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = k.tg.ntx * k.tg.nty * k.tg.ntz;
+  const bool collide = (mode & 2) && k.collide;
   unsigned int nacc = 0, nref = 0;  // collision counters of this thread, flushed at the end
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  for (int t = t_begin + blockIdx.x; t < t_end; t += gridDim.x) {
     const int tx = t % k.tg.ntx, ty = (t / k.tg.ntx) % k.tg.nty, tz = t / (k.tg.ntx * k.tg.nty);
     // window origin: one cell below the tile on every axis
-    const int wx0 = tx * ECS_TILE_X - 1, wy0 = ty * ECS_TILE_Y - 1, wz0 = tz * ECS_TILE_Z - 1;
+    const TileCtx tc{tx * ECS_TILE_X - 1, ty * ECS_TILE_Y - 1, tz * ECS_TILE_Z - 1};
     const int a = key_off[t * ECS_TILE_CELLS], b = key_off[(t + 1) * ECS_TILE_CELLS];
     if (a == b) continue;
     if (mode & 1) {  // window nodes outside the extended grid are never read
       const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
       for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
-        const int gx = wx0 + e % kWX, gy = wy0 + (e / kWX) % kWY, gz = wz0 + e / (kWX * kWY);
+        const int gx = tc.wx0 + e % kWX, gy = tc.wy0 + (e / kWX) % kWY, gz = tc.wz0 + e / (kWX * kWY);
         const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
-        ewin[(gz - wz0) * kEXY + (gy - wy0) * kEX + (gx - wx0)] =
+        ewin[(gz - tc.wz0) * kEXY + (gy - tc.wy0) * kEX + (gx - tc.wx0)] =
             in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
@@ -950,65 +1047,43 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
       const int L = min(kWindowMax, b - ca);
       const int seg = (L + 31) >> 5;               // lane segment
       const int sub = (seg + kBlock / 32 - 1) / (kBlock / 32);  // a warp's run inside each segment
-      if (mode & 8)
-        for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0;
+      if (mode & 8) {
+        for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0u;
+        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) dcnt[e] = 0;
+      }
       if (count)
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
       __syncthreads();
-      for (int m = 0; m < sub; m++) {  // warp-uniform trip count
-        const int si = warp * sub + m, qi = lane * seg + si;
-        const bool active = si < seg && qi < L;
-        const int64_t ip = (int64_t)ca + qi;
-        const int64_t sp = (perm && active) ? (int64_t)__ldg(perm + ip) : ip;
-        IonState q = ion_state(active ? load_ion_ro(src, sp) : Ion{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0});
-        if (active) ion_update(k, mode, E, st, q, nacc, nref, ewin, wx0, wy0, wz0);
-        if (active) {
-          const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
-          if (count) {
-            const int key = tile_key(q.i, q.j, q.kk, k.tg);
-            keys[ip] = key;
-            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ)
-              atomicAdd(&wcnt[(lk * kCY + lj) * kCX + li], 1);
-            else
-              atomicAdd(&count[key], 1);
-          }
-          if (mode & 8) {
-            const float wxh = q.ox, wyh = q.oy, wzh = q.oz;
-            const float wxl = 1.f - wxh, wyl = 1.f - wyh, wzl = 1.f - wzh;
-            if (li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ && fabsf(q.vx) <= k.vwinf &&
-                fabsf(q.vy) <= k.vwinf && fabsf(q.vz) <= k.vwinf) {
-              const int n0 = lk * kSZ + lj * kSY + li;
-#pragma unroll
-              for (int bc = 0; bc < 8; bc++) {
-                const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
-                const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
-                const int nb = n0 + (bc >> 2) * kSZ + ((bc >> 1) & 1) * kSY + (bc & 1);
-                int hi, lo;
-                k.fixn32.split(val[0], hi, lo);
-                atomicAdd(&win[0][nb], hi);
-                atomicAdd(&win[1][nb], lo);
-#pragma unroll
-                for (int f = 1; f < 4; f++) atomicAdd(&win[1 + f][nb], k.fixf32.word(val[f]));
-              }
-            } else {  // outside the window, or fast: straight into the global accumulators
-#pragma unroll 1
-              for (int bc = 0; bc < 8; bc++) {
-                const long long gnode = corner_node(k, q.i, q.j, q.kk, bc);
-                if (gnode < 0) continue;
-                const float w = ((bc & 4) ? wzh : wzl) * ((bc & 2) ? wyh : wyl) * ((bc & 1) ? wxh : wxl);
-                const float val[4] = {w, q.vx * w, q.vy * w, q.vz * w};
-                int hi, lo;
-                k.fixn32.split(val[0], hi, lo);
-                atomicAdd((unsigned long long *)&acc[gnode], (unsigned long long)fix_join(hi, lo));
-#pragma unroll
-                for (int f = 1; f < 4; f++)
-                  atomicAdd((unsigned long long *)&acc[(size_t)f * k.ncell + gnode],
-                            (unsigned long long)(long long)k.fixf32.word(val[f]));
-              }
-            }
-          }
-          if (mode & 7) store_ion(dst, ip, ion_record(q));
+      // this thread's ions: m = 0 .. sub-1 at qi = lane * seg + warp * sub + m
+      const int qi0 = lane * seg + warp * sub;
+      const int mend = min(sub, min(seg - warp * sub, L - qi0));  // active iterations (may be <= 0)
+      auto src_pos = [&](int m) -> int64_t {
+        const int64_t ip = (int64_t)ca + qi0 + m;
+        return perm ? (int64_t)__ldg(perm + ip) : ip;
+      };
+      int64_t sp_next = 0, sp_after = 0;
+      if (mend > 0) {
+        const int64_t sp0 = src_pos(0);
+        cp_async16(&pre[0][2 * threadIdx.x], src + 2 * sp0);
+        cp_async16(&pre[0][2 * threadIdx.x + 1], src + 2 * sp0 + 1);
+      }
+      cp_async_commit();
+      if (mend > 1) sp_next = src_pos(1);
+      for (int m = 0; m < mend; m++) {
+        if (m + 1 < mend) {  // the next record into the other slot
+          cp_async16(&pre[(m + 1) & 1][2 * threadIdx.x], src + 2 * sp_next);
+          cp_async16(&pre[(m + 1) & 1][2 * threadIdx.x + 1], src + 2 * sp_next + 1);
         }
+        cp_async_commit();
+        if (m + 2 < mend) sp_after = src_pos(m + 2);
+        cp_async_wait_prior1();  // this iteration's record has landed
+        const float4 ra = pre[m & 1][2 * threadIdx.x], rb = pre[m & 1][2 * threadIdx.x + 1];
+        IonState q = ion_state(Ion{__float_as_int(ra.x), ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, __float_as_int(rb.w)});
+        const int64_t ip = (int64_t)ca + qi0 + m;
+        if (mode & 1) ion_push(k, E, q, ewin, tc.wx0, tc.wy0, tc.wz0);
+        if (collide) collide_ion<float>(k, (uint32_t)q.id, kIdTag, (uint32_t)q.id, q.vx, q.vy, q.vz, nacc, nref);
+        tile_finish(k, mode, st, q, ip, tc, win, dcnt, wcnt, acc, count, keys, dst);
+        sp_next = sp_after;
       }
       __syncthreads();
       // window -> global accumulators
@@ -1016,16 +1091,25 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
         for (int nd = threadIdx.x; nd < kWNodes; nd += blockDim.x) {
           const int wxn = nd % kWX, wyn = (nd / kWX) % kWY, wzn = nd / (kWX * kWY);
           const int np_ = wzn * kSZ + wyn * kSY + wxn;
-          int gx = wx0 + wxn, gy = wy0 + wyn, gz = wz0 + wzn;
+          int gx = tc.wx0 + wxn, gy = tc.wy0 + wyn, gz = tc.wz0 + wzn;
           // nodes past the last cell wrap (periodic) or are dropped (ghosts)
           if (gx < 0 || gx >= k.Nx) { if (k.bc[0]) continue; gx = gx < 0 ? gx + k.Nx : gx - k.Nx; }
           if (gy < 0 || gy >= k.Ny) { if (k.bc[1]) continue; gy = gy < 0 ? gy + k.Ny : gy - k.Ny; }
           if (gz < 0 || gz >= k.Nz) { if (k.bc[2]) continue; gz = gz < 0 ? gz + k.Nz : gz - k.Nz; }
-          unsigned long long *dst = (unsigned long long *)acc + ((size_t)gz * k.Ny + gy) * k.Nx + gx;
+          // contributions to this node: window deposits of the (up to) 8 cells around it
+          int nc = 0;
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            const int cx = wxn - (c & 1), cy = wyn - ((c >> 1) & 1), cz = wzn - (c >> 2);
+            if (cx >= 0 && cx < kCX && cy >= 0 && cy < kCY && cz >= 0 && cz < kCZ) nc += dcnt[(cz * kCY + cy) * kCX + cx];
+          }
+          const unsigned bias = (unsigned)nc * kFixBiasBits;
+          unsigned long long *g = (unsigned long long *)acc + ((size_t)gz * k.Ny + gy) * k.Nx + gx;
 #pragma unroll
           for (int f = 0; f < 4; f++) {
-            const long long v = f == 0 ? fix_join(win[0][np_], win[1][np_]) : (long long)win[1 + f][np_];
-            if (v != 0) atomicAdd(dst + (size_t)f * k.ncell, (unsigned long long)v);
+            const long long v = f == 0 ? fix_join((int)(win[0][np_] - bias), (int)(win[1][np_] - bias))
+                                       : (long long)(int)(win[1 + f][np_] - bias);
+            if (v != 0) atomicAdd(g + (size_t)f * k.ncell, (unsigned long long)v);
           }
         }
       }
@@ -1033,7 +1117,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) {
           const int n = wcnt[e];
           if (n == 0) continue;
-          int gx = wx0 + e % kCX, gy = wy0 + (e / kCX) % kCY, gz = wz0 + e / (kCX * kCY);
+          int gx = tc.wx0 + e % kCX, gy = tc.wy0 + (e / kCX) % kCY, gz = tc.wz0 + e / (kCX * kCY);
           if (gx < 0) gx += k.Nx; else if (gx >= k.Nx) gx -= k.Nx;  // cells of moved ions are in range
           if (gy < 0) gy += k.Ny; else if (gy >= k.Ny) gy -= k.Ny;
           if (gz < 0) gz += k.Nz; else if (gz >= k.Nz) gz -= k.Nz;
@@ -1043,7 +1127,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
       __syncthreads();
     }
   }
-  if ((mode & 2) && k.collide) flush_counts(st, nacc, nref);
+  if (collide) flush_counts(st, nacc, nref);
 }
 
 // ---- upload / download conversions ---------------------------------------------
@@ -1116,6 +1200,31 @@ __global__ void k_mixed_to_aos(int64_t n, int nd, PartK k, double *__restrict__ 
 __global__ void k_mixed_ids(int64_t n, const float4 *__restrict__ ions, int32_t *__restrict__ ids) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     ids[i] = __float_as_int(ions[2 * i + 1].w);
+}
+
+// The same conversion as k_mixed_to_aos for the ions in key order: the i-th
+// output is the record at perm[i].
+__global__ void k_mixed_to_aos_perm(int64_t n, int nd, PartK k, double *__restrict__ pos, double *__restrict__ vel,
+                                    const float4 *__restrict__ ions, const int32_t *__restrict__ perm) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const Ion q = load_ion(ions, perm[i]);
+    int ci, cj, ck;
+    unpack_cell(q.c, ci, cj, ck);
+    pos[nd * i] = ((double)ci + (double)q.ox) * k.dx;
+    pos[nd * i + 1] = ((double)cj + (double)q.oy) * k.dy;
+    vel[nd * i] = q.vx; vel[nd * i + 1] = q.vy;
+    if (nd == 3) {
+      pos[3 * i + 2] = ((double)ck + (double)q.oz) * k.dz;
+      vel[3 * i + 2] = q.vz;
+    }
+  }
+}
+
+// out[t] = the first ion of tile t (t <= ntiles; out[ntiles] = np).
+__global__ void k_tile_bounds(int ntiles, const int32_t *__restrict__ key_off, int32_t *__restrict__ out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += gridDim.x * blockDim.x)
+    out[t] = key_off[(size_t)t * ECS_TILE_CELLS];
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
@@ -1267,9 +1376,7 @@ __global__ void k_estimate32(PartK k, int64_t np, const float4 *__restrict__ ion
     float sample = 0.f;
     if (active) {
       const Ion q = load_ion(ions, ip);
-      uint32_t h0, h1;
-      hash32(q.c, q.ox, q.oy, q.oz, q.vx, q.vy, q.vz, h0, h1);
-      sample = accept_sample<float>(k, h0, h1, q.vx, q.vy, q.vz);
+      sample = accept_sample<float>(k, (uint32_t)q.id, kIdTag, q.vx, q.vy, q.vz);
     }
     flush_samples(st, sample, active);
   }
@@ -1548,6 +1655,11 @@ void ecs_part_xfer_free(EcsCtx *ctx) {
     if (ctx->xs[q]) cudaStreamDestroy(ctx->xs[q]);
   }
   if (ctx->xev_ready) cudaEventDestroy(ctx->xev_ready);
+  for (int q = 0; q < 2; q++) {
+    if (ctx->stage_dn[q]) cudaFree(ctx->stage_dn[q]);
+    if (ctx->xev_dn_conv[q]) cudaEventDestroy(ctx->xev_dn_conv[q]);
+    if (ctx->xev_dn_copy[q]) cudaEventDestroy(ctx->xev_dn_copy[q]);
+  }
 }
 
 // Host AoS FP64 -> device: copies on xs[1], conversions on ctx->stream.
@@ -1582,6 +1694,7 @@ int ecs_part_upload(EcsCtx *ctx, const double *pos, const double *vel, int64_t n
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
   }
   ctx->np = np;
+  ctx->pgen++;
   ctx->attempt_rate = -1.0;
   ctx->tiles_valid = false;
   ctx->perm_pending = false;
@@ -1653,6 +1766,7 @@ int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDen
   if (ctx->hstat->flags & ECS_FLAG_RANGE)
     return ecs_fail(ctx, ECS_ERR_RANGE, "rejection sampling gave up after %d attempts for an ion", kInitTries);
   ctx->np = np;
+  ctx->pgen++;
   ctx->attempt_rate = -1.0;
   ctx->tiles_valid = false;
   ctx->perm_pending = false;
@@ -1668,6 +1782,7 @@ int ecs_part_init(EcsCtx *ctx, int dist, int64_t np, uint64_t seed, const EcsDen
 // host transfers and the order-free kernel need the records themselves).
 static int settle_order(EcsCtx *ctx) {
   if (!ctx->perm_pending) return ECS_OK;
+  ctx->pgen++;
   if (ctx->np > 0) {
     k_gather_ions<<<grid_blocks(ctx, ctx->np, 8), kBlock, 0, ctx->stream>>>(ctx->np, ctx->perm, ctx->ions[ctx->cur],
                                                                           ctx->ions[1 - ctx->cur]);
@@ -1746,22 +1861,35 @@ int ecs_part_ids(EcsCtx *ctx, int32_t *ids) {
   return ECS_OK;
 }
 
-// One pass of the particle kernel over all ions.  With `count_for_sort` the
-// pass also counts the ions' (new) cells for the counting sort that follows.
-static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sort = false) {
-  if (ctx->np == 0) return ECS_OK;
-  PartK k = make_k(ctx, dt);
+// Parameters of one particle pass in `mode` (the collision bit dropped when
+// mn = 0).  The collision attempt rate is estimated from the ions' state at
+// the start of the first pass that pushes or collides, so that a step run as
+// separate push and collide passes (the reference's UpdateVelocities) and
+// the same step as one fused pass start from the same rate.
+static int pass_params(EcsCtx *ctx, double dt, int &mode, PartK &k) {
+  k = make_k(ctx, dt);
+  if ((mode & 3) && k.collide && ctx->attempt_rate < 0) {
+    int rc = ecs_part_estimate_rate(ctx, dt);
+    if (rc) return rc;
+  }
   if ((mode & 2) && k.collide) {
-    if (ctx->attempt_rate < 0) {
-      int rc = ecs_part_estimate_rate(ctx, dt);
-      if (rc) return rc;
-    }
     k.rate = ctx->attempt_rate;
     k.ratef = (float)k.rate;
     k.p0f = (float)exp(-k.rate);
     ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   }
   if (!k.collide) mode &= ~2;
+  return ECS_OK;
+}
+
+// One pass of the particle kernel over all ions.  With `count_for_sort` the
+// pass also counts the ions' (new) cells for the counting sort that follows.
+static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sort = false) {
+  if (ctx->np == 0) return ECS_OK;
+  PartK k;
+  int rc = pass_params(ctx, dt, mode, k);
+  if (rc) return rc;
+  ctx->pgen++;
   const size_t shm = (size_t)(kBlock / 32) * 32 * kTileStride * sizeof(long long);
   static std::atomic<bool> attr_set{false};
   if (!attr_set) {
@@ -1787,13 +1915,14 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
     float4 *src = ctx->ions[ctx->cur];
     float4 *dst = gather ? ctx->ions[1 - ctx->cur] : src;
     k_tiles32<<<ntiles, kBlock, 0, ctx->stream>>>(k, mode, src, dst, gather ? ctx->perm : nullptr, ctx->eext32,
-                                                  ctx->acc, ctx->sort_offset, count, ctx->sort_keys, ctx->dstat);
+                                                  ctx->acc, ctx->sort_offset, count, ctx->sort_keys, ctx->dstat, 0,
+                                                  ntiles);
     if (gather && writes) {
       ctx->cur = 1 - ctx->cur;
       ctx->perm_pending = false;
     }
   } else {
-    int rc = settle_order(ctx);
+    rc = settle_order(ctx);
     if (rc) return rc;
     k_particles32<<<g, kBlock, shm, ctx->stream>>>(k, mode, ctx->np, ctx->ions[ctx->cur], ctx->eext32, ctx->acc,
                                                 count, ctx->sort_keys, ctx->dstat);
@@ -1884,6 +2013,8 @@ static int sort_counted(EcsCtx *ctx) {
   ctx->perm_pending = true;
   ctx->steps_since_sort = 0;
   ctx->tiles_valid = true;
+  ctx->bounds_valid = false;
+  ctx->pgen++;
   return ECS_OK;
 }
 
@@ -1925,6 +2056,136 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
   if ((rc = sort_after_pass(ctx, counted))) return rc;
   if (sorted) *sorted = counted ? 1 : 0;
   if (collide) {
+    rc = finish_collisions(ctx, dt);
+    ctx->step_index++;
+  }
+  return rc;
+}
+
+// ---- the particle pass of ecs_step_host, pipelined with the host copies ---------
+// When the host arrays hold the ions as the previous ecs_step_host call
+// returned them (the generation count has not moved since), the records
+// they become are already in tile order, so the upload, the fused pass and
+// the download run chunk by chunk over ranges of whole tiles: the copy in
+// of one chunk overlaps the pass and the copy out of the one before it
+// (copies in on xs[1], copies out on xs[0], kernels on the context's
+// stream).  When the pass counts cells for a sort, the download waits for
+// the sort and returns the ions in the new key order, read through the
+// permutation (conversions on xs[0], copies on xs[1], beside the field phase
+// that follows); the next call's upload then puts them in the buffer in that
+// order.  The identities become the host indices, as in an upload.
+int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, int *sorted) {
+  if (ctx->prec != ECS_PREC_MIXED || ctx->p.ndim != 3 || np != ctx->np || np == 0 || !ctx->tiles_valid ||
+      ctx->host_gen != ctx->pgen)
+    return ECS_ERR_STATE;
+  int rc = ensure_xfer(ctx);
+  if (rc) return rc;
+  const int64_t chunk = ctx->stage_n;
+  const int ntiles = ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2];
+  if (!ctx->bounds_valid) {
+    ctx->tile_bounds.resize((size_t)ntiles + 1);
+    int32_t *d = nullptr;
+    ECS_CUDA(ctx, cudaMallocAsync((void **)&d, ((size_t)ntiles + 1) * sizeof(int32_t), ctx->stream));
+    k_tile_bounds<<<ecs_div_up((size_t)ntiles + 1, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, d);
+    ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_bounds.data(), d, ((size_t)ntiles + 1) * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    ECS_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
+    ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->bounds_valid = true;
+  }
+  const int32_t *tb = ctx->tile_bounds.data();
+  if (tb[ntiles] != np) return ECS_ERR_STATE;
+  for (int t = 0; t < ntiles; t++)
+    if (tb[t + 1] - tb[t] > chunk) return ECS_ERR_STATE;  // a tile larger than a staging chunk
+  if (!ctx->stage_dn[0]) {
+    for (int q = 0; q < 2; q++) {
+      ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage_dn[q], (size_t)chunk * 6 * sizeof(double)));
+      ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_conv[q], cudaEventDisableTiming));
+      ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_copy[q], cudaEventDisableTiming));
+    }
+  }
+  const int collide = ctx->p.mn > 0.0;
+  int mode = 1 | (collide ? 2 : 0) | 4 | 8;
+  PartK k;
+  if ((rc = pass_params(ctx, dt, mode, k))) return rc;
+  const bool counted = sort_due(ctx);
+  if ((rc = ecs_grid_clear_acc(ctx))) return rc;
+  if (counted) ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
+  int32_t *count = counted ? ctx->sort_count : nullptr;
+  const int nd = 3;
+  ctx->perm_pending = false;  // the buffer takes the host's order
+  ctx->pgen++;
+  float4 *ions = ctx->ions[ctx->cur];
+  ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));  // earlier work on the buffers
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_ready, 0));
+  if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
+  int64_t c = 0;
+  for (int t0 = 0; t0 < ntiles;) {
+    int t1 = t0 + 1;
+    while (t1 < ntiles && (int64_t)tb[t1 + 1] - tb[t0] <= chunk) t1++;
+    const int64_t A = tb[t0], n = (int64_t)tb[t1] - A;
+    const int q = (int)(c & 1);
+    double *in = ctx->stage[q], *out = ctx->stage_dn[q];
+    if (n > 0) {
+      if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));  // staging in free
+      ECS_CUDA(ctx, cudaMemcpyAsync(in, pos + nd * A, (size_t)n * nd * sizeof(double), cudaMemcpyHostToDevice,
+                                    ctx->xs[1]));
+      ECS_CUDA(ctx, cudaMemcpyAsync(in + nd * n, vel + nd * A, (size_t)n * nd * sizeof(double),
+                                    cudaMemcpyHostToDevice, ctx->xs[1]));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_copy[q], 0));
+      k_aos_to_mixed<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->stream>>>(n, nd, k, in, in + nd * n, ions + 2 * A, A);
+      ECS_LAUNCHED(ctx);
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
+    }
+    k_tiles32<<<t1 - t0, kBlock, 0, ctx->stream>>>(k, mode, ions, ions, nullptr, ctx->eext32, ctx->acc,
+                                                    ctx->sort_offset, count, ctx->sort_keys, ctx->dstat, t0, t1);
+    ECS_LAUNCHED(ctx);
+    if (n > 0 && !counted) {
+      if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_dn_copy[q], 0));  // staging out free
+      k_mixed_to_aos<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->stream>>>(n, nd, k, out, out + nd * n, ions + 2 * A);
+      ECS_LAUNCHED(ctx);
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[q], ctx->stream));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[q], 0));
+      ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * A, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->xs[0]));
+      ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * A, out + nd * n, (size_t)n * nd * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->xs[0]));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[q], ctx->xs[0]));
+    }
+    if (n > 0) c++;
+    t0 = t1;
+  }
+  if (ctx->ev[1]) {
+    cudaEventRecord(ctx->ev[1], ctx->stream);
+    ctx->ev_particle = true;
+  }
+  if ((rc = sort_after_pass(ctx, counted))) return rc;
+  if (counted) {  // the ions in the new key order, read through the permutation
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
+    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
+    int64_t c2 = 0;
+    for (int64_t off = 0; off < np; off += chunk, c2++) {
+      const int q = (int)(c2 & 1);
+      const int64_t n = np - off < chunk ? np - off : chunk;
+      double *out = ctx->stage_dn[q];
+      if (c2 >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_copy[q], 0));
+      k_mixed_to_aos_perm<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs[0]>>>(n, nd, k, out, out + nd * n, ions,
+                                                                              ctx->perm + off);
+      ECS_LAUNCHED(ctx);
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[q], ctx->xs[0]));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_dn_conv[q], 0));
+      ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * off, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->xs[1]));
+      ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * off, out + nd * n, (size_t)n * nd * sizeof(double),
+                                    cudaMemcpyDeviceToHost, ctx->xs[1]));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[q], ctx->xs[1]));
+    }
+  }
+  if (sorted) *sorted = counted ? 1 : 0;
+  if (mode & 2) {
     rc = finish_collisions(ctx, dt);
     ctx->step_index++;
   }

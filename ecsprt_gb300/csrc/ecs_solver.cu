@@ -62,6 +62,7 @@ struct KrylovDev {
 template <typename T>
 __global__ void k_apply(OpK o, const T *__restrict__ n, const T *__restrict__ x, const T *__restrict__ b,
                         T *__restrict__ y, int mode) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const Nbr q = nbr_of(o.g, i, j, k);
@@ -104,6 +105,7 @@ static inline int seg_len(int N) {
 template <typename T>
 __global__ void k_zline_rows(OpK o, const T *__restrict__ n, T *__restrict__ lo, T *__restrict__ up,
                              T *__restrict__ dg) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const Nbr q = nbr_of(o.g, i, j, k);
@@ -120,6 +122,7 @@ __global__ void k_zline_rows(OpK o, const T *__restrict__ n, T *__restrict__ lo,
 template <typename T>
 __global__ void k_zline_setup(GridG g, const T *__restrict__ lo, const T *__restrict__ up,
                               const T *__restrict__ dg, ZlP<T> z, int S) {
+  ECS_PDL_ENTRY();
   const int ncol = g.nx * g.ny;
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
@@ -210,6 +213,7 @@ __global__ void k_zline_setup(GridG g, const T *__restrict__ lo, const T *__rest
 template <typename T>
 __global__ void k_zline_rhs(OpK o, const T *__restrict__ n, const T *__restrict__ b, const T *__restrict__ xo,
                             T *__restrict__ r) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const Nbr q = nbr_of(o.g, i, j, k);
@@ -234,6 +238,7 @@ template <typename T, int S>
 __global__ void __launch_bounds__(32 * kMaxSeg) k_zline_seg(GridG g, ZlP<T> z, const T *__restrict__ r,
                                                             const T *__restrict__ xo, T *__restrict__ xn,
                                                             T omega) {
+  ECS_PDL_ENTRY();
   __shared__ T sA[kMaxSeg][33], sB[kMaxSeg][33], sIn[kMaxSeg][33];
   __shared__ T sLast[32], sS[32];
   const int tx = threadIdx.x, p = threadIdx.y, P = blockDim.y;
@@ -333,6 +338,7 @@ __global__ void __launch_bounds__(32 * kMaxSeg) k_zline_seg(GridG g, ZlP<T> z, c
 // 27 fine cells through the neighbour offsets of the fine cell (2I, 2J, 2K).
 template <typename T>
 __global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
+  ECS_PDL_ENTRY();
   int I, J, K;
   if (!at3(gc.nx, gc.ny, I, J, K)) return;
   const Nbr q = nbr_of(gf, 2 * I, 2 * J, 2 * K);
@@ -394,6 +400,7 @@ __device__ __forceinline__ T prolong_at(const GridG &gc, const T *__restrict__ c
 // added only for an odd index, in the order of prolong_at.
 template <typename T>
 __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__restrict__ f) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(gf.nx, gf.ny, i, j, k)) return;
   const Nbr q = nbr_of(gc, i >> 1, j >> 1, k >> 1);
@@ -513,6 +520,7 @@ __device__ __noinline__ void blk_sweep(const SmallLevel<T> &L, T *sm, const T *b
 template <typename T>
 __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc, const T *__restrict__ b_in,
                                                                 T *__restrict__ x_out, int coarse_sweeps, T omega) {
+  ECS_PDL_ENTRY();
   extern __shared__ unsigned char small_smem[];
   T *sm = reinterpret_cast<T *>(small_smem);
   const int nl = sc.nl;
@@ -630,6 +638,7 @@ constexpr int kInvThreads = 1024;
 template <typename T>
 __global__ void __launch_bounds__(kInvThreads) k_coarse_inverse(OpK o, const T *__restrict__ dens, int regularize,
                                                          T *__restrict__ Mg, T *__restrict__ invT) {
+  ECS_PDL_ENTRY();
   extern __shared__ unsigned char inv_smem[];
   T *M = Mg ? Mg : reinterpret_cast<T *>(inv_smem);  // work matrix in shared memory when it fits
   __shared__ T fac[kDirectMax];
@@ -732,6 +741,7 @@ constexpr int kRegCols = 2 * kRegInvMax * kRegInvMax / kInvThreads;  // 8 column
 template <typename T>
 __global__ void __launch_bounds__(kInvThreads) k_coarse_inverse_reg(OpK o, const T *__restrict__ dens,
                                                                     int regularize, T *__restrict__ invT) {
+  ECS_PDL_ENTRY();
   __shared__ T colbuf[2][kRegInvMax];
   __shared__ T prow[2][2 * kRegInvMax];
   __shared__ int rowpos[kRegInvMax];
@@ -986,12 +996,14 @@ __device__ __forceinline__ void slot_totals(const double *partial, int ns, int n
 // x64 += a * e (e in T)
 template <typename T>
 __global__ void k_axpy64(size_t n, double a, const T *__restrict__ e, double *__restrict__ x) {
+  ECS_PDL_ENTRY();
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     x[q] += a * (double)e[q];
 }
 // d = s * scale[0] in the precision of d (the FP64 residual, normalised, to T)
 template <typename T>
 __global__ void k_scale_to(size_t n, const double *__restrict__ s, const double *__restrict__ scale, T *__restrict__ d) {
+  ECS_PDL_ENTRY();
   const T a = (T)scale[0];
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     d[q] = (T)s[q] * a;
@@ -999,6 +1011,7 @@ __global__ void k_scale_to(size_t n, const double *__restrict__ s, const double 
 // v -= value[0]
 template <typename T>
 __global__ void k_sub_value(size_t n, T *__restrict__ v, const double *__restrict__ value) {
+  ECS_PDL_ENTRY();
   const double m = value[0];
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
     v[e] = (T)((double)v[e] - m);
@@ -1034,6 +1047,7 @@ __device__ __forceinline__ void block_chunk(const KSum<T> (&acc)[kChunk], int v0
 template <typename T, int W>
 __global__ void __launch_bounds__(kB, 4) k_dots1(size_t n, const T *__restrict__ V, KrylovDev *__restrict__ kd,
                                                  double *__restrict__ partial) {
+  ECS_PDL_ENTRY();
   const int nv = kd->j + 1;
   const T *w = V + (size_t)nv * n;
   const size_t nw = n / W, stride = (size_t)gridDim.x * blockDim.x;
@@ -1113,6 +1127,7 @@ template <typename T, int W>
 __global__ void __launch_bounds__(kB, 4) k_orth1_dots2(size_t n, T *__restrict__ V, KrylovDev *__restrict__ kd,
                                                        double *__restrict__ partial, cudaGraphConditionalHandle cond,
                                                        int use_graph) {
+  ECS_PDL_ENTRY();
   __shared__ T h[kSlots];
   const int nv = kd->j + 1, nslot = nv + 1;
   if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h1[threadIdx.x] : T(0);
@@ -1155,6 +1170,7 @@ __global__ void __launch_bounds__(kB, 4) k_orth1_dots2(size_t n, T *__restrict__
 // preconditioner input vin (j = the step that just finished).
 template <typename T, int W>
 __global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__restrict__ kd, T *__restrict__ vin) {
+  ECS_PDL_ENTRY();
   __shared__ T h[kSlots + 1];
   const int j = kd->jprev, nv = j + 1;
   if (threadIdx.x < kSlots) h[threadIdx.x] = (int)threadIdx.x < nv ? (T)kd->h2[threadIdx.x] : T(0);
@@ -1184,6 +1200,7 @@ __global__ void k_orth2_scale(size_t n, T *__restrict__ V, const KrylovDev *__re
 template <typename T>
 __global__ void k_apply_dyn(OpK o, const T *__restrict__ n, const T *__restrict__ x, const double *__restrict__ mean,
                             T *__restrict__ Z, T *__restrict__ V, const KrylovDev *__restrict__ kd) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const int jj = kd->j;
@@ -1211,6 +1228,7 @@ template <typename T, int W, int M>
 __global__ void __launch_bounds__(kB) k_reduce(size_t nw, const T *__restrict__ v, double *__restrict__ partial,
                                                double div, double *out, KrylovDev *kd,
                                                cudaGraphConditionalHandle cond, int use_graph) {
+  ECS_PDL_ENTRY();
   KSum<T> acc;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += (size_t)gridDim.x * blockDim.x) {
     const Pack<T, W> p = ld_pack<T, W>(v + e * W);
@@ -1245,6 +1263,7 @@ __global__ void __launch_bounds__(kB) k_reduce(size_t nw, const T *__restrict__ 
 template <typename T>
 __global__ void k_cycle_start(size_t n, const T *__restrict__ b, T *__restrict__ V, T *__restrict__ vin,
                               T *__restrict__ x, const KrylovDev *__restrict__ kd) {
+  ECS_PDL_ENTRY();
   const T sc = (T)kd->inv_scale;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const T v = b[e] * sc;
@@ -1256,6 +1275,7 @@ __global__ void k_cycle_start(size_t n, const T *__restrict__ b, T *__restrict__
 
 // y = H^-1 g (upper triangular, nits x nits)
 __global__ void k_cycle_solve(KrylovDev *kd) {
+  ECS_PDL_ENTRY();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int m = kKrylovMax, nj = kd->nits;
   for (int q = nj - 1; q >= 0; q--) {
@@ -1268,6 +1288,7 @@ __global__ void k_cycle_solve(KrylovDev *kd) {
 // x += sum_q y[q] Z_q
 template <typename T>
 __global__ void k_cycle_combine(size_t n, const T *__restrict__ Z, const KrylovDev *__restrict__ kd, T *__restrict__ x) {
+  ECS_PDL_ENTRY();
   __shared__ T y[kKrylovMax];
   const int nj = kd->nits;
   if (threadIdx.x < kKrylovMax) y[threadIdx.x] = (int)threadIdx.x < nj ? (T)kd->y[threadIdx.x] : T(0);
@@ -1304,9 +1325,9 @@ int launch_reduce(EcsCtx *ctx, size_t n, const T *v, double div, double *out, cu
   KrylovDev *kd = (KrylovDev *)ctx->kdev;
   constexpr int W = kPack<T>;
   if (packed4(n))
-    k_reduce<T, W, M><<<dot_blocks(ctx, n / W), kB, 0, ctx->stream>>>(n / W, v, ctx->red, div, out, kd, cond, use_graph);
+    ecs_launch_pdl(k_reduce<T, W, M>, dot_blocks(ctx, n / W), kB, 0, ctx->stream, n / W, v, ctx->red, div, out, kd, cond, use_graph);
   else
-    k_reduce<T, 1, M><<<dot_blocks(ctx, n), kB, 0, ctx->stream>>>(n, v, ctx->red, div, out, kd, cond, use_graph);
+    ecs_launch_pdl(k_reduce<T, 1, M>, dot_blocks(ctx, n), kB, 0, ctx->stream, n, v, ctx->red, div, out, kd, cond, use_graph);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1385,6 +1406,7 @@ constexpr T kOmega() { return T(0.8); }
 // weighting) and the z-line factorisation of every level.
 template <typename T>
 __global__ void k_density_in(size_t n, const double *__restrict__ mom, T *__restrict__ d) {
+  ECS_PDL_ENTRY();
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
     d[e] = (T)mom[e];
 }
@@ -1402,9 +1424,9 @@ template <typename T>
 int zline_factor(EcsCtx *ctx, MgLevel<T> &L, cudaStream_t s) {
   const int ncol = L.nx * L.ny;
   const OpK o = op_level(ctx, L);
-  k_zline_rows<T><<<blocks3(o.g), threads3(), 0, s>>>(o, L.dens, L.x, L.b, L.r);  // x, b, r are free here
+  ecs_launch_pdl(k_zline_rows<T>, blocks3(o.g), threads3(), 0, s, o, L.dens, L.x, L.b, L.r);  // x, b, r are free here
   ECS_LAUNCHED(ctx);
-  k_zline_setup<T><<<ecs_div_up(ncol, kColBlock), kColBlock, 0, s>>>(o.g, L.x, L.b, L.r, zl_of(L), seg_len<T>(L.nz));
+  ecs_launch_pdl(k_zline_setup<T>, ecs_div_up(ncol, kColBlock), kColBlock, 0, s, o.g, L.x, L.b, L.r, zl_of(L), seg_len<T>(L.nz));
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1425,13 +1447,13 @@ int mg_setup(EcsCtx *ctx) {
   Multigrid<T> &mg = mg_of<T>(ctx);
   cudaStream_t s0 = ctx->stream, sa = ctx->sst[0], sb = ctx->sst[1];
   MgLevel<T> &L0 = mg.lv[0];
-  k_density_in<T><<<blocks_for(ctx, L0.n), kB, 0, s0>>>(L0.n, op_density(ctx), L0.dens);
+  ecs_launch_pdl(k_density_in<T>, blocks_for(ctx, L0.n), kB, 0, s0, L0.n, op_density(ctx), L0.dens);
   ECS_LAUNCHED(ctx);
   ECS_CUDA(ctx, cudaEventRecord(ctx->sev[0], s0));
   ECS_CUDA(ctx, cudaStreamWaitEvent(sa, ctx->sev[0], 0));
   for (size_t l = 1; l < mg.lv.size(); l++) {
     MgLevel<T> &F = mg.lv[l - 1], &C = mg.lv[l];
-    k_restrict<T><<<blocks3(C.nx, C.ny, C.nz), threads3(), 0, sa>>>(
+    ecs_launch_pdl(k_restrict<T>, blocks3(C.nx, C.ny, C.nz), threads3(), 0, sa, 
         grid_level(ctx, F.nx, F.ny, F.nz), grid_level(ctx, C.nx, C.ny, C.nz), F.dens, C.dens);
     ECS_LAUNCHED(ctx);
   }
@@ -1450,10 +1472,10 @@ int mg_setup(EcsCtx *ctx) {
       attr_set[sizeof(T) == 8] = true;
     }
     if (C.n <= (size_t)kRegInvMax)
-      k_coarse_inverse_reg<T><<<1, kInvThreads, 0, sa>>>(op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0,
+      ecs_launch_pdl(k_coarse_inverse_reg<T>, 1, kInvThreads, 0, sa, op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0,
                                                           mg.cinv);
     else
-      k_coarse_inverse<T><<<1, kInvThreads, in_smem ? bytes : 0, sa>>>(
+      ecs_launch_pdl(k_coarse_inverse<T>, 1, kInvThreads, in_smem ? bytes : 0, sa, 
           op_level(ctx, C), C.dens, fully_periodic(ctx) ? 1 : 0, in_smem ? nullptr : mg.cwork, mg.cinv);
     ECS_LAUNCHED(ctx);
   }
@@ -1469,7 +1491,7 @@ int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
   const OpK o = op_level(ctx, L);
   const T *r = b;
   if (xo) {
-    k_zline_rhs<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, b, xo, L.r);
+    ecs_launch_pdl(k_zline_rhs<T>, blocks3(o.g), threads3(), 0, ctx->stream, o, L.dens, b, xo, L.r);
     ECS_LAUNCHED(ctx);
     r = L.r;
   }
@@ -1477,13 +1499,13 @@ int sweep(EcsCtx *ctx, MgLevel<T> &L, const T *b, const T *xo, T *xn) {
   const dim3 grid((unsigned)((L.nx + 31) / 32), (unsigned)L.ny);
   const dim3 block(32, (unsigned)((L.nz + S - 1) / S));
   if (S == 8)
-    k_zline_seg<T, 8><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+    ecs_launch_pdl(k_zline_seg<T, 8>, grid, block, 0, ctx->stream, o.g, zl_of(L), r, xo, xn, kOmega<T>());
   else if (S == 16)
-    k_zline_seg<T, 16><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+    ecs_launch_pdl(k_zline_seg<T, 16>, grid, block, 0, ctx->stream, o.g, zl_of(L), r, xo, xn, kOmega<T>());
   else if (S == 32)
-    k_zline_seg<T, 32><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+    ecs_launch_pdl(k_zline_seg<T, 32>, grid, block, 0, ctx->stream, o.g, zl_of(L), r, xo, xn, kOmega<T>());
   else
-    k_zline_seg<T, 64><<<grid, block, 0, ctx->stream>>>(o.g, zl_of(L), r, xo, xn, kOmega<T>());
+    ecs_launch_pdl(k_zline_seg<T, 64>, grid, block, 0, ctx->stream, o.g, zl_of(L), r, xo, xn, kOmega<T>());
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1534,7 +1556,7 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
       ECS_CUDA(ctx, cudaFuncSetAttribute(k_vcycle_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmem));
       attr_set[sizeof(T) == 8] = true;
     }
-    k_vcycle_small<T><<<1, kSmallThreads, bytes, ctx->stream>>>(sc, b, xout, kCoarseSweeps, kOmega<T>());
+    ecs_launch_pdl(k_vcycle_small<T>, 1, kSmallThreads, bytes, ctx->stream, sc, b, xout, kCoarseSweeps, kOmega<T>());
     ECS_LAUNCHED(ctx);
     return ECS_OK;
   }
@@ -1549,13 +1571,13 @@ int vcycle(EcsCtx *ctx, size_t l, const T *b, T *xout) {
   MgLevel<T> &C = mg.lv[l + 1];
   const OpK o = op_level(ctx, L);
   if ((rc = sweep<T>(ctx, L, b, nullptr, L.t))) return rc;
-  k_apply<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o, L.dens, L.t, b, L.r, 1);
+  ecs_launch_pdl(k_apply<T>, blocks3(o.g), threads3(), 0, ctx->stream, o, L.dens, L.t, b, L.r, 1);
   ECS_LAUNCHED(ctx);
   const GridG gc = grid_level(ctx, C.nx, C.ny, C.nz);
-  k_restrict<T><<<blocks3(gc), threads3(), 0, ctx->stream>>>(o.g, gc, L.r, C.b);
+  ecs_launch_pdl(k_restrict<T>, blocks3(gc), threads3(), 0, ctx->stream, o.g, gc, L.r, C.b);
   ECS_LAUNCHED(ctx);
   if ((rc = vcycle<T>(ctx, l + 1, C.b, C.x))) return rc;
-  k_prolong_add<T><<<blocks3(o.g), threads3(), 0, ctx->stream>>>(o.g, gc, C.x, L.t);
+  ecs_launch_pdl(k_prolong_add<T>, blocks3(o.g), threads3(), 0, ctx->stream, o.g, gc, C.x, L.t);
   ECS_LAUNCHED(ctx);
   return sweep<T>(ctx, L, b, L.t, xout);
 }
@@ -1595,7 +1617,7 @@ int cycle_pre(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
   const T *b = cycle_b<T>(ctx);
   int rc = launch_reduce<T, kRedBeta>(ctx, n, b, 1.0, nullptr, cond, use_graph);
   if (rc) return rc;
-  k_cycle_start<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, b, basis_v<T>(ctx), mg.lv[0].b, cycle_x<T>(ctx), kd);
+  ecs_launch_pdl(k_cycle_start<T>, blocks_for(ctx, n), kB, 0, ctx->stream, n, b, basis_v<T>(ctx), mg.lv[0].b, cycle_x<T>(ctx), kd);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1617,28 +1639,28 @@ int cycle_step(EcsCtx *ctx, cudaGraphConditionalHandle cond, int use_graph) {
     if ((rc = launch_reduce<T, kRedMean>(ctx, n, L0.x, (double)n, &kd->mean, cond, use_graph))) return rc;
     mean = &kd->mean;
   }
-  k_apply_dyn<T><<<blocks3(o0.g), threads3(), 0, ctx->stream>>>(o0, L0.dens, L0.x, mean, Z, V, kd);
+  ecs_launch_pdl(k_apply_dyn<T>, blocks3(o0.g), threads3(), 0, ctx->stream, o0, L0.dens, L0.x, mean, Z, V, kd);
   ECS_LAUNCHED(ctx);
   // classical Gram-Schmidt, two passes (the second ends with the Arnoldi
   // bookkeeping)
   constexpr int W = kPack<T>;
   if (packed4(n)) {
     const unsigned nb = dot_blocks(ctx, n / W);
-    k_dots1<T, W><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+    ecs_launch_pdl(k_dots1<T, W>, nb, kB, 0, ctx->stream, n, V, kd, ctx->red);
     ECS_LAUNCHED(ctx);
-    k_orth1_dots2<T, W><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red, cond, use_graph);
+    ecs_launch_pdl(k_orth1_dots2<T, W>, nb, kB, 0, ctx->stream, n, V, kd, ctx->red, cond, use_graph);
     ECS_LAUNCHED(ctx);
   } else {
     const unsigned nb = dot_blocks(ctx, n);
-    k_dots1<T, 1><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red);
+    ecs_launch_pdl(k_dots1<T, 1>, nb, kB, 0, ctx->stream, n, V, kd, ctx->red);
     ECS_LAUNCHED(ctx);
-    k_orth1_dots2<T, 1><<<nb, kB, 0, ctx->stream>>>(n, V, kd, ctx->red, cond, use_graph);
+    ecs_launch_pdl(k_orth1_dots2<T, 1>, nb, kB, 0, ctx->stream, n, V, kd, ctx->red, cond, use_graph);
     ECS_LAUNCHED(ctx);
   }
   if (packed4(n))
-    k_orth2_scale<T, W><<<blocks_for(ctx, n / W), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
+    ecs_launch_pdl(k_orth2_scale<T, W>, blocks_for(ctx, n / W), kB, 0, ctx->stream, n, V, kd, L0.b);
   else
-    k_orth2_scale<T, 1><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, V, kd, L0.b);
+    ecs_launch_pdl(k_orth2_scale<T, 1>, blocks_for(ctx, n), kB, 0, ctx->stream, n, V, kd, L0.b);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1648,9 +1670,9 @@ template <typename T>
 int cycle_post(EcsCtx *ctx) {
   const size_t n = ctx->ncell;
   KrylovDev *kd = (KrylovDev *)ctx->kdev;
-  k_cycle_solve<<<1, 32, 0, ctx->stream>>>(kd);
+  ecs_launch_pdl(k_cycle_solve, 1, 32, 0, ctx->stream, kd);
   ECS_LAUNCHED(ctx);
-  k_cycle_combine<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, basis_z<T>(ctx), kd, cycle_x<T>(ctx));
+  ecs_launch_pdl(k_cycle_combine<T>, blocks_for(ctx, n), kB, 0, ctx->stream, n, basis_z<T>(ctx), kd, cycle_x<T>(ctx));
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1690,7 +1712,7 @@ int project_mean(EcsCtx *ctx, T *v) {
   size_t n = ctx->ncell;
   int rc = launch_reduce<T, kRedMean>(ctx, n, v, (double)n, ctx->dots + 2, 0, 0);
   if (rc) return rc;
-  k_sub_value<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, v, ctx->dots + 2);
+  ecs_launch_pdl(k_sub_value<T>, blocks_for(ctx, n), kB, 0, ctx->stream, n, v, ctx->dots + 2);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1705,6 +1727,7 @@ struct RefineDev {
 };
 
 __global__ void k_solve_init(RefineDev *rd, const double *__restrict__ dots) {
+  ECS_PDL_ENTRY();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   rd->bnorm = dots[0];
   rd->rel = 0.0;
@@ -1723,6 +1746,7 @@ constexpr int kMaxSweeps = 64;
 // the FGMRES tolerance and step limit of that correction.
 __global__ void k_refine_check(RefineDev *rd, KrylovDev *kd, const double *__restrict__ dots, double rtol,
                                int max_it, double tol_floor, cudaGraphConditionalHandle cond) {
+  ECS_PDL_ENTRY();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (rd->bnorm > 0.0) {
     const double rel = dots[0] / rd->bnorm;
@@ -1741,6 +1765,7 @@ __global__ void k_refine_check(RefineDev *rd, KrylovDev *kd, const double *__res
 }
 
 __global__ void k_refine_update(RefineDev *rd, const KrylovDev *__restrict__ kd) {
+  ECS_PDL_ENTRY();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   rd->its += kd->nits;
   rd->sweeps += 1;
@@ -1750,6 +1775,7 @@ __global__ void k_refine_update(RefineDev *rd, const KrylovDev *__restrict__ kd)
 // x64 += scale[0] * e (scale nullptr: 1)
 template <typename T>
 __global__ void k_axpy64_dev(size_t n, const double *__restrict__ scale, const T *__restrict__ e, double *__restrict__ x) {
+  ECS_PDL_ENTRY();
   const double a = scale ? scale[0] : 1.0;
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     x[q] += a * (double)e[q];
@@ -1758,6 +1784,7 @@ __global__ void k_axpy64_dev(size_t n, const double *__restrict__ scale, const T
 // Mixed-precision residual: r64 = b64 - A64(n64) x64.
 __global__ void k_residual64(OpK o, const double *__restrict__ n, const double *__restrict__ x,
                              const double *__restrict__ b, double *__restrict__ r) {
+  ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const Nbr q = nbr_of(o.g, i, j, k);
@@ -1826,7 +1853,7 @@ int capture_graph(EcsCtx *ctx, cudaStream_t s, cudaGraph_t *g) {
 template <typename T>
 int refine_decide(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
   const double tol_floor = sizeof(T) == 4 ? 2e-6 : 0.0;
-  k_refine_check<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, (KrylovDev *)ctx->kdev, ctx->dots, rtol, max_it,
+  ecs_launch_pdl(k_refine_check, 1, 32, 0, ctx->stream, (RefineDev *)ctx->rdev, (KrylovDev *)ctx->kdev, ctx->dots, rtol, max_it,
                                             tol_floor, h);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
@@ -1838,7 +1865,7 @@ template <typename T>
 int refine_check(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
   const EcsParams &p = ctx->p;
   const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
-  k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
+  ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
   ECS_LAUNCHED(ctx);
   int rc = norm64_dev(ctx, ctx->r64, ctx->dots);
   if (rc) return rc;
@@ -1852,7 +1879,7 @@ int refine_correct(EcsCtx *ctx, int lvl) {
   const size_t n = ctx->ncell;
   int rc;
   if (sizeof(T) == 4) {  // the normalised FP64 residual to FP32
-    k_scale_to<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, ctx->r64, ctx->dots + 1, (float *)cycle_b<T>(ctx));
+    ecs_launch_pdl(k_scale_to<float>, blocks_for(ctx, n), kB, 0, ctx->stream, n, ctx->r64, ctx->dots + 1, (float *)cycle_b<T>(ctx));
     ECS_LAUNCHED(ctx);
   }
   cudaGraph_t g = nullptr, body = nullptr;
@@ -1872,11 +1899,11 @@ int refine_correct(EcsCtx *ctx, int lvl) {
   if (rc) return rc;
   ECS_CUDA(ctx, ce);
   if ((rc = cycle_post<T>(ctx))) return rc;
-  k_axpy64_dev<T><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, sizeof(T) == 4 ? ctx->dots : nullptr,
+  ecs_launch_pdl(k_axpy64_dev<T>, blocks_for(ctx, n), kB, 0, ctx->stream, n, sizeof(T) == 4 ? ctx->dots : nullptr,
                                                              cycle_x<T>(ctx), ctx->phi);
   ECS_LAUNCHED(ctx);
   if ((rc = project_mean<double>(ctx, ctx->phi))) return rc;
-  k_refine_update<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, (const KrylovDev *)ctx->kdev);
+  ecs_launch_pdl(k_refine_update, 1, 32, 0, ctx->stream, (RefineDev *)ctx->rdev, (const KrylovDev *)ctx->kdev);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
@@ -1897,7 +1924,7 @@ int capture_solve(EcsCtx *ctx, double rtol, int max_it, int warm) {
   cudaGraph_t top = nullptr;
   if ((rc = capture_graph(ctx, ctx->stream, &top))) return rc;
   if ((rc = norm64_dev(ctx, ctx->rhs, ctx->dots))) return rc;  // ||b||
-  k_solve_init<<<1, 32, 0, ctx->stream>>>((RefineDev *)ctx->rdev, ctx->dots);
+  ecs_launch_pdl(k_solve_init, 1, 32, 0, ctx->stream, (RefineDev *)ctx->rdev, ctx->dots);
   ECS_LAUNCHED(ctx);
   if (identity_lhs(ctx)) {  // -lhs identity (ComputeIdentityLHS, src/lhs.c:11-23): phi = b exactly
     ECS_CUDA(ctx, cudaMemcpyAsync(ctx->phi, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -2002,6 +2029,7 @@ int solve_graph_launch(EcsCtx *ctx, double rtol, int max_it, int warm, int setup
 // Fluxes of a loaded density (src/file-io.c:51-59: VecAXPY into a zeroed
 // vector, so G_d = 0 + flux_scale_d * n), into the SoA moment planes 1..3.
 __global__ void k_density_flux(size_t n, double f0, double f1, double f2, double *__restrict__ mom) {
+  ECS_PDL_ENTRY();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     const double d = mom[c];
     mom[n + c] = __dadd_rn(0.0, __dmul_rn(f0, d));
@@ -2063,7 +2091,7 @@ int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it
       break;
     }
     if ((rc = last_captured(ctx, ctx->stream, &rg.in_node))) break;
-    k_density_flux<<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, fs[0], fs[1], fs[2], ctx->mom);
+    ecs_launch_pdl(k_density_flux, blocks_for(ctx, n), kB, 0, ctx->stream, n, fs[0], fs[1], fs[2], ctx->mom);
     if ((ce = cudaGetLastError()) != cudaSuccess) {
       rc = ecs_cuda_check(ctx, ce, "kernel launch");
       break;
@@ -2219,7 +2247,7 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         zero_guess = false;
       } else {
-        k_residual64<<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
+        ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
         ECS_LAUNCHED(ctx);
         if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2244,13 +2272,13 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
       if (ctx->prec == ECS_PREC_FP64) {
         // the cycle solves A e = r64 directly (beta = ||r64||)
         if ((rc = fgmres_cycle<double>(ctx, tol_cycle, max_it - its))) return rc;
-        k_axpy64<double><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, 1.0, ctx->w64, ctx->phi);
+        ecs_launch_pdl(k_axpy64<double>, blocks_for(ctx, n), kB, 0, ctx->stream, n, 1.0, ctx->w64, ctx->phi);
       } else {
         float *r32 = cycle_b<float>(ctx), *e32 = cycle_x<float>(ctx);
-        k_scale_to<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, ctx->r64, ctx->dots + 1, r32);
+        ecs_launch_pdl(k_scale_to<float>, blocks_for(ctx, n), kB, 0, ctx->stream, n, ctx->r64, ctx->dots + 1, r32);
         ECS_LAUNCHED(ctx);
         if ((rc = fgmres_cycle<float>(ctx, std::max(tol_cycle, 2e-6), max_it - its))) return rc;
-        k_axpy64<float><<<blocks_for(ctx, n), kB, 0, ctx->stream>>>(n, rn, e32, ctx->phi);
+        ecs_launch_pdl(k_axpy64<float>, blocks_for(ctx, n), kB, 0, ctx->stream, n, rn, e32, ctx->phi);
       }
       ECS_LAUNCHED(ctx);
       if ((rc = project_mean<double>(ctx, ctx->phi))) return rc;
@@ -2279,7 +2307,7 @@ int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y) {
     ECS_CUDA(ctx, cudaMemcpyAsync(y, x, ctx->ncell * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     return ECS_OK;
   }
-  k_apply<double><<<blocks3(o64.g), threads3(), 0, ctx->stream>>>(o64, op_density(ctx), x, nullptr, y, 0);
+  ecs_launch_pdl(k_apply<double>, blocks3(o64.g), threads3(), 0, ctx->stream, o64, op_density(ctx), x, nullptr, y, 0);
   ECS_LAUNCHED(ctx);
   return ECS_OK;
 }
