@@ -203,8 +203,11 @@ struct EcsCtx {
   int64_t stage_n = 0;              // ions per staging buffer
   // Host hand-off of ecs_step_host: the ions' download runs beside the next
   // chunk's upload, through its own staging buffers and events.
-  double *stage_dn[2] = {nullptr, nullptr};
-  cudaEvent_t xev_dn_conv[2] = {nullptr, nullptr}, xev_dn_copy[2] = {nullptr, nullptr};
+  static constexpr int kStageDn = 3;
+  double *stage_dn[kStageDn] = {nullptr, nullptr, nullptr};
+  cudaStream_t xs_conv = nullptr;   // conversions of the download
+  cudaEvent_t xev_tiled[kStageDn] = {nullptr, nullptr, nullptr};
+  cudaEvent_t xev_dn_conv[kStageDn] = {nullptr, nullptr, nullptr}, xev_dn_copy[kStageDn] = {nullptr, nullptr, nullptr};
   uint64_t pgen = 0;                // bumped by every change of the device ions
   uint64_t host_gen = ~0ull;        // pgen when ecs_step_host last returned the ions to the host
   bool bounds_valid = false;        // tile_bounds holds the current sort's tile offsets

@@ -952,6 +952,10 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prior1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// Block shape of the tile kernel: one block a tile.
+constexpr int kTileThreads = 256;
+constexpr int kTileBlocksPerSM = 4;
+
 struct TileCtx {
   int wx0, wy0, wz0;  // window origin (node and cell index of its corner)
 };
@@ -1015,7 +1019,7 @@ __device__ __forceinline__ void tile_finish(const PartK &k, int mode, EcsDevStat
   if (mode & 7) store_ion(dst, ip, ion_record(q));
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const float4 *src, float4 *dst,
+__global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(PartK k, int mode, const float4 *src, float4 *dst,
                                                      const int32_t *__restrict__ perm, const float4 *__restrict__ E,
                                                      long long *__restrict__ acc, const int32_t *__restrict__ key_off,
                                                      int32_t *__restrict__ count, int32_t *__restrict__ keys,
@@ -1024,7 +1028,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
   __shared__ int wcnt[kWCells];       // cells of the moved ions (next sort)
   __shared__ int dcnt[kWCells];       // window deposits a cell (bias removal)
   __shared__ float4 ewin[kEXY * kWZ];  // difference numerators of the window's nodes (padded strides)
-  __shared__ float4 pre[2][2 * kBlock];  // each thread's prefetched records, two iterations
+  __shared__ float4 pre[2][2 * kTileThreads];  // each thread's prefetched records, two iterations
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool collide = (mode & 2) && k.collide;
   unsigned int nacc = 0, nref = 0;  // collision counters of this thread, flushed at the end
@@ -1046,7 +1050,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_tiles32(PartK k, int mode, const 
     for (int ca = a; ca < b; ca += kWindowMax) {
       const int L = min(kWindowMax, b - ca);
       const int seg = (L + 31) >> 5;               // lane segment
-      const int sub = (seg + kBlock / 32 - 1) / (kBlock / 32);  // a warp's run inside each segment
+      const int sub = (seg + kTileThreads / 32 - 1) / (kTileThreads / 32);  // a warp's run inside each segment
       if (mode & 8) {
         for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0u;
         for (int e = threadIdx.x; e < kWCells; e += blockDim.x) dcnt[e] = 0;
@@ -1655,11 +1659,14 @@ void ecs_part_xfer_free(EcsCtx *ctx) {
     if (ctx->xs[q]) cudaStreamDestroy(ctx->xs[q]);
   }
   if (ctx->xev_ready) cudaEventDestroy(ctx->xev_ready);
-  for (int q = 0; q < 2; q++) {
+  if (ctx->xs_conv) cudaStreamSynchronize(ctx->xs_conv);
+  for (int q = 0; q < EcsCtx::kStageDn; q++) {
     if (ctx->stage_dn[q]) cudaFree(ctx->stage_dn[q]);
+    if (ctx->xev_tiled[q]) cudaEventDestroy(ctx->xev_tiled[q]);
     if (ctx->xev_dn_conv[q]) cudaEventDestroy(ctx->xev_dn_conv[q]);
     if (ctx->xev_dn_copy[q]) cudaEventDestroy(ctx->xev_dn_copy[q]);
   }
+  if (ctx->xs_conv) cudaStreamDestroy(ctx->xs_conv);
 }
 
 // Host AoS FP64 -> device: copies on xs[1], conversions on ctx->stream.
@@ -1830,6 +1837,7 @@ int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
 
 int ecs_part_xfer_wait(EcsCtx *ctx) {
   if (!ctx->xs[1]) return ECS_OK;
+  if (ctx->xs_conv) ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs_conv));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[0]));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[1]));
   return ECS_OK;
@@ -1914,7 +1922,7 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
     const bool gather = ctx->perm_pending, writes = (mode & 7) != 0;
     float4 *src = ctx->ions[ctx->cur];
     float4 *dst = gather ? ctx->ions[1 - ctx->cur] : src;
-    k_tiles32<<<ntiles, kBlock, 0, ctx->stream>>>(k, mode, src, dst, gather ? ctx->perm : nullptr, ctx->eext32,
+    k_tiles32<<<ntiles, kTileThreads, 0, ctx->stream>>>(k, mode, src, dst, gather ? ctx->perm : nullptr, ctx->eext32,
                                                   ctx->acc, ctx->sort_offset, count, ctx->sort_keys, ctx->dstat, 0,
                                                   ntiles);
     if (gather && writes) {
@@ -2099,12 +2107,15 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   for (int t = 0; t < ntiles; t++)
     if (tb[t + 1] - tb[t] > chunk) return ECS_ERR_STATE;  // a tile larger than a staging chunk
   if (!ctx->stage_dn[0]) {
-    for (int q = 0; q < 2; q++) {
+    ECS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->xs_conv, cudaStreamNonBlocking));
+    for (int q = 0; q < EcsCtx::kStageDn; q++) {
       ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage_dn[q], (size_t)chunk * 6 * sizeof(double)));
+      ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_tiled[q], cudaEventDisableTiming));
       ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_conv[q], cudaEventDisableTiming));
       ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_copy[q], cudaEventDisableTiming));
     }
   }
+  constexpr int ND = EcsCtx::kStageDn;
   const int collide = ctx->p.mn > 0.0;
   int mode = 1 | (collide ? 2 : 0) | 4 | 8;
   PartK k;
@@ -2120,14 +2131,15 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));  // earlier work on the buffers
   ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
   ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_ready, 0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_ready, 0));
   if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
   int64_t c = 0;
   for (int t0 = 0; t0 < ntiles;) {
     int t1 = t0 + 1;
     while (t1 < ntiles && (int64_t)tb[t1 + 1] - tb[t0] <= chunk) t1++;
     const int64_t A = tb[t0], n = (int64_t)tb[t1] - A;
-    const int q = (int)(c & 1);
-    double *in = ctx->stage[q], *out = ctx->stage_dn[q];
+    const int q = (int)(c & 1), qd = (int)(c % ND);
+    double *in = ctx->stage[q], *out = ctx->stage_dn[qd];
     if (n > 0) {
       if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));  // staging in free
       ECS_CUDA(ctx, cudaMemcpyAsync(in, pos + nd * A, (size_t)n * nd * sizeof(double), cudaMemcpyHostToDevice,
@@ -2140,20 +2152,22 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
       ECS_LAUNCHED(ctx);
       ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
     }
-    k_tiles32<<<t1 - t0, kBlock, 0, ctx->stream>>>(k, mode, ions, ions, nullptr, ctx->eext32, ctx->acc,
+    k_tiles32<<<t1 - t0, kTileThreads, 0, ctx->stream>>>(k, mode, ions, ions, nullptr, ctx->eext32, ctx->acc,
                                                     ctx->sort_offset, count, ctx->sort_keys, ctx->dstat, t0, t1);
     ECS_LAUNCHED(ctx);
-    if (n > 0 && !counted) {
-      if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_dn_copy[q], 0));  // staging out free
-      k_mixed_to_aos<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->stream>>>(n, nd, k, out, out + nd * n, ions + 2 * A);
+    if (n > 0 && !counted) {  // conversion on its own stream, so the copies in never wait for the copies out
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_tiled[qd], ctx->stream));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_tiled[qd], 0));
+      if (c >= ND) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_dn_copy[qd], 0));  // staging out free
+      k_mixed_to_aos<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs_conv>>>(n, nd, k, out, out + nd * n, ions + 2 * A);
       ECS_LAUNCHED(ctx);
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[q], ctx->stream));
-      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[q], 0));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[qd], ctx->xs_conv));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[qd], 0));
       ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * A, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
                                     ctx->xs[0]));
       ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * A, out + nd * n, (size_t)n * nd * sizeof(double),
                                     cudaMemcpyDeviceToHost, ctx->xs[0]));
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[q], ctx->xs[0]));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[qd], ctx->xs[0]));
     }
     if (n > 0) c++;
     t0 = t1;
@@ -2165,23 +2179,23 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   if ((rc = sort_after_pass(ctx, counted))) return rc;
   if (counted) {  // the ions in the new key order, read through the permutation
     ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
-    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
+    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_ready, 0));
     int64_t c2 = 0;
     for (int64_t off = 0; off < np; off += chunk, c2++) {
-      const int q = (int)(c2 & 1);
+      const int qd = (int)(c2 % ND);
       const int64_t n = np - off < chunk ? np - off : chunk;
-      double *out = ctx->stage_dn[q];
-      if (c2 >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_copy[q], 0));
-      k_mixed_to_aos_perm<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs[0]>>>(n, nd, k, out, out + nd * n, ions,
-                                                                              ctx->perm + off);
+      double *out = ctx->stage_dn[qd];
+      if (c2 >= ND) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_dn_copy[qd], 0));
+      k_mixed_to_aos_perm<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs_conv>>>(n, nd, k, out, out + nd * n, ions,
+                                                                                ctx->perm + off);
       ECS_LAUNCHED(ctx);
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[q], ctx->xs[0]));
-      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_dn_conv[q], 0));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[qd], ctx->xs_conv));
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[qd], 0));
       ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * off, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
-                                    ctx->xs[1]));
+                                    ctx->xs[0]));
       ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * off, out + nd * n, (size_t)n * nd * sizeof(double),
-                                    cudaMemcpyDeviceToHost, ctx->xs[1]));
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[q], ctx->xs[1]));
+                                    cudaMemcpyDeviceToHost, ctx->xs[0]));
+      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[qd], ctx->xs[0]));
     }
   }
   if (sorted) *sorted = counted ? 1 : 0;

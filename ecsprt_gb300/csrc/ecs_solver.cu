@@ -334,20 +334,28 @@ __global__ void __launch_bounds__(32 * kMaxSeg) k_zline_seg(GridG g, ZlP<T> z, c
 }
 
 // ---- inter-grid transfer ---------------------------------------------------------
-// Full weighting (1/4,1/2,1/4 per axis) from fine (2I+a) to coarse I: the
-// 27 fine cells through the neighbour offsets of the fine cell (2I, 2J, 2K).
+// A level of more than one plane whose coarser level has as many planes is
+// coarsened in x and y only (reflecting z, see mg_alloc): its transfers act
+// within each plane.
+__device__ __forceinline__ bool semi_z(const GridG &gf, const GridG &gc) { return gf.nz == gc.nz && gf.nz > 1; }
+
+// Full weighting (1/4,1/2,1/4 per coarsened axis) from fine (2I+a) to coarse
+// I: the 27 (9 when z is not coarsened) fine cells through the neighbour
+// offsets of the fine cell (2I, 2J, 2K) (or (2I, 2J, K)).
 template <typename T>
 __global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__restrict__ c) {
   ECS_PDL_ENTRY();
   int I, J, K;
   if (!at3(gc.nx, gc.ny, I, J, K)) return;
-  const Nbr q = nbr_of(gf, 2 * I, 2 * J, 2 * K);
+  const bool semi = semi_z(gf, gc);
+  const Nbr q = nbr_of(gf, 2 * I, 2 * J, semi ? K : 2 * K);
   const int oz[3] = {q.zm, 0, q.zp}, oy[3] = {q.ym, 0, q.yp}, ox[3] = {q.xm, 0, q.xp};
   const bool vz[3] = {q.vzm, true, q.vzp}, vy[3] = {q.vym, true, q.vyp}, vx[3] = {q.vxm, true, q.vxp};
   T s = T(0);
 #pragma unroll
   for (int dk = 0; dk < 3; dk++) {
-    const T wk = dk == 1 ? T(0.5) : T(0.25);
+    if (semi && dk != 1) continue;
+    const T wk = semi ? T(1) : (dk == 1 ? T(0.5) : T(0.25));
 #pragma unroll
     for (int dj = 0; dj < 3; dj++) {
       const T wj = dj == 1 ? T(0.5) : T(0.25);
@@ -364,18 +372,21 @@ __global__ void k_restrict(GridG gf, GridG gc, const T *__restrict__ f, T *__res
 // The same full-weighting sum with the loops kept rolled (less code, for the
 // single-block cycle); the terms are added in the same order as k_restrict.
 template <typename T>
-__device__ __forceinline__ T restrict_at_rolled(const GridG &gf, const T *__restrict__ f, int I, int J, int K) {
+__device__ __forceinline__ T restrict_at_rolled(const GridG &gf, const GridG &gc, const T *__restrict__ f, int I,
+                                                int J, int K) {
+  const bool semi = semi_z(gf, gc);
+  const int zl = semi ? 0 : -1, zc = semi ? K : 2 * K;
   T s = T(0);
 #pragma unroll 1
-  for (int dk = -1; dk <= 1; dk++) {
-    const T wk = dk == 0 ? T(0.5) : T(0.25);
+  for (int dk = zl; dk <= -zl; dk++) {
+    const T wk = semi ? T(1) : (dk == 0 ? T(0.5) : T(0.25));
 #pragma unroll 1
     for (int dj = -1; dj <= 1; dj++) {
       const T wj = dj == 0 ? T(0.5) : T(0.25);
 #pragma unroll 1
       for (int di = -1; di <= 1; di++) {
         const T wi = di == 0 ? T(0.5) : T(0.25);
-        s += wk * wj * wi * gval(f, gf, 2 * K + dk, 2 * J + dj, 2 * I + di);
+        s += wk * wj * wi * gval(f, gf, zc + dk, 2 * J + dj, 2 * I + di);
       }
     }
   }
@@ -384,9 +395,11 @@ __device__ __forceinline__ T restrict_at_rolled(const GridG &gf, const T *__rest
 
 // Trilinear prolongation value at fine cell (i,j,k).
 template <typename T>
-__device__ __forceinline__ T prolong_at(const GridG &gc, const T *__restrict__ c, int i, int j, int k) {
-  int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
-  int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+__device__ __forceinline__ T prolong_at(const GridG &gf, const GridG &gc, const T *__restrict__ c, int i, int j,
+                                        int k) {
+  const bool semi = semi_z(gf, gc);
+  int i0 = i >> 1, j0 = j >> 1, k0 = semi ? k : k >> 1;
+  int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (!semi && (k & 1)) ? 2 : 1;
   T wi = ni == 2 ? T(0.5) : T(1), wj = nj == 2 ? T(0.5) : T(1), wk = nk == 2 ? T(0.5) : T(1);
   T s = T(0);
   for (int a = 0; a < nk; a++)
@@ -403,8 +416,9 @@ __global__ void k_prolong_add(GridG gf, GridG gc, const T *__restrict__ c, T *__
   ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(gf.nx, gf.ny, i, j, k)) return;
-  const Nbr q = nbr_of(gc, i >> 1, j >> 1, k >> 1);
-  const bool ti = i & 1, tj = j & 1, tk = k & 1;
+  const bool semi = semi_z(gf, gc);
+  const Nbr q = nbr_of(gc, i >> 1, j >> 1, semi ? k : k >> 1);
+  const bool ti = i & 1, tj = j & 1, tk = !semi && (k & 1);
   const T wi = ti ? T(0.5) : T(1), wj = tj ? T(0.5) : T(1), wk = tk ? T(0.5) : T(1);
   T s = T(0);
 #pragma unroll
@@ -568,7 +582,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
     for (unsigned c = threadIdx.x; c < C.o.g.n; c += blockDim.x) {
       int I, J, K;
       cell_ijk(c, C.o.g, I, J, K);
-      cb[c] = restrict_at_rolled(g, (const T *)r, I, J, K);
+      cb[c] = restrict_at_rolled(g, C.o.g, (const T *)r, I, J, K);
     }
     __syncthreads();
   }
@@ -611,7 +625,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(SmallCycle<T> sc
     for (unsigned c = threadIdx.x; c < g.n; c += blockDim.x) {
       int i, j, k;
       cell_ijk(c, g, i, j, k);
-      t[c] += prolong_at(C.o.g, cx, i, j, k);
+      t[c] += prolong_at(g, C.o.g, cx, i, j, k);
     }
     __syncthreads();
     blk_sweep(L, sm, sm + L.sb, t, sm + L.sx, omega);
@@ -1364,13 +1378,22 @@ int mg_alloc(EcsCtx *ctx) {
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_a0g, (size_t)nx * ny * sizeof(T)));
     ECS_CUDA(ctx, cudaMalloc((void **)&L.zl_qden, (size_t)nx * ny * sizeof(T)));
     mg.lv.push_back(L);
-    // a 2-D grid (nz = 1) coarsens in x and y only
+    // A 2-D grid (nz = 1) coarsens in x and y only.  So does a grid with a
+    // reflecting z: its ghost planes one spacing outside the walls do not
+    // nest under z coarsening, and the z-line smoother resolves z on every
+    // level, so the levels keep all planes down to one column (x y = 1 x 1,
+    // whose Nz cells the coarsest inverse solves directly).
     const bool flat = nz == 1;
-    bool even = (nx % 2 == 0) && (ny % 2 == 0) && (flat || nz % 2 == 0);
-    if (!even || std::min(nx, std::min(ny, flat ? nx : nz)) < 8 || mg.lv.size() >= 12) break;
+    const bool semi = !flat && ctx->p.bc[2] != ECS_BC_PERIODIC;
+    if (semi) {
+      if (nx % 2 || ny % 2 || mg.lv.size() >= 12) break;
+    } else {
+      bool even = (nx % 2 == 0) && (ny % 2 == 0) && (flat || nz % 2 == 0);
+      if (!even || std::min(nx, std::min(ny, flat ? nx : nz)) < 8 || mg.lv.size() >= 12) break;
+    }
     nx /= 2; ny /= 2;
     hx *= 2; hy *= 2;
-    if (!flat) {
+    if (!flat && !semi) {
       nz /= 2;
       hz *= 2;
     }

@@ -48,7 +48,11 @@ enum { ECS_SERVE_SOLVE = 0, ECS_SERVE_SIM = 1 };
 
 typedef struct EcsServeConfig {
   int64_t hbm_budget_bytes; /* device bytes the slots may hold together */
-  int32_t max_inflight;     /* worker threads = requests on the GPU at once */
+  int32_t max_inflight;     /* worker threads = requests on the GPU at once.  Streams
+                               overlap on the device only as far as its hardware work
+                               queues allow: set CUDA_DEVICE_MAX_CONNECTIONS (CUDA's
+                               default 8) to at least this before the process first
+                               uses CUDA, else at most about 4 requests overlap. */
   int32_t precision;        /* ECS_PREC_MIXED or ECS_PREC_FP64 */
   double timeout_seconds;   /* per solve request (<= 0: 60 s); ECS_ERR_TIMEOUT after it */
 } EcsServeConfig;

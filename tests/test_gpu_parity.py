@@ -182,15 +182,19 @@ ITERATION_BOUNDS = {  # (grid, prec) -> most FGMRES iterations (mixed: rtol 1e-8
     ((64, 64, 64), E.ECS_PREC_FP64): 11,
     ((128, 128, 1), E.ECS_PREC_MIXED): 10,
     ((128, 128, 1), E.ECS_PREC_FP64): 12,
+    # reflecting z: levels coarsened in x and y only, down to one column
+    ((64, 64, 32, "reflect"), E.ECS_PREC_MIXED): 12,
+    ((64, 64, 32, "reflect"), E.ECS_PREC_FP64): 13,
 }
 
 
 @pytest.mark.parametrize("key", list(ITERATION_BOUNDS), ids=lambda k: f"{'x'.join(map(str, k[0]))}-{k[1]}")
 def test_multigrid_iteration_counts(built, key):
-    (nx, ny, nz), prec = key
+    (nx, ny, nz, *zbc), prec = key
     nd = 2 if nz == 1 else 3
     opts = (f"-ndim {nd} -Nx {nx} -Ny {ny} " + (f"-Nz {nz} -dz 1 " if nd == 3 else "") +
-            "-dx 1 -dy 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 1.0 -nue 8.79e9 -Te 11604.5 -E0 0 -mn 0")
+            "-dx 1 -dy 1 -qi 1 -mi 1 -B0 0.1 -viT 1 -vi0x 1.0 -nue 8.79e9 -Te 11604.5 -E0 0 -mn 0" +
+            (" -zBC inject-reflect" if zbc else ""))
     p = E.params_from_options(opts)
     rng = np.random.default_rng(20261203 + nx + nz)
     x = np.arange(nx) / nx
