@@ -3,8 +3,10 @@ sources (unmodified, compiled from where they lie) linked with the PETSc-API
 shim in oracle/ref_shim.
 
 TEST INFRASTRUCTURE ONLY, and only where the reference sources are present
-(this container).  Build with :func:`build` or
-``make -C oracle/ref_shim REF=<reference>/src``.
+(the container that holds the reference checkout).  Build with
+``build(<reference>/src)`` or ``make -C oracle/ref_shim REF=<reference>/src``;
+without an argument :func:`build` takes the checkout from the environment
+variable ECSPRT_REFERENCE.
 
 The reference keeps process-global RNG and Sobol state (src/random.c), so
 callers that need a freshly started reference run each case in its own
@@ -21,16 +23,23 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_ref" / "libecsref.so"
-DEFAULT_REF_SRC = Path(os.environ.get("ECSPRT_REFERENCE", "/root/reference")) / "src"
+
+
+def env_ref_src() -> Path | None:
+    """<checkout>/src of the reference named by ECSPRT_REFERENCE, or None."""
+    root = os.environ.get("ECSPRT_REFERENCE")
+    return Path(root) / "src" if root else None
 
 
 def available() -> bool:
-    return LIB_PATH.exists() or DEFAULT_REF_SRC.exists()
+    src = env_ref_src()
+    return LIB_PATH.exists() or (src is not None and src.exists())
 
 
-def build(ref_src: Path = DEFAULT_REF_SRC) -> Path:
-    if not Path(ref_src).exists():
-        raise RuntimeError(f"reference sources not found at {ref_src}")
+def build(ref_src: Path | None = None) -> Path:
+    ref_src = ref_src if ref_src is not None else env_ref_src()
+    if ref_src is None or not Path(ref_src).exists():
+        raise RuntimeError(f"reference sources not found (given {ref_src}; set ECSPRT_REFERENCE)")
     subprocess.run(["make", "-s", "-C", str(HERE / "ref_shim"), f"REF={ref_src}"], check=True)
     return LIB_PATH
 
