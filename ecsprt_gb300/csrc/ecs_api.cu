@@ -131,7 +131,7 @@ int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
                          ((p->Nz + ECS_TILE_Z - 1) / ECS_TILE_Z) * ECS_TILE_CELLS;
     b += keys * 4 * 2 + keys / 1024 * 4;  // sort counts and offsets
   }
-  if (cap > 0) b += 2 * ecs_stage_ions(cap) * 48;  // host-transfer staging
+  if (cap > 0) b += (2 + EcsCtx::kStageDn) * 2 * ecs_stage_stride(ecs_stage_ions(cap)) * 8;  // host-transfer staging
   // allocation rounding (about 40 allocations) and instantiated CUDA graphs
   b += (int64_t)8 << 20;
   return b;

@@ -206,12 +206,15 @@ struct EcsCtx {
   static constexpr int kStageDn = 3;
   double *stage_dn[kStageDn] = {nullptr, nullptr, nullptr};
   cudaStream_t xs_conv = nullptr;   // conversions of the download
+  cudaStream_t xs_up = nullptr;     // conversions of the upload
   cudaEvent_t xev_tiled[kStageDn] = {nullptr, nullptr, nullptr};
   cudaEvent_t xev_dn_conv[kStageDn] = {nullptr, nullptr, nullptr}, xev_dn_copy[kStageDn] = {nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> xev_upc;  // upload chunk k converted (one event a chunk)
   uint64_t pgen = 0;                // bumped by every change of the device ions
   uint64_t host_gen = ~0ull;        // pgen when ecs_step_host last returned the ions to the host
   bool bounds_valid = false;        // tile_bounds holds the current sort's tile offsets
   std::vector<int32_t> tile_bounds; // first ion of every tile, and np (ntiles + 1)
+  std::vector<int32_t> tile_srcmax; // largest source position a tile's ions are gathered from (pending sort)
 };
 
 // ---- error helpers -------------------------------------------------------
@@ -226,6 +229,10 @@ inline int64_t ecs_stage_ions(int64_t cap) {
   if (n > ((int64_t)1 << 22)) n = (int64_t)1 << 22;
   return cap < n ? (cap > 0 ? cap : 1) : n;
 }
+// Doubles per array region of a staging buffer of n ions (3 doubles an ion,
+// plus room for the rounding of ecs_step_host's copies to 256-byte host
+// boundaries); a buffer holds a position region and a velocity region.
+inline int64_t ecs_stage_stride(int64_t n) { return 3 * n + 64; }
 
 int ecs_cuda_check(EcsCtx *ctx, cudaError_t e, const char *what);
 #define ECS_CUDA(ctx, call)                                        \

@@ -1200,35 +1200,57 @@ __global__ void k_mixed_to_aos(int64_t n, int nd, PartK k, double *__restrict__ 
   }
 }
 
+// Download conversion onto whole 256-byte host spans (3-D): the records
+// [i0, i1) written as the doubles [d0, d1) of the position array and
+// [e0, e1) of the velocity array (ion i holds doubles 3i..3i+2 of each),
+// each at its index minus d0 (e0) in the staging regions pos and vel.  The
+// first records of the range may belong to the range before, whose span
+// ended at the same host boundary.
+__global__ void k_mixed_to_aos_span(int64_t i0, int64_t i1, int64_t d0, int64_t d1, int64_t e0, int64_t e1, PartK k,
+                                    double *__restrict__ pos, double *__restrict__ vel,
+                                    const float4 *__restrict__ ions) {
+  for (int64_t i = i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < i1;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const Ion q = load_ion(ions, i);
+    int ci, cj, ck;
+    unpack_cell(q.c, ci, cj, ck);
+    const double p3[3] = {((double)ci + (double)q.ox) * k.dx, ((double)cj + (double)q.oy) * k.dy,
+                          ((double)ck + (double)q.oz) * k.dz};
+    const double v3[3] = {q.vx, q.vy, q.vz};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const int64_t d = 3 * i + c;
+      if (d >= d0 && d < d1) pos[d - d0] = p3[c];
+      if (d >= e0 && d < e1) vel[d - e0] = v3[c];
+    }
+  }
+}
+
 // ids[i] = identity of the i-th ion record (the order of a download).
 __global__ void k_mixed_ids(int64_t n, const float4 *__restrict__ ions, int32_t *__restrict__ ids) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     ids[i] = __float_as_int(ions[2 * i + 1].w);
 }
 
-// The same conversion as k_mixed_to_aos for the ions in key order: the i-th
-// output is the record at perm[i].
-__global__ void k_mixed_to_aos_perm(int64_t n, int nd, PartK k, double *__restrict__ pos, double *__restrict__ vel,
-                                    const float4 *__restrict__ ions, const int32_t *__restrict__ perm) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const Ion q = load_ion(ions, perm[i]);
-    int ci, cj, ck;
-    unpack_cell(q.c, ci, cj, ck);
-    pos[nd * i] = ((double)ci + (double)q.ox) * k.dx;
-    pos[nd * i + 1] = ((double)cj + (double)q.oy) * k.dy;
-    vel[nd * i] = q.vx; vel[nd * i + 1] = q.vy;
-    if (nd == 3) {
-      pos[3 * i + 2] = ((double)ck + (double)q.oz) * k.dz;
-      vel[3 * i + 2] = q.vz;
-    }
-  }
-}
-
 // out[t] = the first ion of tile t (t <= ntiles; out[ntiles] = np).
 __global__ void k_tile_bounds(int ntiles, const int32_t *__restrict__ key_off, int32_t *__restrict__ out) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += gridDim.x * blockDim.x)
     out[t] = key_off[(size_t)t * ECS_TILE_CELLS];
+}
+
+// out[t] = the largest perm[j] over tile t's ions j (-1 for an empty tile):
+// the last source position a gathering pass reads for the tile.  One warp a
+// tile.
+__global__ void k_tile_srcmax(int ntiles, const int32_t *__restrict__ key_off, const int32_t *__restrict__ perm,
+                              int32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  for (int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); t < ntiles; t += (int)((gridDim.x * blockDim.x) >> 5)) {
+    const int a = key_off[(size_t)t * ECS_TILE_CELLS], b = key_off[(size_t)(t + 1) * ECS_TILE_CELLS];
+    int m = -1;
+    for (int j = a + lane; j < b; j += 32) m = max(m, __ldg(perm + j));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) out[t] = m;
+  }
 }
 
 // ---- counting sort by cell (mixed path) ------------------------------------------
@@ -1645,7 +1667,8 @@ static int ensure_xfer(EcsCtx *ctx) {
   }
   ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_ready, cudaEventDisableTiming));
   const int64_t n = ecs_stage_ions(ctx->cap);
-  for (int q = 0; q < 2; q++) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage[q], (size_t)n * 6 * sizeof(double)));
+  for (int q = 0; q < 2; q++)
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage[q], (size_t)ecs_stage_stride(n) * 2 * sizeof(double)));
   ctx->stage_n = n;
   return ECS_OK;
 }
@@ -1667,6 +1690,12 @@ void ecs_part_xfer_free(EcsCtx *ctx) {
     if (ctx->xev_dn_copy[q]) cudaEventDestroy(ctx->xev_dn_copy[q]);
   }
   if (ctx->xs_conv) cudaStreamDestroy(ctx->xs_conv);
+  if (ctx->xs_up) {
+    cudaStreamSynchronize(ctx->xs_up);
+    cudaStreamDestroy(ctx->xs_up);
+  }
+  for (cudaEvent_t e : ctx->xev_upc) cudaEventDestroy(e);
+  ctx->xev_upc.clear();
 }
 
 // Host AoS FP64 -> device: copies on xs[1], conversions on ctx->stream.
@@ -1838,6 +1867,7 @@ int ecs_part_download_async(EcsCtx *ctx, double *pos, double *vel) {
 int ecs_part_xfer_wait(EcsCtx *ctx) {
   if (!ctx->xs[1]) return ECS_OK;
   if (ctx->xs_conv) ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs_conv));
+  if (ctx->xs_up) ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs_up));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[0]));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->xs[1]));
   return ECS_OK;
@@ -2072,16 +2102,103 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
 
 // ---- the particle pass of ecs_step_host, pipelined with the host copies ---------
 // When the host arrays hold the ions as the previous ecs_step_host call
-// returned them (the generation count has not moved since), the records
-// they become are already in tile order, so the upload, the fused pass and
-// the download run chunk by chunk over ranges of whole tiles: the copy in
-// of one chunk overlaps the pass and the copy out of the one before it
-// (copies in on xs[1], copies out on xs[0], kernels on the context's
-// stream).  When the pass counts cells for a sort, the download waits for
-// the sort and returns the ions in the new key order, read through the
-// permutation (conversions on xs[0], copies on xs[1], beside the field phase
-// that follows); the next call's upload then puts them in the buffer in that
-// order.  The identities become the host indices, as in an upload.
+// returned them (the generation count has not moved since), they are in the
+// order of the device records, so the upload, the fused pass and the
+// download run chunk by chunk:
+//   uploads   fixed chunks of stage_n ions: copies in on xs[1], conversion
+//             into the records on xs_up (two staging buffers), all issued
+//             at once;
+//   the pass  by ranges of whole tiles (at most stage_n ions) on the
+//             context's stream, each range after the upload chunks it reads
+//             have been converted;
+//   downloads by the same ranges: conversion on xs_conv, copies out on
+//             xs[0] (three staging buffers).
+// The copies in never wait for the copies out, so both directions of the
+// host link stay busy.  After a cell sort (pending permutation) the pass
+// gathers each range's ions from their old positions (the host arrays'
+// order) into the other record buffer in key order: a range then waits for
+// the upload chunks of its largest source position (tile_srcmax) and of its
+// own host span, which its download overwrites.  The pass that counts cells
+// for a sort downloads in its own order; the next call gathers.  The
+// identities become the host indices, as in an upload.
+//
+// The copies start and end on 256-byte host boundaries: a copy of host
+// memory that starts inside a 256-byte block moves about a quarter less per
+// second over the host link while copies run both ways.  An upload reads
+// from the boundary at or below its chunk's first double to the one at or
+// above its last (bytes of the neighbours, not converted); a download
+// writes from the boundary at or below its range's first double to the
+// boundary at or below the next range's, so the few ions before that
+// boundary go out with the next range (their records are final by then).
+constexpr uintptr_t kXferAlign = 256;
+static inline double *xfer_lo(double *P, int64_t A, int64_t np) {
+  if (A <= 0) return P;
+  if (A >= np) return P + 3 * np;
+  if ((uintptr_t)P % sizeof(double)) return P + 3 * A;
+  const uintptr_t a = (uintptr_t)(P + 3 * A) & ~(kXferAlign - 1);
+  return a > (uintptr_t)P ? (double *)a : P;
+}
+static inline double *xfer_hi(double *P, int64_t A, int64_t np) {
+  if (A >= np) return P + 3 * np;
+  if ((uintptr_t)P % sizeof(double)) return P + 3 * A;
+  const uintptr_t a = ((uintptr_t)(P + 3 * A) + kXferAlign - 1) & ~(kXferAlign - 1);
+  return a < (uintptr_t)(P + 3 * np) ? (double *)a : P + 3 * np;
+}
+
+// Download of the records [A, A + n) of recs as the whole host spans from
+// xfer_lo(A) to xfer_lo(A + n): conversion on xs_conv into staging buffer
+// qd, copies on xs[0].
+static int host_span_out(EcsCtx *ctx, const PartK &k, double *pos, double *vel, int64_t np, int64_t A, int64_t n,
+                         const float4 *recs, int qd) {
+  const int64_t stride = ecs_stage_stride(ctx->stage_n);
+  double *out = ctx->stage_dn[qd];
+  double *p0 = xfer_lo(pos, A, np), *p1 = xfer_lo(pos, A + n, np);
+  double *v0 = xfer_lo(vel, A, np), *v1 = xfer_lo(vel, A + n, np);
+  const int64_t d0 = p0 - pos, d1 = p1 - pos, e0 = v0 - vel, e1 = v1 - vel;
+  const int64_t i0 = std::min(d0 / 3, e0 / 3), i1 = A + n;
+  k_mixed_to_aos_span<<<grid_blocks(ctx, i1 - i0, 8), kBlock, 0, ctx->xs_conv>>>(i0, i1, d0, d1, e0, e1, k, out,
+                                                                               out + stride, recs);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[qd], ctx->xs_conv));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[qd], 0));
+  if (d1 > d0)
+    ECS_CUDA(ctx, cudaMemcpyAsync(p0, out, (size_t)(d1 - d0) * sizeof(double), cudaMemcpyDeviceToHost, ctx->xs[0]));
+  if (e1 > e0)
+    ECS_CUDA(ctx, cudaMemcpyAsync(v0, out + stride, (size_t)(e1 - e0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->xs[0]));
+  ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[qd], ctx->xs[0]));
+  return ECS_OK;
+}
+
+// The current sort's first ion of every tile (tile_bounds) and, with a
+// gather pending, every tile's largest source position (tile_srcmax).
+static int host_tile_tables(EcsCtx *ctx, int ntiles, bool gather) {
+  const bool want_b = !ctx->bounds_valid;
+  if (!want_b && !gather) return ECS_OK;
+  const size_t nb = (size_t)ntiles + 1;
+  int32_t *d = nullptr;
+  ECS_CUDA(ctx, cudaMallocAsync((void **)&d, (nb + (size_t)ntiles) * sizeof(int32_t), ctx->stream));
+  if (want_b) {
+    ctx->tile_bounds.resize(nb);
+    k_tile_bounds<<<ecs_div_up(nb, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, d);
+    ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_bounds.data(), d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  }
+  if (gather) {
+    ctx->tile_srcmax.resize((size_t)ntiles);
+    k_tile_srcmax<<<ecs_div_up((size_t)ntiles * 32, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, ctx->perm,
+                                                                                  d + nb);
+    ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_srcmax.data(), d + nb, (size_t)ntiles * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  ECS_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->bounds_valid = true;
+  return ECS_OK;
+}
+
 int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, int *sorted) {
   if (ctx->prec != ECS_PREC_MIXED || ctx->p.ndim != 3 || np != ctx->np || np == 0 || !ctx->tiles_valid ||
       ctx->host_gen != ctx->pgen)
@@ -2090,32 +2207,30 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   if (rc) return rc;
   const int64_t chunk = ctx->stage_n;
   const int ntiles = ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2];
-  if (!ctx->bounds_valid) {
-    ctx->tile_bounds.resize((size_t)ntiles + 1);
-    int32_t *d = nullptr;
-    ECS_CUDA(ctx, cudaMallocAsync((void **)&d, ((size_t)ntiles + 1) * sizeof(int32_t), ctx->stream));
-    k_tile_bounds<<<ecs_div_up((size_t)ntiles + 1, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, d);
-    ECS_LAUNCHED(ctx);
-    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_bounds.data(), d, ((size_t)ntiles + 1) * sizeof(int32_t),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    ECS_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
-    ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    ctx->bounds_valid = true;
-  }
+  const bool gather = ctx->perm_pending;
+  if ((rc = host_tile_tables(ctx, ntiles, gather))) return rc;
   const int32_t *tb = ctx->tile_bounds.data();
   if (tb[ntiles] != np) return ECS_ERR_STATE;
   for (int t = 0; t < ntiles; t++)
     if (tb[t + 1] - tb[t] > chunk) return ECS_ERR_STATE;  // a tile larger than a staging chunk
+  const int64_t nup = ecs_div_up(np, chunk);
   if (!ctx->stage_dn[0]) {
     ECS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->xs_conv, cudaStreamNonBlocking));
+    ECS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->xs_up, cudaStreamNonBlocking));
     for (int q = 0; q < EcsCtx::kStageDn; q++) {
-      ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage_dn[q], (size_t)chunk * 6 * sizeof(double)));
+      ECS_CUDA(ctx, cudaMalloc((void **)&ctx->stage_dn[q], (size_t)ecs_stage_stride(chunk) * 2 * sizeof(double)));
       ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_tiled[q], cudaEventDisableTiming));
       ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_conv[q], cudaEventDisableTiming));
       ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->xev_dn_copy[q], cudaEventDisableTiming));
     }
   }
+  while ((int64_t)ctx->xev_upc.size() < nup) {
+    cudaEvent_t e;
+    ECS_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->xev_upc.push_back(e);
+  }
   constexpr int ND = EcsCtx::kStageDn;
+  const int64_t stride = ecs_stage_stride(chunk);
   const int collide = ctx->p.mn > 0.0;
   int mode = 1 | (collide ? 2 : 0) | 4 | 8;
   PartK k;
@@ -2125,79 +2240,94 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   if (counted) ECS_CUDA(ctx, cudaMemsetAsync(ctx->sort_count, 0, ctx->nkeys * sizeof(int32_t), ctx->stream));
   int32_t *count = counted ? ctx->sort_count : nullptr;
   const int nd = 3;
-  ctx->perm_pending = false;  // the buffer takes the host's order
   ctx->pgen++;
-  float4 *ions = ctx->ions[ctx->cur];
+  float4 *src = ctx->ions[ctx->cur];
+  float4 *dst = gather ? ctx->ions[1 - ctx->cur] : src;
   ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));  // earlier work on the buffers
-  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_ready, 0));
-  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_ready, 0));
-  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_ready, 0));
+  for (cudaStream_t s : {ctx->xs[0], ctx->xs[1], ctx->xs_conv, ctx->xs_up})
+    ECS_CUDA(ctx, cudaStreamWaitEvent(s, ctx->xev_ready, 0));
   if (ctx->ev[0]) cudaEventRecord(ctx->ev[0], ctx->stream);
-  int64_t c = 0;
+  // every upload chunk: copies in, then its conversion into the records
+  for (int64_t u = 0; u < nup; u++) {
+    const int q = (int)(u & 1);
+    const int64_t A = u * chunk, n = std::min(chunk, np - A);
+    double *in = ctx->stage[q];
+    if (u >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_upc[u - 2], 0));  // staging in free
+    double *p0 = xfer_lo(pos, A, np), *p1 = xfer_hi(pos, A + n, np);
+    double *v0 = xfer_lo(vel, A, np), *v1 = xfer_hi(vel, A + n, np);
+    ECS_CUDA(ctx, cudaMemcpyAsync(in, p0, (size_t)(p1 - p0) * sizeof(double), cudaMemcpyHostToDevice, ctx->xs[1]));
+    ECS_CUDA(ctx, cudaMemcpyAsync(in + stride, v0, (size_t)(v1 - v0) * sizeof(double), cudaMemcpyHostToDevice,
+                                  ctx->xs[1]));
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
+    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_up, ctx->xev_copy[q], 0));
+    k_aos_to_mixed<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs_up>>>(n, nd, k, in + (pos + nd * A - p0),
+                                                                    in + stride + (vel + nd * A - v0), src + 2 * A, A);
+    ECS_LAUNCHED(ctx);
+    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_upc[u], ctx->xs_up));
+  }
+  // the pass and the download by ranges of whole tiles; a range waits for
+  // the upload chunk of the last ion it reads (gathered sources) or
+  // overwrites on the host (its own span)
+  struct Range {
+    int t0, t1;
+    int64_t A, n, need;
+  };
+  std::vector<Range> rg;
+  const int32_t *smax = gather ? ctx->tile_srcmax.data() : nullptr;
   for (int t0 = 0; t0 < ntiles;) {
     int t1 = t0 + 1;
     while (t1 < ntiles && (int64_t)tb[t1 + 1] - tb[t0] <= chunk) t1++;
     const int64_t A = tb[t0], n = (int64_t)tb[t1] - A;
-    const int q = (int)(c & 1), qd = (int)(c % ND);
-    double *in = ctx->stage[q], *out = ctx->stage_dn[qd];
     if (n > 0) {
-      if (c >= 2) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[1], ctx->xev_kern[q], 0));  // staging in free
-      ECS_CUDA(ctx, cudaMemcpyAsync(in, pos + nd * A, (size_t)n * nd * sizeof(double), cudaMemcpyHostToDevice,
-                                    ctx->xs[1]));
-      ECS_CUDA(ctx, cudaMemcpyAsync(in + nd * n, vel + nd * A, (size_t)n * nd * sizeof(double),
-                                    cudaMemcpyHostToDevice, ctx->xs[1]));
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_copy[q], ctx->xs[1]));
-      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_copy[q], 0));
-      k_aos_to_mixed<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->stream>>>(n, nd, k, in, in + nd * n, ions + 2 * A, A);
-      ECS_LAUNCHED(ctx);
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_kern[q], ctx->stream));
+      int64_t last = A + n - 1;
+      if (smax)
+        for (int t = t0; t < t1; t++) last = std::max(last, (int64_t)smax[t]);
+      rg.push_back({t0, t1, A, n, std::min(last / chunk, nup - 1)});
     }
-    k_tiles32<<<t1 - t0, kTileThreads, 0, ctx->stream>>>(k, mode, ions, ions, nullptr, ctx->eext32, ctx->acc,
-                                                    ctx->sort_offset, count, ctx->sort_keys, ctx->dstat, t0, t1);
+    t0 = t1;
+  }
+  // The kernels run in the order of the chunks they wait for (after a sort,
+  // ions that crossed a periodic face come from the far end of the old
+  // order: their ranges go last).  A range's download also carries the last
+  // few ions of the range before it, so it goes out once both are done.
+  const int R = (int)rg.size();
+  std::vector<int> order(R);
+  for (int r = 0; r < R; r++) order[r] = r;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rg[a].need < rg[b].need; });
+  std::vector<char> done(R, 0), out(R, 0);
+  int64_t waited = -1, c = 0;
+  for (int r : order) {
+    const Range &g = rg[r];
+    if (g.need > waited) {
+      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_upc[g.need], 0));
+      waited = g.need;
+    }
+    k_tiles32<<<g.t1 - g.t0, kTileThreads, 0, ctx->stream>>>(k, mode, src, dst, gather ? ctx->perm : nullptr,
+                                                          ctx->eext32, ctx->acc, ctx->sort_offset, count,
+                                                          ctx->sort_keys, ctx->dstat, g.t0, g.t1);
     ECS_LAUNCHED(ctx);
-    if (n > 0 && !counted) {  // conversion on its own stream, so the copies in never wait for the copies out
+    done[r] = 1;
+    for (int d = r; d <= r + 1 && d < R; d++) {
+      if (out[d] || !done[d] || (d > 0 && !done[d - 1])) continue;
+      const int qd = (int)(c % ND);
       ECS_CUDA(ctx, cudaEventRecord(ctx->xev_tiled[qd], ctx->stream));
       ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_tiled[qd], 0));
       if (c >= ND) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_dn_copy[qd], 0));  // staging out free
-      k_mixed_to_aos<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs_conv>>>(n, nd, k, out, out + nd * n, ions + 2 * A);
-      ECS_LAUNCHED(ctx);
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[qd], ctx->xs_conv));
-      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[qd], 0));
-      ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * A, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
-                                    ctx->xs[0]));
-      ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * A, out + nd * n, (size_t)n * nd * sizeof(double),
-                                    cudaMemcpyDeviceToHost, ctx->xs[0]));
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[qd], ctx->xs[0]));
+      if ((rc = host_span_out(ctx, k, pos, vel, np, rg[d].A, rg[d].n, dst, qd))) return rc;
+      out[d] = 1;
+      c++;
     }
-    if (n > 0) c++;
-    t0 = t1;
   }
+  if (waited < nup - 1) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xev_upc[nup - 1], 0));
   if (ctx->ev[1]) {
     cudaEventRecord(ctx->ev[1], ctx->stream);
     ctx->ev_particle = true;
   }
-  if ((rc = sort_after_pass(ctx, counted))) return rc;
-  if (counted) {  // the ions in the new key order, read through the permutation
-    ECS_CUDA(ctx, cudaEventRecord(ctx->xev_ready, ctx->stream));
-    ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_ready, 0));
-    int64_t c2 = 0;
-    for (int64_t off = 0; off < np; off += chunk, c2++) {
-      const int qd = (int)(c2 % ND);
-      const int64_t n = np - off < chunk ? np - off : chunk;
-      double *out = ctx->stage_dn[qd];
-      if (c2 >= ND) ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs_conv, ctx->xev_dn_copy[qd], 0));
-      k_mixed_to_aos_perm<<<grid_blocks(ctx, n, 8), kBlock, 0, ctx->xs_conv>>>(n, nd, k, out, out + nd * n, ions,
-                                                                                ctx->perm + off);
-      ECS_LAUNCHED(ctx);
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_conv[qd], ctx->xs_conv));
-      ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->xev_dn_conv[qd], 0));
-      ECS_CUDA(ctx, cudaMemcpyAsync(pos + nd * off, out, (size_t)n * nd * sizeof(double), cudaMemcpyDeviceToHost,
-                                    ctx->xs[0]));
-      ECS_CUDA(ctx, cudaMemcpyAsync(vel + nd * off, out + nd * n, (size_t)n * nd * sizeof(double),
-                                    cudaMemcpyDeviceToHost, ctx->xs[0]));
-      ECS_CUDA(ctx, cudaEventRecord(ctx->xev_dn_copy[qd], ctx->xs[0]));
-    }
+  if (gather) {
+    ctx->cur = 1 - ctx->cur;
+    ctx->perm_pending = false;
   }
+  if ((rc = sort_after_pass(ctx, counted))) return rc;
   if (sorted) *sorted = counted ? 1 : 0;
   if (mode & 2) {
     rc = finish_collisions(ctx, dt);

@@ -77,6 +77,53 @@ def test_host_step_matches_device_step(built, sort_every):
     assert nsorted >= 2
 
 
+@pytest.mark.parametrize("shift", [(1, 0), (0, 5), (3, 30)])
+def test_host_step_unaligned_host_arrays(built, shift):
+    """The host copies run on 256-byte host boundaries, read a little past
+    each chunk and write the few ions before a boundary with the next chunk:
+    with the position and velocity arrays at different offsets from those
+    boundaries (views `shift` doubles into pinned buffers), the ions, moments
+    and potential still equal the device-resident step's, over steps with and
+    without a sort, and no double outside the arrays changes."""
+    p, pos, vel = setup(n=24, ppc=20, seed=11)
+    N = pos.shape[0]
+    steps = 5
+    with E.Context(p, E.ECS_PREC_MIXED, np_capacity=N) as ctx:
+        ctx.set_sort_every(2)
+        ctx.upload_particles(pos, vel)
+        ctx.collect()
+        ctx.compute_potential(rtol=1e-8, max_it=400)
+        ref = []
+        for _ in range(steps):
+            ctx.step(0.1, 1e-8, 400)
+            ref.append((ctx.moments, ctx.phi, as_set(*ctx.download_particles())))
+    with E.Context(p, E.ECS_PREC_MIXED, np_capacity=N) as ctx:
+        ctx.set_sort_every(2)
+        ctx.upload_particles(pos, vel)
+        ctx.collect()
+        ctx.compute_potential(rtol=1e-8, max_it=400)
+        gp, gv = ctx.download_particles()
+        sp, sv = shift
+        bp = E.pinned_empty((3 * N + sp + 40,))
+        bv = E.pinned_empty((3 * N + sv + 40,))
+        bp[:] = -7.0
+        bv[:] = -7.0
+        hp = bp[sp:sp + 3 * N].reshape(N, 3)
+        hv = bv[sv:sv + 3 * N].reshape(N, 3)
+        hp[:] = gp
+        hv[:] = gv
+        hm = E.pinned_empty(ctx.shape + (4,))
+        hphi = E.pinned_empty(ctx.shape)
+        for s in range(steps):
+            ctx.step_host(hp, hv, 0.1, 1e-8, 400, hm, hphi)
+            m, phi, ions = ref[s]
+            assert np.array_equal(hm, m), s
+            assert np.array_equal(hphi, phi), s
+            assert np.array_equal(as_set(hp, hv), ions), s
+        assert (bp[:sp] == -7.0).all() and (bp[sp + 3 * N:] == -7.0).all()
+        assert (bv[:sv] == -7.0).all() and (bv[sv + 3 * N:] == -7.0).all()
+
+
 def test_host_step_reordered_between_calls(built):
     p, pos, vel = setup(seed=5)
     with E.Context(p, E.ECS_PREC_MIXED, np_capacity=pos.shape[0]) as ctx:

@@ -26,9 +26,11 @@ def test_request_bytes(built):
     ions = 32 ** 3 * 16
     sim = E.serve_request_bytes(p, E.ECS_PREC_MIXED, E.ECS_SERVE_SIM, ions)
     solve = E.serve_request_bytes(p, E.ECS_PREC_MIXED, E.ECS_SERVE_SOLVE, ions)
-    # two 32-byte records, a sort key and a permutation entry an ion, plus two
-    # staging chunks of 48 bytes an ion
-    assert sim - solve == 72 * ions + 2 * max(ions // 8, 1 << 16) * 48
+    # two 32-byte records, a sort key and a permutation entry an ion, plus five
+    # staging buffers (two in, three out) of a position and a velocity region
+    # of 3 doubles an ion and 64 doubles of alignment room each
+    chunk = max(ions // 8, 1 << 16)
+    assert sim - solve == 72 * ions + 5 * 2 * (3 * chunk + 64) * 8
     assert E.serve_request_bytes(params(16)) > 8 << 20  # fixed allowance: rounding, graphs
 
 
