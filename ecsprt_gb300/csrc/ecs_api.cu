@@ -118,6 +118,7 @@ int64_t ecs_ctx_device_bytes(const EcsParams *p, int precision, int64_t cap) {
   int64_t b = 0;
   b += n * 8 * (1 + 4 + 1) + n * 8 * 4;  // phi, moments, rhs; fixed-point accumulators
   b += n * 8 * 2 + (m + 2) * 1024 * 8;   // FP64 residual and correction, reductions
+  if (p->lhs_type != ECS_LHS_IDENTITY) b += n * 8 * 11;  // FP64 row coefficients of the residuals
   // multigrid: 11 cell arrays and 2 plane arrays a level, levels summing to
   // at most 8/7 of the finest; the coarsest level's inverse (<= 128 cells)
   b += (n * 11 + n / 4) * t * 8 / 7 + 128 * 128 * 3 * t;

@@ -159,6 +159,7 @@ struct EcsCtx {
   float *kz32 = nullptr;
   double *w64 = nullptr;            // FP64 work vectors
   double *r64 = nullptr;
+  double *coef64 = nullptr;         // the FP64 operator's 11 row coefficients a cell (SoA), for the refinement residuals
   double *dots = nullptr;           // device scalars (norms, means) [m+2]
   double *h_dots = nullptr;         // pinned host copy
   void *kdev = nullptr;             // device FGMRES control block
@@ -170,10 +171,11 @@ struct EcsCtx {
   void *rdev = nullptr;             // device state of the refinement loop
   void *rdev_host = nullptr;        // pinned copy
   cudaStream_t capst[3] = {nullptr, nullptr, nullptr};  // capture streams (graph nesting levels)
-  // side streams and events of the multigrid set-up, which forks off the
-  // context's stream and joins it again
-  cudaStream_t sst[2] = {nullptr, nullptr};
-  cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // side streams and events of the field set-up (multigrid levels, FP64 row
+  // coefficients, right-hand side), which forks off the context's stream and
+  // joins it again
+  cudaStream_t sst[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t sev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_solve[2] = {nullptr, nullptr};
   bool lhs_ready = false;
   bool moments_ready = false;

@@ -1454,22 +1454,48 @@ int zline_factor(EcsCtx *ctx, MgLevel<T> &L, cudaStream_t s) {
   return ECS_OK;
 }
 
+// The 11 FP64 row coefficients of every cell, coef[e * n + c] (e in the
+// order of off_i/off_j/off_k), computed once per operator set-up: FP64
+// arithmetic runs at a small fraction of the FP32 rate on this GPU, and the
+// coefficients take about three quarters of a residual's FP64 operations.
+__global__ void k_coef64(OpK o, const double *__restrict__ n, double *__restrict__ coef) {
+  ECS_PDL_ENTRY();
+  int i, j, k;
+  if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
+  const Nbr q = nbr_of(o.g, i, j, k);
+  double v[11];
+  row11_n(n, o, q, v);
+#pragma unroll
+  for (int e = 0; e < 11; e++) coef[(size_t)e * o.g.n + q.c] = v[e];
+}
+
 // Operator set-up of the multigrid levels: level densities, z-line factors,
-// coarsest inverse.  The pieces are latency-bound small launches with few
-// dependencies, so they run on three streams (also inside a graph capture,
-// where the fork and join become graph edges):
+// coarsest inverse, and the FP64 row coefficients of the refinement
+// residuals.  The pieces are latency-bound small launches with few
+// dependencies (and one FP64-bound kernel), so they run on four streams
+// (also inside a graph capture, where the fork and join become graph edges):
 //   context stream: fine density, fine z-line factors
 //   sst[0]:         restriction chain of the densities, then the coarse inverse
 //   sst[1]:         z-line factors of the coarse levels (after the chain)
-// and the context stream waits for both side streams at the end.
+//   sst[2]:         FP64 row coefficients
+// and the context stream waits for the side streams at the end.
 template <typename T>
 int mg_setup(EcsCtx *ctx) {
   int rc = mg_alloc<T>(ctx);
   if (rc) return rc;
   if ((rc = ensure_setup_streams(ctx))) return rc;
   Multigrid<T> &mg = mg_of<T>(ctx);
-  cudaStream_t s0 = ctx->stream, sa = ctx->sst[0], sb = ctx->sst[1];
+  cudaStream_t s0 = ctx->stream, sa = ctx->sst[0], sb = ctx->sst[1], sc = ctx->sst[2];
   MgLevel<T> &L0 = mg.lv[0];
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[4], s0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(sc, ctx->sev[4], 0));
+  {
+    const EcsParams &p = ctx->p;
+    const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
+    ecs_launch_pdl(k_coef64, blocks3(o64.g), threads3(), 0, sc, o64, op_density(ctx), ctx->coef64);
+    ECS_LAUNCHED(ctx);
+  }
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[5], sc));
   ecs_launch_pdl(k_density_in<T>, blocks_for(ctx, L0.n), kB, 0, s0, L0.n, op_density(ctx), L0.dens);
   ECS_LAUNCHED(ctx);
   ECS_CUDA(ctx, cudaEventRecord(ctx->sev[0], s0));
@@ -1506,6 +1532,7 @@ int mg_setup(EcsCtx *ctx) {
   if ((rc = zline_factor<T>(ctx, L0, s0))) return rc;
   ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[2], 0));
   ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[3], 0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[5], 0));
   return ECS_OK;
 }
 
@@ -1805,18 +1832,19 @@ __global__ void k_axpy64_dev(size_t n, const double *__restrict__ scale, const T
 }
 
 // Mixed-precision residual: r64 = b64 - A64(n64) x64.
-__global__ void k_residual64(OpK o, const double *__restrict__ n, const double *__restrict__ x,
+// r = b - A x in FP64 from the stored coefficients (the same products and
+// sum as computing them in place).
+__global__ void k_residual64(OpK o, const double *__restrict__ coef, const double *__restrict__ x,
                              const double *__restrict__ b, double *__restrict__ r) {
   ECS_PDL_ENTRY();
   int i, j, k;
   if (!at3(o.g.nx, o.g.ny, i, j, k)) return;
   const Nbr q = nbr_of(o.g, i, j, k);
-  double v[11], xe[11];
-  row11_n(n, o, q, v);
+  double xe[11];
   row_x(x, q, xe);
   double s = 0.0;
 #pragma unroll
-  for (int e = 0; e < 11; e++) s += v[e] * xe[e];
+  for (int e = 0; e < 11; e++) s += __ldg(&coef[(size_t)e * o.g.n + q.c]) * xe[e];
   r[q.c] = b[q.c] - s;
 }
 
@@ -1888,7 +1916,7 @@ template <typename T>
 int refine_check(EcsCtx *ctx, double rtol, int max_it, cudaGraphConditionalHandle h) {
   const EcsParams &p = ctx->p;
   const OpK o64 = make_op(p, p.Nx, p.Ny, p.Nz, p.dx, p.dy, p.dz);
-  ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
+  ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, (const double *)ctx->coef64, ctx->phi, ctx->rhs, ctx->r64);
   ECS_LAUNCHED(ctx);
   int rc = norm64_dev(ctx, ctx->r64, ctx->dots);
   if (rc) return rc;
@@ -1992,6 +2020,27 @@ int ensure_capture_streams(EcsCtx *ctx) {
   return ECS_OK;
 }
 
+// The right-hand side (FP64-bound) on sst[3] beside the operator set-up
+// (latency-bound) on the context's stream and sst[0..2]; both need only the
+// moments, and the context's stream waits for both.
+template <typename T>
+int rhs_beside_setup(EcsCtx *ctx) {
+  int rc = ensure_setup_streams(ctx);
+  if (rc) return rc;
+  if (identity_lhs(ctx)) return ecs_grid_rhs(ctx);
+  cudaStream_t s0 = ctx->stream;
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[6], s0));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->sst[3], ctx->sev[6], 0));
+  ctx->stream = ctx->sst[3];
+  rc = ecs_grid_rhs(ctx);
+  ctx->stream = s0;
+  if (rc) return rc;
+  ECS_CUDA(ctx, cudaEventRecord(ctx->sev[7], ctx->sst[3]));
+  if ((rc = mg_setup<T>(ctx))) return rc;
+  ECS_CUDA(ctx, cudaStreamWaitEvent(s0, ctx->sev[7], 0));
+  return ECS_OK;
+}
+
 // One solve as one graph (see capture_solve), built for (rtol, max_it, warm).
 template <typename T>
 int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm, int setup) {
@@ -2017,8 +2066,7 @@ int build_solve_graph(EcsCtx *ctx, double rtol, int max_it, int warm, int setup)
   rc = ECS_OK;
   sg.k_pre = 0;
   if (setup) {
-    rc = ecs_grid_rhs(ctx);
-    if (!rc && !identity_lhs(ctx)) rc = mg_setup<T>(ctx);
+    rc = rhs_beside_setup<T>(ctx);
     sg.k_pre = ctx->launches - launches0;
   }
   if (!rc) rc = capture_solve<T>(ctx, rtol, max_it, warm);
@@ -2120,8 +2168,7 @@ int build_request_graph(EcsCtx *ctx, const double fs[3], double rtol, int max_it
       break;
     }
     ctx->launches++;
-    if ((rc = ecs_grid_rhs(ctx))) break;
-    if (!identity_lhs(ctx) && (rc = mg_setup<T>(ctx))) break;
+    if ((rc = rhs_beside_setup<T>(ctx))) break;
     rg.k_pre = ctx->launches - launches0;
     if ((rc = capture_solve<T>(ctx, rtol, max_it, 0))) break;
     if ((ce = cudaMemcpyAsync(rg.h_out, ctx->phi, bytes, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess) {
@@ -2184,6 +2231,7 @@ int ecs_solver_alloc(EcsCtx *ctx) {
     ECS_CUDA(ctx, cudaMallocHost(&ctx->kctl_host, sizeof(KrylovDev)));
     memset(ctx->kdev_host, 0, sizeof(KrylovDev));
     memset(ctx->kctl_host, 0, sizeof(KrylovDev));
+    if (!identity_lhs(ctx)) ECS_CUDA(ctx, cudaMalloc((void **)&ctx->coef64, 11 * n * sizeof(double)));
     ECS_CUDA(ctx, cudaMalloc(&ctx->rdev, sizeof(RefineDev)));
     ECS_CUDA(ctx, cudaMemset(ctx->rdev, 0, sizeof(RefineDev)));
     ECS_CUDA(ctx, cudaMallocHost(&ctx->rdev_host, sizeof(RefineDev)));
@@ -2270,7 +2318,7 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->r64, ctx->rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         zero_guess = false;
       } else {
-        ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, op_density(ctx), ctx->phi, ctx->rhs, ctx->r64);
+        ecs_launch_pdl(k_residual64, blocks3(o64.g), threads3(), 0, ctx->stream, o64, (const double *)ctx->coef64, ctx->phi, ctx->rhs, ctx->r64);
         ECS_LAUNCHED(ctx);
         if ((rc = norm64_dev(ctx, ctx->r64, ctx->dots))) return rc;
         ECS_CUDA(ctx, cudaMemcpyAsync(ctx->h_dots, ctx->dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2348,8 +2396,8 @@ int ecs_solver_free(EcsCtx *ctx) {
     if (e) cudaEventDestroy(e);
   free_mg(ctx->mg64);
   free_mg(ctx->mg32);
-  void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->dots, ctx->red, ctx->kdev,
-                  ctx->rdev};
+  void *ptrs[] = {ctx->kv64, ctx->kz64, ctx->kv32, ctx->kz32, ctx->w64, ctx->r64, ctx->coef64, ctx->dots, ctx->red,
+                  ctx->kdev, ctx->rdev};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_dots) cudaFreeHost(ctx->h_dots);
