@@ -57,10 +57,10 @@ SORT_EVERY = 2          # cell sort cadence of the mixed path
 # the ions from the old order, so some of its tile ranges wait for upload
 # chunks far ahead (ions that crossed a periodic face) and it runs a little
 # longer than the others.  The host-buffer run sorts every 4 steps (the
-# results do not depend on the cadence) and is timed over two cycles after
-# warm-up steps.
+# results do not depend on the cadence) and is timed over three cycles after
+# warm-up steps; each cycle's rate is reported beside the whole run's.
 E2E_SORT_EVERY = 4
-E2E_CYCLES = 2
+E2E_CYCLES = 3
 # Algorithmic bytes per particle-step (the roofline's numerator): the ion's
 # state read and written once, mixed: int32 cell + 3 FP32 offsets + 3 FP32
 # velocities = 28 B each way; FP64: 6 FP64 each way.  The grid fields and the
@@ -670,13 +670,19 @@ def run_ours(args, world, rank, local):
             ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)
         barrier(world)
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        marks = [t0]
+        for q in range(e2e_steps):
             ctx.step_host(hpos, hvel, dt, rtol, 400, hmom, hphi)
+            if (q + 1) % E2E_SORT_EVERY == 0:
+                marks.append(time.perf_counter())
         e2e_el = max_over_ranks(time.perf_counter() - t0, world)
         e2e = {"value": N * e2e_steps * world / e2e_el, "unit": "particle-steps/s",
                "h2d_bytes_per_step": 48 * N, "d2h_bytes_per_step": 48 * N + 40 * p.Nx * p.Ny * p.Nz,
                "steps": e2e_steps, "api": "ecs_step_host", "sort_every": E2E_SORT_EVERY,
-               "link_gbs": (96 * N + 40 * p.Nx * p.Ny * p.Nz) * e2e_steps / e2e_el / 1e9}
+               "link_gbs": (96 * N + 40 * p.Nx * p.Ny * p.Nz) * e2e_steps / e2e_el / 1e9,
+               # each sort cycle on its own (host wall clock, this rank): the
+               # value above is the whole run
+               "cycle_values": [N * E2E_SORT_EVERY / (b - a) for a, b in zip(marks, marks[1:])]}
         del hpos, hvel
     ctx.close()
 

@@ -227,6 +227,8 @@ int ecs_ctx_destroy(EcsCtx *ctx) {
   if (ctx->hstat) cudaFreeHost(ctx->hstat);
   for (int q = 0; q < 4; q++)
     if (ctx->ev[q]) cudaEventDestroy(ctx->ev[q]);
+  if (ctx->ev_stat) cudaEventDestroy(ctx->ev_stat);
+  if (ctx->ev_mom) cudaEventDestroy(ctx->ev_mom);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return ECS_OK;
@@ -327,6 +329,25 @@ static int moments_to_host(EcsCtx *ctx, double *m) {
   return ECS_OK;
 }
 
+// The same without waiting, for ecs_step_host after its pipelined pass: the
+// conversion into the free upload staging buffer on the context's stream,
+// the copy behind the ions' download (xs[0], waited for with them).  *sent
+// stays false when the staging buffer is too small (then use the above).
+static int moments_to_host_async(EcsCtx *ctx, double *m, bool *sent) {
+  *sent = false;
+  const size_t bytes = ctx->ncell * 4 * sizeof(double);
+  if (!ctx->stage[0] || !ctx->xs[0] || bytes > (size_t)ecs_stage_stride(ctx->stage_n) * 2 * sizeof(double))
+    return ECS_OK;
+  if (!ctx->ev_mom) ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_mom, cudaEventDisableTiming));
+  k_moments_aos<<<blocks(ctx, ctx->ncell), 256, 0, ctx->stream>>>(ctx->ncell, ctx->mom, ctx->stage[0]);
+  ECS_LAUNCHED(ctx);
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_mom, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamWaitEvent(ctx->xs[0], ctx->ev_mom, 0));
+  ECS_CUDA(ctx, cudaMemcpyAsync(m, ctx->stage[0], bytes, cudaMemcpyDeviceToHost, ctx->xs[0]));
+  *sent = true;
+  return ECS_OK;
+}
+
 int ecs_moments_download(EcsCtx *ctx, double *m) {
   if (!ctx || !m) return ECS_ERR_INVALID;
   return moments_to_host(ctx, m);
@@ -413,25 +434,40 @@ int ecs_lhs_apply_host(EcsCtx *ctx, const double *x, double *y) {
 }
 
 // Particle phase of a step (src/pic.c:244-252): push, collide, move + BC,
-// deposit, the cell sort when due, and the FP64 moments.
-static int step_particles(EcsCtx *ctx, double dt, EcsDevStatus *coll, int *sorted) {
-  int rc = ensure_eext(ctx, ctx->eext_ready);
+// deposit, the cell sort when due, and the FP64 moments; the copy of the
+// pass's counters to the host is queued behind them (read by status_hook).
+static int step_particles(EcsCtx *ctx, double dt, int *sorted) {
+  int rc = ecs_part_settle(ctx);
   if (rc) return rc;
+  if ((rc = ensure_eext(ctx, ctx->eext_ready))) return rc;
   *sorted = 0;
   ctx->ev_particle = ctx->ev_sort = false;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   if ((rc = ecs_part_fused(ctx, dt, 1, sorted))) return rc;
-  *coll = *ctx->hstat;
-  if (ctx->p.mn <= 0.0) memset(coll, 0, sizeof *coll);
   if ((rc = ecs_grid_moments(ctx))) return rc;
-  return read_status(ctx);
+  return ecs_part_status_async(ctx);
+}
+
+// Runs while the field phase is on the device: the particle pass's counters
+// (collision-rate update, refusals, range and finiteness flags).
+struct StepStatus {
+  EcsDevStatus coll;
+  double *moments_out;  // ecs_step_host: moments to copy to the host meanwhile
+};
+static int status_hook(EcsCtx *ctx, void *arg) {
+  StepStatus *ss = (StepStatus *)arg;
+  const int rc = ecs_part_status_finish(ctx);
+  ss->coll = *ctx->hstat;
+  if (ctx->p.mn <= 0.0) memset(&ss->coll, 0, sizeof ss->coll);
+  return rc;
 }
 
 // Field phase (src/pic.c:253-258): RHS, operator, potential solve.
-// The RHS, the operator set-up and the solve are one graph launch.
-static int step_field(EcsCtx *ctx, double rtol, int max_it, EcsSolveStats *st) {
+// The RHS, the operator set-up and the solve are one graph launch; the
+// particle status is read while it runs.
+static int step_field(EcsCtx *ctx, double rtol, int max_it, EcsSolveStats *st, StepStatus *ss) {
   memset(st, 0, sizeof *st);
-  int rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, st, 1);
+  int rc = ecs_solver_run(ctx, rtol, max_it, ctx->warm_start, st, 1, status_hook, ss);
   ctx->eext_ready = false;
   return rc;
 }
@@ -452,13 +488,13 @@ static void step_stats(EcsCtx *ctx, const EcsDevStatus &coll, int sorted, const 
 
 int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stats) {
   if (!ctx || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
-  EcsDevStatus coll;
   int sorted = 0;
-  int rc = step_particles(ctx, dt, &coll, &sorted);
+  int rc = step_particles(ctx, dt, &sorted);
   if (rc) return rc;
   EcsSolveStats st;
-  rc = step_field(ctx, rtol, max_it, &st);
-  step_stats(ctx, coll, sorted, st, stats);
+  StepStatus ss = {};
+  rc = step_field(ctx, rtol, max_it, &st, &ss);
+  step_stats(ctx, ss.coll, sorted, st, stats);
   return rc;
 }
 
@@ -470,31 +506,33 @@ int ecs_step(EcsCtx *ctx, double dt, double rtol, int max_it, EcsStepStats *stat
 int ecs_step_host(EcsCtx *ctx, double *pos, double *vel, int64_t np, double dt, double rtol, int max_it,
                   double *moments_out, double *phi_out, EcsStepStats *stats) {
   if (!ctx || !pos || !vel || !(rtol > 0) || max_it < 1) return ECS_ERR_INVALID;
-  EcsDevStatus coll;
   int sorted = 0;
-  int rc = ensure_eext(ctx, ctx->eext_ready);
+  int rc = ecs_part_settle(ctx);
   if (rc) return rc;
+  if ((rc = ensure_eext(ctx, ctx->eext_ready))) return rc;
   ctx->ev_particle = ctx->ev_sort = false;
   ECS_CUDA(ctx, cudaMemsetAsync(ctx->dstat, 0, sizeof(EcsDevStatus), ctx->stream));
   rc = ecs_part_host_pass(ctx, pos, vel, np, dt, &sorted);
+  bool moments_sent = false;
   if (rc == ECS_ERR_STATE) {  // no hand-off from a previous call: upload (and sort) first
     if ((rc = ecs_part_upload(ctx, pos, vel, np))) return rc;
-    if ((rc = step_particles(ctx, dt, &coll, &sorted))) return rc;
+    if ((rc = step_particles(ctx, dt, &sorted))) return rc;
     if ((rc = ecs_part_download_async(ctx, pos, vel))) return rc;
   } else {
     if (rc) return rc;
-    coll = *ctx->hstat;
-    if (ctx->p.mn <= 0.0) memset(&coll, 0, sizeof coll);
     if ((rc = ecs_grid_moments(ctx))) return rc;
-    if ((rc = read_status(ctx))) return rc;
+    if ((rc = ecs_part_status_async(ctx))) return rc;
+    // the moments go out behind the ions' download while the solve runs
+    if (moments_out && (rc = moments_to_host_async(ctx, moments_out, &moments_sent))) return rc;
   }
   EcsSolveStats st;
-  const int rc_field = step_field(ctx, rtol, max_it, &st);
+  StepStatus ss = {};
+  const int rc_field = step_field(ctx, rtol, max_it, &st, &ss);
   if ((rc = ecs_part_xfer_wait(ctx))) return rc;
   ctx->host_gen = ctx->pgen;  // the host arrays now hold the device's ions, in the buffer's next order
   if (rc_field) return rc_field;
-  step_stats(ctx, coll, sorted, st, stats);
-  if (moments_out && (rc = moments_to_host(ctx, moments_out))) return rc;
+  step_stats(ctx, ss.coll, sorted, st, stats);
+  if (moments_out && !moments_sent && (rc = moments_to_host(ctx, moments_out))) return rc;
   if (phi_out) {
     ECS_CUDA(ctx, cudaMemcpyAsync(phi_out, ctx->phi, ctx->ncell * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -188,6 +188,14 @@ struct EcsCtx {
   double attempt_rate = -1.0;       // attempts per ion per call (< 0: not yet estimated)
   EcsDevStatus *dstat = nullptr;
   EcsDevStatus *hstat = nullptr;    // pinned
+  // A step's counters are copied to hstat behind its particle pass (event
+  // ev_stat) and read while the field phase runs; the collision-rate update
+  // of a fused pass waits for that read (coll_pending, with the pass's dt).
+  cudaEvent_t ev_stat = nullptr;
+  bool stat_queued = false;         // the copy behind ev_stat is the current pass's
+  bool coll_pending = false;
+  double coll_dt = 0.0;
+  cudaEvent_t ev_mom = nullptr;     // moments converted for the host (ecs_step_host)
 
   int shift_n = 48, shift_f = 48;   // deposit fixed-point shifts (density, flux)
   int64_t launches = 0;
@@ -330,7 +338,11 @@ int ecs_solver_alloc(EcsCtx *ctx);       // reductions, Krylov bases, control bl
 int ecs_solver_setup(EcsCtx *ctx);       // multigrid hierarchy from the density
 // setup = 1: compute the RHS and set up the operator first (the step's field
 // phase), in the same graph launch as the solve.
-int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup = 0);
+// `between` (optional) runs on the host once the solve is enqueued and
+// before the host waits for it; its status is returned if nonzero.
+typedef int (*EcsHostHook)(EcsCtx *ctx, void *arg);
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup = 0,
+                   EcsHostHook between = nullptr, void *arg = nullptr);
 int ecs_operator_apply64(EcsCtx *ctx, const double *x, double *y);
 int ecs_solver_free(EcsCtx *ctx);
 // Stand-alone solve request: launch (asynchronous, on ctx->stream) and, once
@@ -358,6 +370,14 @@ int ecs_part_collide(EcsCtx *ctx, double dt);
 int ecs_part_move(EcsCtx *ctx, double dt);
 int ecs_part_collect(EcsCtx *ctx);
 int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted);
+// Copy of the step's device counters to the host, behind the work enqueued
+// so far; ecs_part_status_finish waits for it, applies the pending
+// collision-rate update and returns the first error the counters show.
+int ecs_part_status_async(EcsCtx *ctx);
+int ecs_part_status_finish(EcsCtx *ctx);
+// Applies a pending collision-rate update (reading the counters first if
+// their copy was not queued); called before the counters are cleared.
+int ecs_part_settle(EcsCtx *ctx);
 int ecs_part_sort(EcsCtx *ctx);
 int ecs_part_estimate_rate(EcsCtx *ctx, double dt);
 extern "C" int ecs_fix_shifts(const EcsParams *p, int precision, int32_t *shift_density, int32_t *shift_flux);

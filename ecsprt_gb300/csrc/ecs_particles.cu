@@ -1905,6 +1905,8 @@ int ecs_part_ids(EcsCtx *ctx, int32_t *ids) {
 // separate push and collide passes (the reference's UpdateVelocities) and
 // the same step as one fused pass start from the same rate.
 static int pass_params(EcsCtx *ctx, double dt, int &mode, PartK &k) {
+  int rc0 = ecs_part_settle(ctx);  // a rate update still pending from a fused pass
+  if (rc0) return rc0;
   k = make_k(ctx, dt);
   if ((mode & 3) && k.collide && ctx->attempt_rate < 0) {
     int rc = ecs_part_estimate_rate(ctx, dt);
@@ -1973,10 +1975,8 @@ static int launch_particles(EcsCtx *ctx, double dt, int mode, bool count_for_sor
   return ECS_OK;
 }
 
-// After a collision pass: read the counters, update the next pass's rate.
-static int finish_collisions(EcsCtx *ctx, double dt) {
-  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
-  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+// After a collision pass, from its counters in hstat: the next pass's rate.
+static int collisions_update(EcsCtx *ctx, double dt) {
   const EcsDevStatus &s = *ctx->hstat;
   // Attempt rate of the next pass: the expected number of accepted
   // collisions is rate * sum_i P_accept(v_i), so scale the rate by
@@ -1993,6 +1993,53 @@ static int finish_collisions(EcsCtx *ctx, double dt) {
   }
   if (s.refused >= 10) return ecs_fail(ctx, ECS_ERR_COLLISION, "%llu collisions refused (final speed > 10 viT)", s.refused);
   return ECS_OK;
+}
+// After a collision pass: read the counters, update the next pass's rate.
+static int finish_collisions(EcsCtx *ctx, double dt) {
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return collisions_update(ctx, dt);
+}
+
+int ecs_part_status_async(EcsCtx *ctx) {
+  if (!ctx->ev_stat) ECS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_stat, cudaEventDisableTiming));
+  ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  ECS_CUDA(ctx, cudaEventRecord(ctx->ev_stat, ctx->stream));
+  ctx->stat_queued = true;
+  return ECS_OK;
+}
+
+// The counters in hstat: wait for their queued copy, or copy them now.
+static int status_to_host(EcsCtx *ctx) {
+  if (ctx->stat_queued) {
+    ECS_CUDA(ctx, cudaEventSynchronize(ctx->ev_stat));
+  } else {
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(EcsDevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+    ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->stat_queued = false;
+  return ECS_OK;
+}
+
+int ecs_part_settle(EcsCtx *ctx) {
+  if (!ctx->coll_pending) return ECS_OK;
+  int rc = status_to_host(ctx);
+  if (rc) return rc;
+  ctx->coll_pending = false;
+  return collisions_update(ctx, ctx->coll_dt);
+}
+
+int ecs_part_status_finish(EcsCtx *ctx) {
+  int rc = status_to_host(ctx);
+  if (rc) return rc;
+  if (ctx->coll_pending) {
+    ctx->coll_pending = false;
+    rc = collisions_update(ctx, ctx->coll_dt);
+  }
+  const unsigned int f = ctx->hstat->flags;
+  if (f & ECS_FLAG_NONFINITE) return ecs_fail(ctx, ECS_ERR_NONFINITE, "non-finite particle velocity");
+  if (f & ECS_FLAG_RANGE) return ecs_fail(ctx, ECS_ERR_RANGE, "particle outside the domain or deposit range exceeded");
+  return rc;
 }
 
 int ecs_part_estimate_rate(EcsCtx *ctx, double dt) {
@@ -2093,8 +2140,9 @@ int ecs_part_fused(EcsCtx *ctx, double dt, int do_collide, int *sorted) {
   if (rc) return rc;
   if ((rc = sort_after_pass(ctx, counted))) return rc;
   if (sorted) *sorted = counted ? 1 : 0;
-  if (collide) {
-    rc = finish_collisions(ctx, dt);
+  if (collide) {  // the rate update waits for the counters (ecs_part_status_finish)
+    ctx->coll_pending = true;
+    ctx->coll_dt = dt;
     ctx->step_index++;
   }
   return rc;
@@ -2329,8 +2377,9 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   }
   if ((rc = sort_after_pass(ctx, counted))) return rc;
   if (sorted) *sorted = counted ? 1 : 0;
-  if (mode & 2) {
-    rc = finish_collisions(ctx, dt);
+  if (mode & 2) {  // the rate update waits for the counters (ecs_part_status_finish)
+    ctx->coll_pending = true;
+    ctx->coll_dt = dt;
     ctx->step_index++;
   }
   return rc;

@@ -2260,8 +2260,14 @@ int ecs_solver_setup(EcsCtx *ctx) {
 
 // Iterative refinement around FGMRES cycles.  Per refinement the host waits
 // once, for the FP64 residual norm and the finished cycle's control block.
-int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup) {
+int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats *st, int setup,
+                   EcsHostHook between, void *arg) {
   const bool graphs = ctx->use_graphs || identity_lhs(ctx);
+  if (between && !graphs) {  // the host-driven loop waits on the device from its start
+    const int rc_h = between(ctx, arg);
+    if (rc_h) return rc_h;
+    between = nullptr;
+  }
   if (setup && !graphs) {  // the host-driven loop: RHS and set-up launched one by one
     int rc0 = ecs_grid_rhs(ctx);
     if (!rc0) rc0 = ecs_solver_setup(ctx);
@@ -2285,7 +2291,9 @@ int ecs_solver_run(EcsCtx *ctx, double rtol, int max_it, int warm, EcsSolveStats
     RefineDev *hr = (RefineDev *)ctx->rdev_host;
     ECS_CUDA(ctx, cudaMemcpyAsync(hr, ctx->rdev, sizeof(RefineDev), cudaMemcpyDeviceToHost, ctx->stream));
     ECS_CUDA(ctx, cudaEventRecord(ctx->ev_solve[1], ctx->stream));
+    const int rc_h = between ? between(ctx, arg) : ECS_OK;
     ECS_CUDA(ctx, cudaEventSynchronize(ctx->ev_solve[1]));
+    if (rc_h) return rc_h;
     const SolverGraph &sg = ctx->sgraph;
     ctx->launches += sg.k_pre + sg.k_head + hr->sweeps * sg.k_sweep + (int64_t)hr->its * sg.k_step;
     float ms = 0.f;
