@@ -452,7 +452,6 @@ static int step_particles(EcsCtx *ctx, double dt, int *sorted) {
 // (collision-rate update, refusals, range and finiteness flags).
 struct StepStatus {
   EcsDevStatus coll;
-  double *moments_out;  // ecs_step_host: moments to copy to the host meanwhile
 };
 static int status_hook(EcsCtx *ctx, void *arg) {
   StepStatus *ss = (StepStatus *)arg;
