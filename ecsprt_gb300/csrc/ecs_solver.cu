@@ -887,10 +887,13 @@ __global__ void __launch_bounds__(kInvThreads) k_coarse_inverse_reg(OpK o, const
 }
 
 // ---- vectors ----------------------------------------------------------------------
-// Sums of one thread use compensated (Kahan) summation in T; a warp adds its
-// 32 lanes in T (fixed tree); from there on (warps of a block, blocks) the
-// sums are FP64 in a fixed order.  FP32 sums thus need no FP64 instruction
-// per element, which matters on sm_103 where FP64 issues on a narrow pipe.
+// Sums of one thread use compensated (Kahan) summation in FP32; a warp adds
+// its 32 lanes in T (fixed tree); from there on (warps of a block, blocks)
+// the sums are FP64 in a fixed order.  FP32 sums thus need no FP64
+// instruction per element, which matters on sm_103 where FP64 issues on a
+// narrow pipe.  An FP64 thread sum (a dozen terms or so) is plain, one
+// multiply-add a term for the norms: compensation would add four FP64
+// operations a term for digits beyond what a norm or a mean needs.
 template <typename T>
 struct KSum {
   T s, c;
@@ -902,6 +905,13 @@ struct KSum {
     s = t;
   }
   __device__ __forceinline__ T value() const { return s - c; }
+};
+template <>
+struct KSum<double> {
+  double s;
+  __device__ __forceinline__ KSum() : s(0.0) {}
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
 };
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
