@@ -223,8 +223,11 @@ struct EcsCtx {
   uint64_t pgen = 0;                // bumped by every change of the device ions
   uint64_t host_gen = ~0ull;        // pgen when ecs_step_host last returned the ions to the host
   bool bounds_valid = false;        // tile_bounds holds the current sort's tile offsets
-  std::vector<int32_t> tile_bounds; // first ion of every tile, and np (ntiles + 1)
-  std::vector<int32_t> tile_srcmax; // largest source position a tile's ions are gathered from (pending sort)
+  // Page-locked host tables, filled through a device buffer of the same
+  // layout (both allocated once, on first use):
+  int32_t *tile_bounds = nullptr;   // first ion of every tile, and np (ntiles + 1)
+  int32_t *tile_srcmax = nullptr;   // largest source position a tile's ions are gathered from (pending sort)
+  int32_t *tile_tables_dev = nullptr;
 };
 
 // ---- error helpers -------------------------------------------------------

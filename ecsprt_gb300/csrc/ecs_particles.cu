@@ -1696,6 +1696,9 @@ void ecs_part_xfer_free(EcsCtx *ctx) {
   }
   for (cudaEvent_t e : ctx->xev_upc) cudaEventDestroy(e);
   ctx->xev_upc.clear();
+  if (ctx->tile_tables_dev) cudaFree(ctx->tile_tables_dev);
+  if (ctx->tile_bounds) cudaFreeHost(ctx->tile_bounds);
+  ctx->tile_tables_dev = ctx->tile_bounds = ctx->tile_srcmax = nullptr;
 }
 
 // Host AoS FP64 -> device: copies on xs[1], conversions on ctx->stream.
@@ -2220,28 +2223,30 @@ static int host_span_out(EcsCtx *ctx, const PartK &k, double *pos, double *vel, 
 
 // The current sort's first ion of every tile (tile_bounds) and, with a
 // gather pending, every tile's largest source position (tile_srcmax).
+// The tables and their device buffer are allocated once per context, so that
+// no step allocates or frees memory.
 static int host_tile_tables(EcsCtx *ctx, int ntiles, bool gather) {
   const bool want_b = !ctx->bounds_valid;
   if (!want_b && !gather) return ECS_OK;
-  const size_t nb = (size_t)ntiles + 1;
-  int32_t *d = nullptr;
-  ECS_CUDA(ctx, cudaMallocAsync((void **)&d, (nb + (size_t)ntiles) * sizeof(int32_t), ctx->stream));
+  const size_t nb = (size_t)ntiles + 1, words = nb + (size_t)ntiles;
+  if (!ctx->tile_tables_dev) {
+    ECS_CUDA(ctx, cudaMalloc((void **)&ctx->tile_tables_dev, words * sizeof(int32_t)));
+    ECS_CUDA(ctx, cudaMallocHost((void **)&ctx->tile_bounds, words * sizeof(int32_t)));
+    ctx->tile_srcmax = ctx->tile_bounds + nb;
+  }
+  int32_t *d = ctx->tile_tables_dev;
   if (want_b) {
-    ctx->tile_bounds.resize(nb);
     k_tile_bounds<<<ecs_div_up(nb, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, d);
     ECS_LAUNCHED(ctx);
-    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_bounds.data(), d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_bounds, d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   }
   if (gather) {
-    ctx->tile_srcmax.resize((size_t)ntiles);
     k_tile_srcmax<<<ecs_div_up((size_t)ntiles * 32, 256), 256, 0, ctx->stream>>>(ntiles, ctx->sort_offset, ctx->perm,
                                                                                   d + nb);
     ECS_LAUNCHED(ctx);
-    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_srcmax.data(), d + nb, (size_t)ntiles * sizeof(int32_t),
+    ECS_CUDA(ctx, cudaMemcpyAsync(ctx->tile_srcmax, d + nb, (size_t)ntiles * sizeof(int32_t),
                                   cudaMemcpyDeviceToHost, ctx->stream));
   }
-  ECS_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
   ECS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   ctx->bounds_valid = true;
   return ECS_OK;
@@ -2257,7 +2262,7 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
   const int ntiles = ctx->ntile[0] * ctx->ntile[1] * ctx->ntile[2];
   const bool gather = ctx->perm_pending;
   if ((rc = host_tile_tables(ctx, ntiles, gather))) return rc;
-  const int32_t *tb = ctx->tile_bounds.data();
+  const int32_t *tb = ctx->tile_bounds;
   if (tb[ntiles] != np) return ECS_ERR_STATE;
   for (int t = 0; t < ntiles; t++)
     if (tb[t + 1] - tb[t] > chunk) return ECS_ERR_STATE;  // a tile larger than a staging chunk
@@ -2321,7 +2326,7 @@ int ecs_part_host_pass(EcsCtx *ctx, double *pos, double *vel, int64_t np, double
     int64_t A, n, need;
   };
   std::vector<Range> rg;
-  const int32_t *smax = gather ? ctx->tile_srcmax.data() : nullptr;
+  const int32_t *smax = gather ? ctx->tile_srcmax : nullptr;
   for (int t0 = 0; t0 < ntiles;) {
     int t1 = t0 + 1;
     while (t1 < ntiles && (int64_t)tb[t1 + 1] - tb[t0] <= chunk) t1++;
