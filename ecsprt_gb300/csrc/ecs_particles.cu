@@ -1041,26 +1041,10 @@ __global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(Part
     const TileCtx tc{tx * ECS_TILE_X - 1, ty * ECS_TILE_Y - 1, tz * ECS_TILE_Z - 1};
     const int a = key_off[t * ECS_TILE_CELLS], b = key_off[(t + 1) * ECS_TILE_CELLS];
     if (a == b) continue;
-    if (mode & 1) {  // window nodes outside the extended grid are never read
-      const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
-      for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
-        const int gx = tc.wx0 + e % kWX, gy = tc.wy0 + (e / kWX) % kWY, gz = tc.wz0 + e / (kWX * kWY);
-        const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
-        ewin[(gz - tc.wz0) * kEXY + (gy - tc.wy0) * kEX + (gx - tc.wx0)] =
-            in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-    }
     for (int ca = a; ca < b; ca += kWindowMax) {
       const int L = min(kWindowMax, b - ca);
       const int seg = (L + 31) >> 5;               // lane segment
       const int sub = (seg + kTileThreads / 32 - 1) / (kTileThreads / 32);  // a warp's run inside each segment
-      if (mode & 8) {
-        for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0u;
-        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) dcnt[e] = 0;
-      }
-      if (count)
-        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
-      __syncthreads();
       // this thread's ions: m = 0 .. sub-1 at qi = lane * seg + warp * sub + m
       const int qi0 = lane * seg + warp * sub;
       const int mend = min(sub, min(seg - warp * sub, L - qi0));  // active iterations (may be <= 0)
@@ -1068,10 +1052,28 @@ __global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(Part
         const int64_t ip = (int64_t)ca + qi0 + m;
         return perm ? (int64_t)__ldg(perm + ip) : ip;
       };
+      // the chunk's first record (and the permutation entry of the second)
+      // are requested before the window set-up, which hides their latency
       int64_t sp_next = 0;
       float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb4 = na;  // the next record
       if (mend > 0) ld_record(src + 2 * src_pos(0), na, nb4);
       if (mend > 1) sp_next = src_pos(1);
+      if ((mode & 1) && ca == a) {  // window nodes outside the extended grid are never read
+        const int sx = k.Nx + 1, sxy = sx * (k.Ny + 1);
+        for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
+          const int gx = tc.wx0 + e % kWX, gy = tc.wy0 + (e / kWX) % kWY, gz = tc.wz0 + e / (kWX * kWY);
+          const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
+          ewin[(gz - tc.wz0) * kEXY + (gy - tc.wy0) * kEX + (gx - tc.wx0)] =
+              in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+      if (mode & 8) {
+        for (int e = threadIdx.x; e < 5 * kWPad; e += blockDim.x) (&win[0][0])[e] = 0u;
+        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) dcnt[e] = 0;
+      }
+      if (count)
+        for (int e = threadIdx.x; e < kWCells; e += blockDim.x) wcnt[e] = 0;
+      __syncthreads();
       for (int m = 0; m < mend; m++) {
         const float4 ra = na, rb = nb4;
         if (m + 1 < mend) {  // the next record, in flight while this one is worked on
