@@ -57,10 +57,13 @@ SORT_EVERY = 2          # cell sort cadence of the mixed path
 # the ions from the old order, so some of its tile ranges wait for upload
 # chunks far ahead (ions that crossed a periodic face) and it runs a little
 # longer than the others.  The host-buffer run sorts every 4 steps (the
-# results do not depend on the cadence) and is timed over three cycles after
-# two cycles of warm-up; each cycle's rate is reported beside the whole run's.
+# results do not depend on the cadence) and is timed over eight cycles (32
+# steps, about 1.4 s) after two cycles of warm-up, long enough that one
+# transient slow-down of the host link (about 100 ms, seen in some runs) does
+# not dominate the figure; each cycle's rate is reported beside the whole
+# run's.
 E2E_SORT_EVERY = 4
-E2E_CYCLES = 3
+E2E_CYCLES = 8
 # Algorithmic bytes per particle-step (the roofline's numerator): the ion's
 # state read and written once, mixed: int32 cell + 3 FP32 offsets + 3 FP32
 # velocities = 28 B each way; FP64: 6 FP64 each way.  The grid fields and the
