@@ -78,11 +78,11 @@ ALGO_BYTES_FP64 = 96
 RECORD_BYTES_MIXED = 68
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ion of a
 # k_tiles32 step launch, measured by ncu on the 64^3 x 64 ppc case of this
-# workload: 67.6 B for a pass that counts cells for the next sort, 71.9 B for
+# workload: 66.3 B for a pass that counts cells for the next sort, 70.4 B for
 # the pass after a sort (records read through the permutation); the steps
 # alternate, so a launch moves their mean x N (the traffic grows with the ion
 # count).
-TRAFFIC_BYTES_PER_ION = 69.8
+TRAFFIC_BYTES_PER_ION = 68.3
 
 
 def mg_levels(nx, ny, nz):
