@@ -809,10 +809,13 @@ __device__ __forceinline__ bool bound_axis(int bc, int N, int &c, float &o, floa
 
 constexpr int kWX = ECS_TILE_X + 3, kWY = ECS_TILE_Y + 3, kWZ = ECS_TILE_Z + 3;  // window nodes per axis
 constexpr int kWNodes = kWX * kWY * kWZ;
-// Padded strides of the field window (float4 a node).  A 16-byte shared load
-// is served 8 lanes at a time; with the ions sorted, those 8 lanes sit in a
-// 4 x 2 block of cells of one z plane, and lx + 12 ly takes 8 different
-// values mod 8 there, so the eight corner loads are free of bank conflicts.
+// Padded strides of the field window's x and y numerators (a float2 a node;
+// the z numerators are kept apart, at the deposit window's strides below).
+// An 8-byte shared load is served 16 lanes at a time; with the ions sorted,
+// those 16 lanes sit in the 4 x 4 cells of one z plane, and lx + 12 ly takes
+// 16 different values mod 16 there, so the eight corner loads are free of
+// bank conflicts.  Three words a corner instead of a padded float4 take a
+// quarter of the window's load traffic off the shared-memory pipe.
 constexpr int kEX = 12, kEXY = kEX * kWY;
 static_assert(kWX <= kEX, "field window stride");
 // Padded strides of the deposit window: the 32 cells of a tile (one lane
@@ -835,18 +838,22 @@ struct IonState {
   float ox, oy, oz, vx, vy, vz;
   int id;
 };
-// Push (src/velocities.c:281-371) of one ion.  Ew (nullptr: none) is a
+// Push (src/velocities.c:281-371) of one ion.  Exy, Ez (nullptr: none) are a
 // window of the difference numerators in shared memory, kWX x kWY x kWZ nodes
-// from node (wx0, wy0, wz0) at strides kEX, kEXY.
+// from node (wx0, wy0, wz0): x and y at strides kEX, kEXY, z at kSY, kSZ.
 __device__ __forceinline__ void ion_push(const PartK &k, const float4 *__restrict__ E, IonState &q,
-                                         const float4 *Ew = nullptr, int wx0 = 0, int wy0 = 0, int wz0 = 0) {
+                                         const float2 *Exy = nullptr, const float *Ez = nullptr, int wx0 = 0,
+                                         int wy0 = 0, int wz0 = 0) {
   float f[3];
   const int li = q.i - wx0, lj = q.j - wy0, lk = q.kk - wz0;
-  if (Ew && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
-    const int base = lk * kEXY + lj * kEX + li;
+  if (Exy && li >= 0 && li < kCX && lj >= 0 && lj < kCY && lk >= 0 && lk < kCZ) {
+    const int bxy = lk * kEXY + lj * kEX + li, bz = lk * kSZ + lj * kSY + li;
     float4 D[8];
 #pragma unroll
-    for (int b = 0; b < 8; b++) D[b] = Ew[corner_at(base, kEX, kEXY, b)];
+    for (int b = 0; b < 8; b++) {
+      const float2 xy = Exy[corner_at(bxy, kEX, kEXY, b)];
+      D[b] = make_float4(xy.x, xy.y, Ez[corner_at(bz, kSY, kSZ, b)], 0.f);
+    }
     interp8(D, q.ox, q.oy, q.oz, f);
   } else {
     gather32(E, k, q.i, q.j, q.kk, q.ox, q.oy, q.oz, f);
@@ -1031,7 +1038,8 @@ __global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(Part
   __shared__ unsigned win[5][kWPad];  // biased words [H, rint(r), flux x, y, z][node, padded strides]
   __shared__ int wcnt[kWCells];       // cells of the moved ions (next sort)
   __shared__ int dcnt[kWCells];       // window deposits a cell (bias removal)
-  __shared__ float4 ewin[kEXY * kWZ];  // difference numerators of the window's nodes (padded strides)
+  __shared__ float2 ewxy[kEXY * kWZ];  // x, y difference numerators of the window's nodes (padded strides)
+  __shared__ float ewz[kWPad];         // z numerators, at the deposit window's strides
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool collide = (mode & 2) && k.collide;
   unsigned int nacc = 0, nref = 0;  // collision counters of this thread, flushed at the end
@@ -1063,8 +1071,9 @@ __global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(Part
         for (int e = threadIdx.x; e < kWNodes; e += blockDim.x) {
           const int gx = tc.wx0 + e % kWX, gy = tc.wy0 + (e / kWX) % kWY, gz = tc.wz0 + e / (kWX * kWY);
           const bool in = gx >= 0 && gx <= k.Nx && gy >= 0 && gy <= k.Ny && gz >= 0 && gz <= k.Nz;
-          ewin[(gz - tc.wz0) * kEXY + (gy - tc.wy0) * kEX + (gx - tc.wx0)] =
-              in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 v = in ? __ldg(&E[gz * sxy + gy * sx + gx]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          ewxy[(gz - tc.wz0) * kEXY + (gy - tc.wy0) * kEX + (gx - tc.wx0)] = make_float2(v.x, v.y);
+          ewz[(gz - tc.wz0) * kSZ + (gy - tc.wy0) * kSY + (gx - tc.wx0)] = v.z;
         }
       }
       if (mode & 8) {
@@ -1082,7 +1091,7 @@ __global__ void __launch_bounds__(kTileThreads, kTileBlocksPerSM) k_tiles32(Part
         }
         IonState q = ion_state(Ion{__float_as_int(ra.x), ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, __float_as_int(rb.w)});
         const int64_t ip = (int64_t)ca + qi0 + m;
-        if (mode & 1) ion_push(k, E, q, ewin, tc.wx0, tc.wy0, tc.wz0);
+        if (mode & 1) ion_push(k, E, q, ewxy, ewz, tc.wx0, tc.wy0, tc.wz0);
         if (collide) collide_ion<float>(k, (uint32_t)q.id, kIdTag, (uint32_t)q.id, q.vx, q.vy, q.vz, nacc, nref);
         tile_finish(k, mode, st, q, ip, tc, win, dcnt, wcnt, acc, count, keys, dst);
       }
