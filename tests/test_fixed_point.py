@@ -6,13 +6,21 @@ exact rational arithmetic (no GPU):
   H = rint(v 2^(S-B)) and rint(v 2^S - H 2^B), and H 2^B + rint(r) equals
   rint(v 2^S) (round half to even);
 - flux (FixWord32::word, S = 22 - e_v): for |v 2^S| <= 2^22 one FP32
-  multiply-add of the bias gives bits(bias) + rint(v 2^S), and 500 such words
-  (the tile window's flush interval) sum without leaving int32.
+  multiply-add of the bias gives bits(bias) + rint(v 2^S);
+- the tile window (k_tiles32): an ion deposits there only when each velocity
+  component is within vmax / 8, so its flux words are at most 2^19 quanta,
+  and a chunk of kWindowMax ions (read from the kernel source) adds at most
+  one word an ion to a node: the biased uint32 sums, less count * bits(bias)
+  at the flush, are the exact int32 sums.
 """
 import random
+import re
 from fractions import Fraction as F
+from pathlib import Path
 
 import numpy as np
+
+KERNEL_SRC = Path(__file__).resolve().parents[1] / "ecsprt_gb300" / "csrc" / "ecs_particles.cu"
 
 BIAS = F(12582912)  # 1.5 * 2^23
 BIAS_BITS = 0x4B400000
@@ -78,7 +86,12 @@ def test_split_is_exact_rounding():
 
 
 S_FLUX = 22
-WINDOW_MAX = 500
+
+
+def window_max() -> int:
+    m = re.search(r"constexpr int kWindowMax = (\d+);", KERNEL_SRC.read_text())
+    assert m, "kWindowMax not found in the tile kernel"
+    return int(m.group(1))
 
 
 def word(v: F, S: int) -> int:
@@ -104,8 +117,34 @@ def test_flux_word_is_exact_rounding():
 
 
 def test_flux_window_bound():
-    # the largest flux contribution (|v w| at the velocity bound) is 2^22
-    # quanta; a window node sums at most WINDOW_MAX of them
+    # velocities in units of vmax = 2^e_v (S_FLUX = 22 for e_v = 0): the
+    # largest contribution of an ion anywhere is 2^22 quanta (the int64 path),
+    # of an ion within vmax / 8 (the window) 2^19; a window node sums at most
+    # one word an ion of a chunk of kWindowMax ions
+    wmax = window_max()
     assert word(F(1), S_FLUX) == 2 ** 22
-    assert word(F(-1), S_FLUX) == -(2 ** 22)
-    assert WINDOW_MAX * 2 ** 22 < 2 ** 31
+    assert word(F(1, 8), S_FLUX) == 2 ** 19
+    assert word(F(-1, 8), S_FLUX) == -(2 ** 19)
+    assert wmax * 2 ** 19 < 2 ** 31  # flux words and the density's high words
+    assert wmax * 2 ** 18 < 2 ** 31  # the density's low words
+
+
+def test_biased_window_sums_are_exact():
+    # each shared-memory word adds bits(bias) + value, wrapping in uint32; the
+    # flush subtracts count * bits(bias) and reads the word as int32
+    rng = np.random.default_rng(5)
+    wmax = window_max()
+    for trial in range(24):
+        n = wmax if trial < 8 else int(rng.integers(1, wmax + 1))
+        if trial % 4 == 0:
+            vals = np.full(n, 2 ** 19, dtype=np.int64)
+        elif trial % 4 == 1:
+            vals = np.full(n, -(2 ** 19), dtype=np.int64)
+        else:
+            vals = rng.integers(-(2 ** 19), 2 ** 19 + 1, size=n)
+        word_u32 = 0
+        for v in vals.tolist():
+            word_u32 = (word_u32 + BIAS_BITS + v) & 0xFFFFFFFF
+        unbiased = (word_u32 - n * BIAS_BITS) & 0xFFFFFFFF
+        as_int32 = unbiased - 2 ** 32 if unbiased >= 2 ** 31 else unbiased
+        assert as_int32 == int(vals.sum())
