@@ -147,6 +147,21 @@ def test_device_bytes_estimate(built):
     assert 6e9 < b_fp64 < 12e9
 
 
+@pytest.mark.parametrize("viT,vi0", [(1.0, 0.0), (1.0, 1.0), (1.0, 0.5), (0.3, 0.0), (2.0, 7.0), (1e-4, 0.0)])
+def test_fixed_point_shifts(built, viT, vi0):
+    """Deposit quanta: density 2^-48 (FP64) or 2^-38 (mixed); flux
+    2^-(S - e_v) with 2^e_v the velocity bound 16 (viT + vi0) rounded up to a
+    power of two (e_v clamped to [-8, 40]); a host-only helper of the ABI."""
+    import math
+    p = E.params_from_options(f"-Nx 8 -Ny 8 -Nz 8 -dx 1 -dy 1 -dz 1 -viT {viT} -vi0x {vi0}")
+    ev = min(max(math.ceil(math.log2(16.0 * (p.viT + p.vi0))), -8), 40)
+    for prec, S, Sf in ((E.ECS_PREC_FP64, 48, 48), (E.ECS_PREC_MIXED, 38, 22)):
+        sn, sf = ctypes.c_int32(), ctypes.c_int32()
+        assert _lib.gpu().ecs_fix_shifts(ctypes.byref(p), prec, ctypes.byref(sn), ctypes.byref(sf)) == 0
+        assert (sn.value, sf.value) == (S, Sf - ev)
+    assert _lib.gpu().ecs_fix_shifts(None, 0, ctypes.byref(sn), ctypes.byref(sf)) == _lib.ECS_ERR_INVALID
+
+
 @pytest.mark.parametrize("opts,expect", [
     ("", ("EcsGpuApply3DBC", "EcsGpuCollect3D", "EcsGpuPushBz3D", "EcsGpuFullLHS3D", "EcsGpuFullRHS3D")),
     ("-ndim 2 -mn 0", ("EcsGpuApply2DBC", "EcsGpuCollect2D", "EcsGpuPushBz2D", "EcsGpuFullLHS2D", "EcsGpuFullRHS2D")),
